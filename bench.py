@@ -1,0 +1,354 @@
+"""Benchmark of the Schur-block Liouvillian hot path on GB300.
+
+Workload (one step): the fused L x of the N=120 qubit-ensemble model (H = 0.3 Jz + 1.2 Jx,
+local decay 0.2, local dephasing 0.1, collective decay 0.05/N; PI dimension 302,621) applied
+to a batch of 128 resident state vectors (inputs larger than L2, no flush needed).  The
+headline is the FP32 apply (the mixed-precision path's inner operator) in population
+coordinates: value = algorithmic bytes (read x once, write y once) / device time.
+The FP64 apply, the end-to-end host-buffer call, the steady-state solve rate and the CPU
+baseline (C restatement of the reference's threaded apply) are reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "permutationalinvariantdynamics.jl_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "L·x HBM GB/s; solves/s + p50/p99 latency at 1e-8 residual, mixed vs FP64"
+N_QUBITS = 120
+BATCH = 128
+
+
+def model_c2(picuda, N=N_QUBITS):
+    s = picuda.spin_matrices(2)
+    return picuda.qubit_ensemble_model(N, hamiltonian=0.3 * s["jz"] + 1.2 * s["jx"], emission=0.2,
+                                       dephasing=0.1, collective_emission=0.05 / N)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name):
+    """DRAM bytes per launch recorded from an ncu capture summary in profiles/ (or None)."""
+    p = ROOT / "profiles" / "traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith(name + ":"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(value, world):
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def stencil_flops(picuda, model):
+    """Algorithmic real flops of one FP64 apply (fma counted as 2) from the stencil tables."""
+    table, _ = picuda.stencil_tables(model)
+    dims = model.basis.dims
+    cost = {(0, 0): 10, (0, 1): 10, (0, 2): 10, (1, 0): 4, (1, 1): 4, (1, 2): 8,
+            (2, 0): 4, (2, 1): 4, (2, 2): 8, (3, 0): 5, (3, 1): 14, (3, 2): 14}
+    total = 0
+    for s, src, kind, cls, dr, dc, *_ in table:
+        n, m = dims[s], dims[src]
+        rows = max(0, min(n, m - dr) - max(0, -dr))
+        cols = max(0, min(n, m - dc) - max(0, -dc))
+        total += cost[(int(kind), int(cls))] * rows * cols
+    return total
+
+
+def cpu_baseline_apply(model_oracle_plan, n, budget_s=10.0, max_vectors=2000):
+    """Times the oracle's C threaded apply (FP64, all host cores) on a bounded sample."""
+    from oracle import cpu_baseline
+    ta = cpu_baseline.ThreadedApply(model_oracle_plan)
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(1)
+    x = (rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex128)
+    y = np.empty_like(x)
+    ta(x, y, threads)  # warm
+    count = 0
+    t0 = time.perf_counter()
+    while count < max_vectors:
+        ta(x, y, threads)
+        count += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    gbs = 2 * 16 * n * count / dt / 1e9
+    return gbs, threads, count, dt
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the reference's CPU matrix-free apply (restated in C, threaded)."""
+    if rank != 0:
+        return 0
+    import picuda
+    from oracle import pi_oracle as O
+    from tests.models import to_oracle
+    model = model_c2(picuda)
+    plan = O.Plan(to_oracle(model))
+    from oracle import cpu_baseline
+    ta = cpu_baseline.ThreadedApply(plan)
+    n = len(plan)
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(1)
+    per_step = 8
+    xs = [(rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex128) for _ in range(per_step)]
+    y = np.empty_like(xs[0])
+    for _ in range(args.warmup):
+        for x in xs:
+            ta(x, y, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for x in xs:
+            ta(x, y, threads)
+    dt = time.perf_counter() - t0
+    bytes_step = 2 * 16 * n * per_step
+    value = bytes_step * args.steps / dt / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": "L x, N=120 qubit ensemble (dim 302,621), FP64",
+                   "vectors_per_step": per_step, "l2": "inputs > L2 not applicable (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} applies per step x {args.steps} steps, N=120, FP64"},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import torch
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import picuda
+    torch.cuda.set_device(local)
+    model = model_c2(picuda)
+    compiled = picuda.compile(model)
+    n = len(model.basis)
+    g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    X32 = torch.randn((BATCH, n), dtype=torch.complex64, device="cuda", generator=g)
+    Y32 = torch.empty_like(X32)
+    stream = torch.cuda.current_stream()
+
+    def step32():
+        picuda.apply_(Y32, compiled, X32, precision="fp32", coords="population")
+
+    for _ in range(args.warmup):
+        step32()
+    torch.cuda.synchronize()
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step32()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(ms, world)
+    bytes32 = 2 * 8 * n * BATCH
+    value = world * bytes32 / (ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    achieved = bytes32 / (ms * 1e-3) / 1e9
+
+    # FP64 apply on the same batch (plain path), timed the same way
+    X64 = X32.to(torch.complex128)
+    Y64 = torch.empty_like(X64)
+    for _ in range(3):
+        picuda.apply_(Y64, compiled, X64)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    k64 = max(3, args.steps // 5)
+    for _ in range(k64):
+        picuda.apply_(Y64, compiled, X64)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1) / k64
+    bytes64 = 2 * 16 * n * BATCH
+    flops64 = stencil_flops(picuda, model) * BATCH
+    del X64, Y64
+
+    # End to end through the host-buffer C-ABI call (pinned host memory, H2D + apply + D2H)
+    xh = X32.cpu().pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
+    lib = picuda.load_library()
+    import ctypes as C
+    for _ in range(2):
+        lib.pi_apply_host_f32(compiled.handle, C.c_void_p(yh.data_ptr()), C.c_void_p(xh.data_ptr()), BATCH, 1)
+    k_e2e = max(3, args.steps // 10)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        rc = lib.pi_apply_host_f32(compiled.handle, C.c_void_p(yh.data_ptr()), C.c_void_p(xh.data_ptr()), BATCH, 1)
+        if rc != 0:
+            raise RuntimeError(picuda._lib.last_error())
+    e2e_s = (time.perf_counter() - t0) / k_e2e
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e_value = world * bytes32 / e2e_s / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import pi_oracle as O
+        from tests.models import to_oracle
+        gbs, threads, count, dt = cpu_baseline_apply(O.Plan(to_oracle(model)), n)
+        cpu = {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
+               "sample": f"{count} FP64 applies of one N=120 state vector in {dt:.1f} s "
+                         "(C restatement of the reference's sector-owned threaded apply)"}
+
+    if rank == 0:
+        cl = clocks.summary()
+        line = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+            "config": {"workload": "fused L x, N=120 qubit ensemble (dim 302,621), batch of 128 resident "
+                                   "state vectors, FP32 population coordinates",
+                       "model": "H=0.3Jz+1.2Jx, local decay 0.2, local dephasing 0.1, collective decay 0.05/N",
+                       "batch": BATCH, "pi_dim": n, "l2": "inputs larger than L2 (310 MB per step read)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": profile_traffic("apply_f32_batch128_N120"),
+                         "algorithmic_bytes_per_launch": bytes32},
+            "fp64": {"value": bytes64 / (ms64 * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": ms64,
+                     "frac_hbm": bytes64 / (ms64 * 1e-3) / 1e9 / peak,
+                     "tflops": flops64 / (ms64 * 1e-3) / 1e12,
+                     "note": "plain FP64 apply on the same batch; FP64-ALU bound on GB300"},
+            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 8 * n * BATCH,
+                    "d2h_bytes_per_step": 8 * n * BATCH, "ms_per_step": e2e_s * 1e3,
+                    "call": "pi_apply_host_f32 (pinned host buffers)"},
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": cl,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

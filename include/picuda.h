@@ -1,0 +1,222 @@
+/*
+ * picuda.h -- C ABI of libpicuda.so, the GB300 (sm_103a) backend for the matrix-free
+ * Schur-block Liouvillian of PermutationalInvariantDynamics.jl and the Krylov solvers
+ * wrapped around it.
+ *
+ * The reference package has no native FFI; each entry point below names the Julia
+ * function whose work it replaces (paths are inside the reference project).  A Julia
+ * extension binds these with `ccall` behind `compile(model; backend=:cuda)`,
+ * `apply!`, `solve_dynamics(...; algorithm=ExpvAlgorithm(...))` and
+ * `stationary_state(...; algorithm=GMRESAlgorithm(...))`.
+ *
+ * Conventions
+ *  - Every function returns PI_OK (0) or a negative status; pi_last_error() gives the
+ *    message of the last failure on the calling thread.
+ *  - Complex vectors are interleaved (re, im) arrays in the reference's coordinate order:
+ *    sectors in descending partition order (basis.jl:27), column-major n x n blocks
+ *    (basis.jl:31, :90-93), GT patterns in ascending entry order (gtpatterns.jl:92-106).
+ *  - "dev" pointers are device pointers; "host" pointers are ordinary host memory.
+ *  - Sector offsets reported by this ABI are 0-based (the Julia basis stores 1-based).
+ */
+#ifndef PICUDA_H
+#define PICUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PI_OK 0
+#define PI_ERR_INVALID_ARGUMENT (-1)   /* maps to ArgumentError */
+#define PI_ERR_DIMENSION (-2)          /* maps to DimensionMismatch */
+#define PI_ERR_OUT_OF_MEMORY (-3)
+#define PI_ERR_NOT_CONVERGED (-4)      /* krylov.jl:873, krylov_extensions.jl:1559-1561 */
+#define PI_ERR_CUDA (-5)
+#define PI_ERR_UNSUPPORTED (-6)        /* model outside the CUDA backend (d != 2, p-body, ...) */
+#define PI_ERR_NO_DEVICE (-7)
+#define PI_ERR_BUSY (-8)               /* a handle used concurrently */
+
+/* Term kinds (terms.jl:118-149). Operators are 2x2 complex, column-major interleaved. */
+#define PI_TERM_HAMILTONIAN 0      /* CollectiveHamiltonian / LocalHamiltonian: rate/hbar */
+#define PI_TERM_LOCAL_JUMP 1       /* LocalJump: rate * sum_i D[L_i] */
+#define PI_TERM_COLLECTIVE_JUMP 2  /* CollectiveJump: rate * D[sum_i L_i] */
+
+/* Precision of an apply or solve. */
+#define PI_FP64 0  /* plain complex FP64 in reference coordinates */
+#define PI_FP32 1  /* complex FP32 applies; solver accuracy restored in FP64 */
+
+/* Coordinates of an FP32 vector. */
+#define PI_COORDS_REFERENCE 0   /* the reference's PI coefficients x */
+#define PI_COORDS_POPULATION 1  /* population coordinates z = sqrt(f^nu) x per sector */
+
+typedef struct pi_plan pi_plan;
+
+/* ---- library / device -------------------------------------------------------------- */
+
+/* Message of the last failing call on this thread (accelerators.jl:348-350 reasons). */
+int pi_last_error(char* buf, size_t len);
+
+/* Capability report; replaces _accelerator_extension_capability(::Val{:cuda})
+ * (accelerators.jl:41).  functional = 1 only after a device query succeeded. */
+typedef struct {
+  int functional;
+  int supports_matrixfree_pi;
+  int device_count;
+  int sm_count;
+  int cc_major, cc_minor;
+  size_t total_memory;
+  char device_name[128];
+} pi_capability_t;
+int pi_capability(pi_capability_t* out);
+
+/* ---- plan: compile(model; backend=:cuda) -------------------------------------------- */
+
+/* Builds and uploads the fused plan of a qubit model; replaces compile (liouvillian.jl:
+ * 4040-4098) -> LiouvillianPlan (:1844-1851) -> compile_term (:1290-1371) and the fusion
+ * (:1700-1738).  sector_ks lists the retained sectors (N-k, k) (NULL = all); ops holds
+ * nterms 2x2 column-major interleaved complex matrices (8 doubles each); hbar may be NULL
+ * (all ones).  The plan owns its device tables and a CUDA stream. */
+int pi_plan_create(int N, int d, int nsectors, const int* sector_ks, int nterms,
+                   const int* term_kind, const double* ops, const double* rates,
+                   const double* hbar, pi_plan** out);
+int pi_plan_destroy(pi_plan* plan);
+
+typedef struct {
+  int N;
+  int nsectors;
+  long long dim;     /* length(basis) = sum n^2 (basis.jl:35) */
+  int max_block;     /* largest block dimension */
+  int max_terms;     /* stencil terms of the busiest sector */
+  long long stencil_terms; /* total stencil terms over all sectors */
+  size_t device_bytes;     /* device memory owned by the plan tables */
+} pi_plan_info_t;
+int pi_plan_info(const pi_plan* plan, pi_plan_info_t* out);
+
+/* Bit-exact basis maps (basis.jl:20-34): k values, 0-based offsets and block sizes of
+ * every sector, each array of length nsectors. */
+int pi_plan_sectors(const pi_plan* plan, int* ks, long long* offsets, int* dims);
+/* GT patterns of one sector as entry triples {m, lam1, lam2} in in-block order
+ * (gtpatterns.jl:92-106); entries has room for 3*n ints. */
+int pi_plan_gt_patterns(const pi_plan* plan, int sector, int* entries);
+/* Trace functional: sqrt(f^nu) on every block diagonal (source_protocol.jl:15-34).
+ * idx/vals have room for sum_s n_s entries. */
+int pi_plan_trace_functional(const pi_plan* plan, long long* idx, double* vals);
+/* Per-sector sqrt(f^nu) (the population scaling of the FP32 coordinates). */
+int pi_plan_sector_scales(const pi_plan* plan, double* sqrt_f);
+
+/* ---- host-only inspection of the lowering (no device needed) ----------------------- */
+
+/* Exports the stencil tables that pi_plan_create would upload, for the same arguments.
+ * Two-call pattern: with term_table and coef NULL it only writes counts[0] = number of
+ * stencil terms and counts[1] = number of complex coefficients.  term_table receives 8
+ * ints per term {out_sector, src_sector, kind, cls, dr, dc, alpha_off, beta_off} (kind 0
+ * ADD (alpha[a]+beta[b]) x[a,b], 1 LEFT alpha[a] x[a+dr,b], 2 RIGHT beta[b] x[a,b+dc],
+ * 3 SAND alpha[a] beta[b] x[a+dr,b+dc]; offsets -1 when unused) and coef the interleaved
+ * complex FP64 coefficient pool in reference coordinates. */
+int pi_stencil_export(int N, int d, int nsectors, const int* sector_ks, int nterms,
+                      const int* term_kind, const double* ops, const double* rates,
+                      const double* hbar, long long* counts, int* term_table, double* coef);
+
+/* Dense block of the collective operator sum_i X_i in sector (N-k, k), column-major
+ * interleaved complex n x n (geometry.jl:1238-1256); op is 2x2 column-major interleaved. */
+int pi_collective_block(int N, int k, const double* op, double* out);
+
+/* f^(N-k,k) (partitions.jl:119-127) rounded to double, and its square root. */
+int pi_sector_multiplicity(int N, int k, double* f, double* sqrt_f);
+
+/* ---- apply!(y, compiled, x, t, p, work) (liouvillian.jl:4165-4171, :3205-3230) ------ */
+
+/* y = L x for ncols right-hand sides with leading dimension ld (elements), device
+ * buffers, complex FP64 reference coordinates.  stream may be NULL (the plan's stream).
+ * Aliasing of x and y is rejected (liouvillian.jl:3220-3221). */
+int pi_apply_f64(pi_plan* plan, double* y_dev, const double* x_dev, int ncols, long long ld,
+                 void* stream);
+/* Same action in complex FP32, in reference (x) or population (z = sqrt(f) x)
+ * coordinates (PI_COORDS_*).  Population coordinates keep every sector inside the FP32
+ * exponent range (stored PI coefficients of large-f sectors fall below 1e-38 near N=300). */
+int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld,
+                 int coords, void* stream);
+/* Convenience with host buffers: copies x in, applies, copies y out (pinned host memory
+ * gives full link bandwidth).  The FP32 variant takes PI_COORDS_* like pi_apply_f32. */
+int pi_apply_host_f64(pi_plan* plan, double* y_host, const double* x_host, int ncols);
+int pi_apply_host_f32(pi_plan* plan, float* y_host, const float* x_host, int ncols, int coords);
+
+/* ---- observables (highlevel.jl:665-677) --------------------------------------------- */
+
+/* Device dot(a, b) = sum conj(a) b, FP64, deterministic two-stage reduction. */
+int pi_dot_f64(pi_plan* plan, const double* a_dev, const double* b_dev, double* out_host2);
+
+/* ---- steady state: krylov_steady_state (krylov.jl:797-891) -------------------------- */
+
+typedef struct {
+  int krylovdim;          /* GMRES restart length m (default 30) */
+  int maxiter;            /* total Arnoldi steps (default 500) */
+  double atol, rtol;      /* defaults 1e-10, 1e-8 */
+  double operator_scale;  /* <= 0: estimate from 3 random probes (krylov.jl:156-169) */
+  int precision;          /* PI_FP64, or PI_FP32 = FP32 inner applies with FP64 refinement */
+  int use_initial;        /* 1: x_dev holds the initial state; 0: start from v = t/|t|^2 */
+  int max_refinements;    /* PI_FP32 only: outer FP64 refinement cycles (default 200) */
+} pi_gmres_opts_t;
+
+typedef struct {
+  int converged;
+  int iterations;           /* Arnoldi steps */
+  int restarts;
+  int refinements;          /* PI_FP32 outer cycles */
+  int operator_applications;
+  double residual;          /* ||L x|| */
+  double normalized_residual; /* ||L x|| / s */
+  double trace_error;       /* |t^H x - 1| */
+  double operator_scale;
+  double linear_residual;
+} pi_gmres_info_t;
+
+void pi_gmres_default_opts(pi_gmres_opts_t* opts);
+/* Solves for the trace-one stationary state into x_dev (complex FP64, device). */
+int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts,
+                    pi_gmres_info_t* info);
+
+/* ---- time evolution: krylov_expv! (krylov_extensions.jl:1452-1573) ------------------- */
+
+typedef struct {
+  int krylovdim;         /* default 30 */
+  double atol, rtol;     /* defaults 1e-10, 1e-8 */
+  double initial_step;   /* <= 0: nothing */
+  double minimum_step;   /* <= 0: nothing */
+  double maximum_step;   /* <= 0: nothing */
+  int max_steps;         /* default 10000 */
+  double safety;         /* default 0.9 */
+  int precision;         /* PI_FP64, or PI_FP32 = FP32 applies with FP64 orthogonalisation */
+} pi_expv_opts_t;
+
+typedef struct {
+  int converged;
+  double reached_time;
+  int accepted_steps, rejected_steps;
+  int operator_applications;
+  int arnoldi_factorizations;
+  int trial_evaluations;
+  double estimated_error;
+} pi_expv_info_t;
+
+void pi_expv_default_opts(pi_expv_opts_t* opts);
+/* x_dev <- exp(t L) x_dev (complex FP64, device). */
+int pi_expv(pi_plan* plan, double* x_dev, double t, const pi_expv_opts_t* opts,
+            pi_expv_info_t* info);
+
+/* solve_dynamics(..., algorithm=ExpvAlgorithm(...), saveat=times, observables=obs,
+ * save_states=false) (highlevel.jl:559-733): propagates rho (device, in place) through
+ * the nt saved times and writes nobs complex expectation values per time into
+ * values_host[(it*nobs + o)*2 + {0,1}]; obs_dev holds nobs observable vectors of
+ * length dim (PIOperator data) back to back. */
+int pi_solve_dynamics(pi_plan* plan, double* rho_dev, int nt, const double* times,
+                      int nobs, const double* obs_dev, double* values_host,
+                      const pi_expv_opts_t* opts, pi_expv_info_t* info);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PICUDA_H */

@@ -1,0 +1,502 @@
+// C ABI of libpicuda.so: plan upload, capability, basis maps, apply and dot entry points.
+// The Krylov solver entry points live in pi_solvers.cu.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/picuda.h"
+#include "pi_handle.hpp"
+
+namespace picuda {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? PI_ERR_OUT_OF_MEMORY : PI_ERR_CUDA;
+}
+
+void* plan_alloc(pi_plan* plan, size_t bytes) {
+  void* p = nullptr;
+  if (bytes == 0) bytes = 16;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+  plan->allocations.push_back(p);
+  plan->device_bytes += bytes;
+  return p;
+}
+
+namespace {
+
+template <typename T>
+int upload(pi_plan* plan, const std::vector<T>& host, const T** out) {
+  void* d = plan_alloc(plan, host.size() * sizeof(T));
+  if (!d) return fail(PI_ERR_OUT_OF_MEMORY, "device allocation of plan tables failed");
+  if (!host.empty()) {
+    cudaError_t e = cudaMemcpy(d, host.data(), host.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "plan upload");
+  }
+  *out = (const T*)d;
+  return PI_OK;
+}
+
+void free_plan(pi_plan* plan) {
+  if (!plan) return;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(plan->device);
+  if (plan->stream) cudaStreamSynchronize(plan->stream);
+  for (void* p : plan->allocations) cudaFree(p);
+  if (plan->host_pinned) cudaFreeHost(plan->host_pinned);
+  if (plan->stream) cudaStreamDestroy(plan->stream);
+  cudaSetDevice(cur);
+  delete plan;
+}
+
+bool overlap(const void* a, size_t abytes, const void* b, size_t bbytes) {
+  const char* pa = (const char*)a;
+  const char* pb = (const char*)b;
+  return pa < pb + bbytes && pb < pa + abytes;
+}
+
+}  // namespace
+
+// Flattens the host plan into device tables (explicit_once transfer policy,
+// accelerators.jl:9-11: the plan is uploaded once; applies move no host data).
+int upload_plan(pi_plan* plan) {
+  const QubitPlan& hp = plan->host;
+  const int S = (int)hp.sectors.size();
+  std::vector<DevSector> sectors(S);
+  std::vector<DevTerm> terms;
+  std::vector<double2> coef64;
+  std::vector<float2> coef32x, coef32z;
+  std::vector<DevTile> tiles;
+  std::vector<int> diag_sector;
+  std::vector<long long> diag_index;
+  for (int s = 0; s < S; ++s) {
+    const Sector& sec = hp.sectors[s];
+    DevSector& ds = sectors[s];
+    ds.offset = sec.offset;
+    ds.n = sec.n;
+    ds.term_begin = (int)terms.size();
+    ds.term_count = (int)sec.terms.size();
+    ds.pad = 0;
+    ds.border_x = sec.sqrt_f / hp.trace_norm2;
+    ds.border_z = sec.f / hp.trace_norm2;
+    ds.sqrt_f = sec.sqrt_f;
+    for (const StencilTerm& t : sec.terms) {
+      DevTerm dt;
+      const Sector& src = hp.sectors[t.src];
+      dt.src_off = src.offset;
+      dt.src_n = src.n;
+      dt.kind = t.kind;
+      dt.cls = t.cls;
+      dt.dr = t.e + t.p;
+      dt.dc = t.e + t.q;
+      dt.pad = 0;
+      const double ratio = sec.sqrt_f / src.sqrt_f;  // population-coordinate rescaling
+      dt.alpha_off = -1;
+      dt.beta_off = -1;
+      if (!t.alpha.empty()) {
+        dt.alpha_off = (int)coef64.size();
+        for (const auto& z : t.alpha) {
+          coef64.push_back(make_double2(z.real(), z.imag()));
+          coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
+          coef32z.push_back(make_float2((float)(z.real() * ratio), (float)(z.imag() * ratio)));
+        }
+      }
+      if (!t.beta.empty()) {
+        dt.beta_off = (int)coef64.size();
+        for (const auto& z : t.beta) {
+          // ratio is applied once, on alpha (or on beta for a RIGHT term, which has no alpha)
+          const double r = t.alpha.empty() ? ratio : 1.0;
+          coef64.push_back(make_double2(z.real(), z.imag()));
+          coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
+          coef32z.push_back(make_float2((float)(z.real() * r), (float)(z.imag() * r)));
+        }
+      }
+      terms.push_back(dt);
+    }
+    for (int a0 = 0; a0 < sec.n; a0 += kTileRows)
+      for (int b0 = 0; b0 < sec.n; b0 += kTileCols) tiles.push_back(DevTile{s, a0, b0, 0});
+    for (int a = 0; a < sec.n; ++a) {
+      diag_sector.push_back(s);
+      diag_index.push_back(sec.offset + a + (long long)a * sec.n);
+    }
+  }
+  // Largest sectors first: their tiles are the longest-running.
+  std::stable_sort(tiles.begin(), tiles.end(), [&](const DevTile& x, const DevTile& y) {
+    return hp.sectors[x.sector].n > hp.sectors[y.sector].n;
+  });
+  if (coef64.size() > (size_t)0x7fffffff) return fail(PI_ERR_UNSUPPORTED, "coefficient pool too large");
+  int rc;
+  if ((rc = upload(plan, sectors, &plan->dev.sectors))) return rc;
+  if ((rc = upload(plan, terms, &plan->dev.terms))) return rc;
+  if ((rc = upload(plan, tiles, &plan->dev.tiles))) return rc;
+  if ((rc = upload(plan, coef64, &plan->dev.coef64))) return rc;
+  if ((rc = upload(plan, coef32x, &plan->dev.coef32x))) return rc;
+  if ((rc = upload(plan, coef32z, &plan->dev.coef32z))) return rc;
+  if ((rc = upload(plan, diag_sector, &plan->dev.diag_sector))) return rc;
+  if ((rc = upload(plan, diag_index, &plan->dev.diag_index))) return rc;
+  plan->dev.nsectors = S;
+  plan->dev.ntiles = (int)tiles.size();
+  plan->dev.ndiag = (int)diag_index.size();
+  plan->dev.dim = hp.dim;
+  plan->stencil_terms = (long long)terms.size();
+  plan->rs.partial = (double2*)plan_alloc(plan, sizeof(double2) * kReduceBlocks * kMaxDots);
+  plan->rs.result = (double2*)plan_alloc(plan, sizeof(double2) * kMaxDots);
+  plan->rs.rpartial = (double*)plan_alloc(plan, sizeof(double) * kReduceBlocks);
+  plan->rs.rresult = (double*)plan_alloc(plan, sizeof(double) * 16);
+  if (!plan->rs.partial || !plan->rs.result || !plan->rs.rpartial || !plan->rs.rresult)
+    return fail(PI_ERR_OUT_OF_MEMORY, "device allocation of reduction scratch failed");
+  cudaError_t e = cudaMallocHost((void**)&plan->host_pinned, sizeof(double) * 4 * kMaxDots);
+  if (e != cudaSuccess) return cuda_fail(e, "pinned staging allocation");
+  return PI_OK;
+}
+
+}  // namespace picuda
+
+using namespace picuda;
+
+extern "C" {
+
+int pi_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return PI_ERR_INVALID_ARGUMENT;
+  std::strncpy(buf, g_last_error.c_str(), len - 1);
+  buf[len - 1] = '\0';
+  return PI_OK;
+}
+
+int pi_capability(pi_capability_t* out) {
+  if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "null capability pointer");
+  std::memset(out, 0, sizeof(*out));
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    out->functional = 0;
+    return fail(PI_ERR_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+  }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceProp prop;
+  e = cudaGetDeviceProperties(&prop, dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceProperties");
+  out->device_count = count;
+  out->sm_count = prop.multiProcessorCount;
+  out->cc_major = prop.major;
+  out->cc_minor = prop.minor;
+  out->total_memory = prop.totalGlobalMem;
+  std::strncpy(out->device_name, prop.name, sizeof(out->device_name) - 1);
+  // The kernels are built for sm_103a only.
+  out->functional = (prop.major == 10 && prop.minor == 3) ? 1 : 0;
+  out->supports_matrixfree_pi = out->functional;
+  if (!out->functional) return fail(PI_ERR_NO_DEVICE, "libpicuda is built for sm_103a only");
+  return PI_OK;
+}
+
+static int build_host_plan(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                           const double* ops, const double* rates, const double* hbar, QubitPlan* out) {
+  if (d != 2) return fail(PI_ERR_UNSUPPORTED, "the CUDA backend supports qubit ensembles (d == 2) only");
+  if (N < 1) return fail(PI_ERR_INVALID_ARGUMENT, "N must be positive");
+  if (nterms < 0 || (nterms > 0 && (!term_kind || !ops || !rates)))
+    return fail(PI_ERR_INVALID_ARGUMENT, "term arrays are missing");
+  if (nsectors < 0 || (nsectors > 0 && !sector_ks)) return fail(PI_ERR_INVALID_ARGUMENT, "sector list is missing");
+  std::vector<int> ks(sector_ks, sector_ks + (nsectors > 0 ? nsectors : 0));
+  std::vector<TermSpec> terms(nterms);
+  for (int t = 0; t < nterms; ++t) {
+    terms[t].kind = term_kind[t];
+    // column-major interleaved: element (i, j) at (i + 2j) * 2
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 2; ++j)
+        terms[t].op[i][j] = std::complex<double>(ops[t * 8 + (i + 2 * j) * 2], ops[t * 8 + (i + 2 * j) * 2 + 1]);
+    terms[t].rate = rates[t];
+    terms[t].hbar = hbar ? hbar[t] : 1.0;
+  }
+  try {
+    *out = build_qubit_plan(N, ks, terms);
+  } catch (const std::invalid_argument& ex) {
+    return fail(PI_ERR_INVALID_ARGUMENT, ex.what());
+  } catch (const std::exception& ex) {
+    return fail(PI_ERR_UNSUPPORTED, ex.what());
+  }
+  return PI_OK;
+}
+
+int pi_stencil_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                      const double* ops, const double* rates, const double* hbar, long long* counts,
+                      int* term_table, double* coef) {
+  if (!counts) return fail(PI_ERR_INVALID_ARGUMENT, "null counts");
+  QubitPlan hp;
+  int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
+  if (rc) return rc;
+  long long nt = 0, nc = 0;
+  for (const auto& sec : hp.sectors)
+    for (const auto& t : sec.terms) {
+      ++nt;
+      nc += (long long)t.alpha.size() + (long long)t.beta.size();
+    }
+  counts[0] = nt;
+  counts[1] = nc;
+  if (!term_table || !coef) return PI_OK;
+  long long it = 0, ic = 0;
+  for (size_t s = 0; s < hp.sectors.size(); ++s)
+    for (const auto& t : hp.sectors[s].terms) {
+      int* row = term_table + 8 * it++;
+      row[0] = (int)s;
+      row[1] = t.src;
+      row[2] = t.kind;
+      row[3] = t.cls;
+      row[4] = t.e + t.p;
+      row[5] = t.e + t.q;
+      row[6] = -1;
+      row[7] = -1;
+      if (!t.alpha.empty()) {
+        row[6] = (int)ic;
+        for (const auto& z : t.alpha) {
+          coef[2 * ic] = z.real();
+          coef[2 * ic + 1] = z.imag();
+          ++ic;
+        }
+      }
+      if (!t.beta.empty()) {
+        row[7] = (int)ic;
+        for (const auto& z : t.beta) {
+          coef[2 * ic] = z.real();
+          coef[2 * ic + 1] = z.imag();
+          ++ic;
+        }
+      }
+    }
+  return PI_OK;
+}
+
+int pi_collective_block(int N, int k, const double* op, double* out) {
+  if (!op || !out) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  if (N < 1 || k < 0 || 2 * k > N) return fail(PI_ERR_INVALID_ARGUMENT, "sector is not a two-row partition of N");
+  std::complex<double> X[2][2];
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 2; ++j) X[i][j] = std::complex<double>(op[(i + 2 * j) * 2], op[(i + 2 * j) * 2 + 1]);
+  try {
+    auto B = collective_block_dense(N, k, X);
+    for (size_t e = 0; e < B.size(); ++e) {
+      out[2 * e] = B[e].real();
+      out[2 * e + 1] = B[e].imag();
+    }
+  } catch (const std::exception& ex) {
+    return fail(PI_ERR_INVALID_ARGUMENT, ex.what());
+  }
+  return PI_OK;
+}
+
+int pi_sector_multiplicity(int N, int k, double* f, double* sqrt_f) {
+  if (N < 0 || k < 0 || 2 * k > N) return fail(PI_ERR_INVALID_ARGUMENT, "sector is not a two-row partition of N");
+  const double v = sector_multiplicity_double(N, k);
+  if (f) *f = v;
+  if (sqrt_f) *sqrt_f = std::sqrt(v);
+  return PI_OK;
+}
+
+int pi_plan_create(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                   const double* ops, const double* rates, const double* hbar, pi_plan** out) {
+  if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  pi_plan* plan = new (std::nothrow) pi_plan();
+  if (!plan) return fail(PI_ERR_OUT_OF_MEMORY, "host allocation failed");
+  int brc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &plan->host);
+  if (brc != PI_OK) {
+    delete plan;
+    return brc;
+  }
+  if (plan->host.dim > (long long)1 << 31) {
+    delete plan;
+    return fail(PI_ERR_UNSUPPORTED, "PI dimension exceeds the 32-bit tile addressing of this build");
+  }
+  cudaError_t e = cudaGetDevice(&plan->device);
+  if (e != cudaSuccess) {
+    delete plan;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  e = cudaStreamCreateWithFlags(&plan->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete plan;
+    return cuda_fail(e, "cudaStreamCreate");
+  }
+  int rc = upload_plan(plan);
+  if (rc != PI_OK) {
+    std::string msg = g_last_error;
+    free_plan(plan);
+    return fail(rc, msg);
+  }
+  *out = plan;
+  return PI_OK;
+}
+
+int pi_plan_destroy(pi_plan* plan) {
+  free_plan(plan);
+  return PI_OK;
+}
+
+int pi_plan_info(const pi_plan* plan, pi_plan_info_t* out) {
+  if (!plan || !out) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  out->N = plan->host.N;
+  out->nsectors = (int)plan->host.sectors.size();
+  out->dim = plan->host.dim;
+  out->max_block = plan->host.max_n;
+  out->max_terms = plan->host.max_terms;
+  out->stencil_terms = plan->stencil_terms;
+  out->device_bytes = plan->device_bytes;
+  return PI_OK;
+}
+
+int pi_plan_sectors(const pi_plan* plan, int* ks, long long* offsets, int* dims) {
+  if (!plan) return fail(PI_ERR_INVALID_ARGUMENT, "null plan");
+  const auto& sec = plan->host.sectors;
+  for (size_t s = 0; s < sec.size(); ++s) {
+    if (ks) ks[s] = sec[s].k;
+    if (offsets) offsets[s] = sec[s].offset;
+    if (dims) dims[s] = sec[s].n;
+  }
+  return PI_OK;
+}
+
+int pi_plan_gt_patterns(const pi_plan* plan, int sector, int* entries) {
+  if (!plan || !entries) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  if (sector < 0 || sector >= (int)plan->host.sectors.size()) return fail(PI_ERR_INVALID_ARGUMENT, "sector out of range");
+  const auto& sec = plan->host.sectors[sector];
+  const int N = plan->host.N;
+  for (int a = 0; a < sec.n; ++a) {
+    entries[3 * a] = sec.k + a;  // row 1 entry m, ascending
+    entries[3 * a + 1] = N - sec.k;
+    entries[3 * a + 2] = sec.k;
+  }
+  return PI_OK;
+}
+
+int pi_plan_trace_functional(const pi_plan* plan, long long* idx, double* vals) {
+  if (!plan || !idx || !vals) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  long long i = 0;
+  for (const auto& sec : plan->host.sectors)
+    for (int a = 0; a < sec.n; ++a, ++i) {
+      idx[i] = sec.offset + a + (long long)a * sec.n;
+      vals[i] = sec.sqrt_f;
+    }
+  return PI_OK;
+}
+
+int pi_plan_sector_scales(const pi_plan* plan, double* sqrt_f) {
+  if (!plan || !sqrt_f) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  for (size_t s = 0; s < plan->host.sectors.size(); ++s) sqrt_f[s] = plan->host.sectors[s].sqrt_f;
+  return PI_OK;
+}
+
+static int check_apply_args(pi_plan* plan, const void* y, const void* x, int ncols, long long ld, size_t elem) {
+  if (!plan || !x || !y) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  if (ncols < 1 || ncols > 65535) return fail(PI_ERR_INVALID_ARGUMENT, "ncols must lie in 1:65535");
+  if (ld < plan->host.dim) return fail(PI_ERR_DIMENSION, "leading dimension is smaller than the PI dimension");
+  const size_t bytes = ((size_t)(ncols - 1) * (size_t)ld + (size_t)plan->host.dim) * elem;
+  if (overlap(x, bytes, y, bytes))
+    return fail(PI_ERR_INVALID_ARGUMENT, "source and destination must not share storage");
+  return PI_OK;
+}
+
+int pi_apply_f64(pi_plan* plan, double* y_dev, const double* x_dev, int ncols, long long ld, void* stream) {
+  int rc = check_apply_args(plan, y_dev, x_dev, ncols, ld, sizeof(double2));
+  if (rc) return rc;
+  BorderArgs border{1.0, nullptr, 0};
+  cudaStream_t s = stream ? (cudaStream_t)stream : plan->stream;
+  cudaError_t e = launch_apply_f64(plan->dev, x_dev, y_dev, ncols, ld, border, s);
+  if (e != cudaSuccess) return cuda_fail(e, "apply launch");
+  return PI_OK;
+}
+
+int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld, int coords,
+                 void* stream) {
+  int rc = check_apply_args(plan, y_dev, x_dev, ncols, ld, sizeof(float2));
+  if (rc) return rc;
+  if (coords != PI_COORDS_REFERENCE && coords != PI_COORDS_POPULATION)
+    return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
+  BorderArgs border{1.0, nullptr, coords};
+  cudaStream_t s = stream ? (cudaStream_t)stream : plan->stream;
+  cudaError_t e = launch_apply_f32(plan->dev, x_dev, y_dev, ncols, ld, border, s);
+  if (e != cudaSuccess) return cuda_fail(e, "apply launch");
+  return PI_OK;
+}
+
+}  // extern "C"
+
+template <typename T>
+static int apply_host(pi_plan* plan, void* y_host, const void* x_host, int ncols, int coords) {
+  if (!plan || !y_host || !x_host) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  if (ncols < 1 || ncols > 65535) return fail(PI_ERR_INVALID_ARGUMENT, "ncols must lie in 1:65535");
+  if (coords != PI_COORDS_REFERENCE && coords != PI_COORDS_POPULATION)
+    return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
+  const size_t bytes = (size_t)ncols * (size_t)plan->host.dim * 2 * sizeof(T);
+  if (overlap(x_host, bytes, y_host, bytes))
+    return fail(PI_ERR_INVALID_ARGUMENT, "source and destination must not share storage");
+  BusyGuard guard(plan);
+  if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
+  cudaStream_t s = plan->stream;
+  void *dx = nullptr, *dy = nullptr;
+  cudaError_t e = cudaMallocAsync(&dx, bytes, s);
+  if (e != cudaSuccess) return cuda_fail(e, "device allocation");
+  e = cudaMallocAsync(&dy, bytes, s);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(dx, s);
+    cudaStreamSynchronize(s);
+    return cuda_fail(e, "device allocation");
+  }
+  BorderArgs border{1.0, nullptr, coords};
+  e = cudaMemcpyAsync(dx, x_host, bytes, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    if (sizeof(T) == sizeof(double))
+      e = launch_apply_f64(plan->dev, (const double*)dx, (double*)dy, ncols, plan->host.dim, border, s);
+    else
+      e = launch_apply_f32(plan->dev, (const float*)dx, (float*)dy, ncols, plan->host.dim, border, s);
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(y_host, dy, bytes, cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(dx, s);
+  cudaFreeAsync(dy, s);
+  cudaError_t e2 = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "host apply");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "host apply synchronize");
+  return PI_OK;
+}
+
+extern "C" {
+
+int pi_apply_host_f64(pi_plan* plan, double* y_host, const double* x_host, int ncols) {
+  return apply_host<double>(plan, y_host, x_host, ncols, PI_COORDS_REFERENCE);
+}
+
+int pi_apply_host_f32(pi_plan* plan, float* y_host, const float* x_host, int ncols, int coords) {
+  return apply_host<float>(plan, y_host, x_host, ncols, coords);
+}
+
+int pi_dot_f64(pi_plan* plan, const double* a_dev, const double* b_dev, double* out_host2) {
+  if (!plan || !a_dev || !b_dev || !out_host2) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  BusyGuard guard(plan);
+  if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
+  cudaStream_t s = plan->stream;
+  cudaError_t e = mdot_f64((const double2*)a_dev, plan->host.dim, 1, (const double2*)b_dev, plan->host.dim,
+                           plan->rs, plan->rs.result, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(plan->host_pinned, plan->rs.result, sizeof(double2), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "dot");
+  out_host2[0] = plan->host_pinned[0];
+  out_host2[1] = plan->host_pinned[1];
+  return PI_OK;
+}
+
+}  // extern "C"

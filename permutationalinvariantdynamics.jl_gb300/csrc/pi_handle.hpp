@@ -1,0 +1,47 @@
+// The opaque pi_plan handle behind the C ABI.
+#pragma once
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "pi_internal.hpp"
+#include "pi_plan.hpp"
+
+struct pi_plan {
+  picuda::QubitPlan host;
+  picuda::DevicePlan dev;
+  std::vector<void*> allocations;  // device buffers owned by the plan tables
+  size_t device_bytes = 0;
+  long long stencil_terms = 0;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  picuda::ReduceScratch rs;        // reduction scratch (device)
+  double* host_pinned = nullptr;   // small pinned staging buffer for reductions
+  std::atomic<int> busy{0};
+};
+
+namespace picuda {
+
+// Thread-local error message for pi_last_error.
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+// RAII guard that rejects concurrent use of one plan (threaded_apply.jl:575).
+struct BusyGuard {
+  pi_plan* p;
+  bool ok;
+  explicit BusyGuard(pi_plan* plan) : p(plan) {
+    int expected = 0;
+    ok = p->busy.compare_exchange_strong(expected, 1);
+  }
+  ~BusyGuard() {
+    if (ok) p->busy.store(0);
+  }
+};
+
+// Device allocation tracked by the plan; returns nullptr on failure.
+void* plan_alloc(pi_plan* plan, size_t bytes);
+
+}  // namespace picuda

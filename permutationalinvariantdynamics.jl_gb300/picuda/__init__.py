@@ -1,0 +1,18 @@
+"""picuda: GB300 backend for the Schur-block Liouvillian hot path of PermutationalInvariantDynamics.jl.
+
+The Python layer mirrors the reference's user-facing API (PIBasis, qubit models,
+compile(model; backend=:cuda), apply!, solve_dynamics, stationary_state) over the C ABI of
+libpicuda.so (include/picuda.h), whose sm_103a kernels do all numerical work.
+"""
+from ._lib import (PI_FP32, PI_FP64, PiArgumentError, PiDimensionMismatch, PiError, PiNotConverged,
+                   load as load_library)
+from .backend import (AcceleratorCapability, CompiledPIModel, DynamicsResult, DynamicsStreamResult,
+                      ExpvAlgorithm, GMRESAlgorithm, SteadyStateResult, accelerator_capability, apply_,
+                      compile, krylov_expv, mul, saved_times, solve_dynamics, stationary_state,
+                      steady_state, stencil_tables)
+from .core import (CollectiveHamiltonian, CollectiveJump, LocalHamiltonian, LocalJump, Models, PIBasis,
+                   PIModel, PIOperator, PIState, Term, collective_operator, collective_spin,
+                   computational_product_state, expectation, iid_pure_state, qubit_ensemble_model,
+                   spin_matrices)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

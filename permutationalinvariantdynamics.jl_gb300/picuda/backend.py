@@ -1,0 +1,524 @@
+"""compile(model; backend=:cuda), apply!, solve_dynamics and stationary_state over libpicuda.
+
+Mirrors the reference's high-level entry points (src/liouvillian.jl:4040-4098 compile,
+:4165-4189 apply!/mul!, src/highlevel.jl:321-371 stationary_state, :559-733 solve_dynamics,
+src/accelerators.jl:83-85 accelerator_capability) for the CUDA backend.  Every numerical
+step runs in libpicuda on the GPU; device buffers come from torch (plumbing only).  There
+is no CPU fallback: without the library or a GPU these functions raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import PiArgumentError, PiDimensionMismatch
+from .core import PIBasis, PIModel, PIOperator, PIState, collective_operator, spin_matrices
+
+_DEFAULT_MEMORY_BUDGET = 512 * 1024 ** 2
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise _lib.PiError("the CUDA backend needs a CUDA device; no CPU fallback exists")
+    return torch
+
+
+@dataclass(frozen=True)
+class AcceleratorCapability:
+    """accelerators.jl:13-25 fields for backend :cuda."""
+    backend: str
+    extension_loaded: bool
+    functional: bool
+    supports_sparse_pi: bool
+    supports_matrixfree_pi: bool
+    rhs_kinds: tuple
+    scalar_types: tuple
+    index_type: str
+    transfer_policy: str
+    reason: str
+    message: str
+    device_name: str = ""
+    sm_count: int = 0
+
+
+def accelerator_capability(backend: str = "cuda") -> AcceleratorCapability:
+    """Reports whether the CUDA backend is loaded and functional (accelerators.jl:83-85)."""
+    if backend != "cuda":
+        return AcceleratorCapability(backend, False, False, False, False, (), (), "Int", "unsupported",
+                                     "unknown_backend",
+                                     f"accelerator backend :{backend} is not registered")
+    try:
+        lib = _lib.load()
+    except _lib.PiError as err:
+        return AcceleratorCapability("cuda", False, False, False, False, ("vector", "matrix"),
+                                     ("ComplexF64", "ComplexF32"), "Int32", "explicit_once",
+                                     "extension_not_loaded", str(err))
+    cap = _lib.pi_capability_t()
+    rc = lib.pi_capability(C.byref(cap))
+    functional = rc == _lib.PI_OK and bool(cap.functional)
+    return AcceleratorCapability(
+        "cuda", True, functional, False, functional, ("vector", "matrix"), ("ComplexF64", "ComplexF32"),
+        "Int32", "explicit_once", "ready" if functional else "device_unavailable",
+        "libpicuda matrix-free Schur-block backend" if functional else _lib.last_error(),
+        cap.device_name.decode(errors="replace"), cap.sm_count)
+
+
+def _term_arrays(model: PIModel):
+    kinds = np.array([t.kind for t in model.terms], dtype=np.int32)
+    ops = np.zeros((max(len(model.terms), 1), 8), dtype=np.float64)
+    for i, t in enumerate(model.terms):
+        ops[i] = t.operator.reshape(-1, order="F").view(np.float64)
+    rates = np.array([t.rate for t in model.terms] or [0.0], dtype=np.float64)
+    hbar = np.array([t.hbar for t in model.terms] or [1.0], dtype=np.float64)
+    ks = np.array(model.basis.ks, dtype=np.int32)
+    return kinds, np.ascontiguousarray(ops), rates, hbar, ks
+
+
+def stencil_tables(model: PIModel):
+    """Host-only export of the lowered stencil (pi_stencil_export): (terms[n,8], coef[c])."""
+    lib = _lib.load()
+    kinds, ops, rates, hbar, ks = _term_arrays(model)
+    counts = np.zeros(2, dtype=np.int64)
+    args = (model.basis.N, model.basis.d, len(ks), _lib.iptr(ks), len(model.terms), _lib.iptr(kinds),
+            _lib.dptr(ops), _lib.dptr(rates), _lib.dptr(hbar), _lib.llptr(counts))
+    _lib.check(lib.pi_stencil_export(*args, None, None), "pi_stencil_export")
+    table = np.zeros((int(counts[0]), 8), dtype=np.int32)
+    coef = np.zeros(int(counts[1]), dtype=np.complex128)
+    _lib.check(lib.pi_stencil_export(*args, _lib.iptr(table), _lib.dptr(coef.view(np.float64))),
+               "pi_stencil_export")
+    return table, coef
+
+
+class CompiledPIModel:
+    """A model lowered and uploaded once to the GPU (CompiledPIModel, liouvillian.jl:3495-3501)."""
+
+    def __init__(self, model: PIModel, memory_budget=_DEFAULT_MEMORY_BUDGET):
+        self.model = model
+        self.basis = model.basis
+        self.backend = "cuda"
+        lib = _lib.load()
+        kinds, ops, rates, hbar, ks = _term_arrays(model)
+        handle = C.c_void_p()
+        _lib.check(lib.pi_plan_create(model.basis.N, model.basis.d, len(ks), _lib.iptr(ks),
+                                      len(model.terms), _lib.iptr(kinds), _lib.dptr(ops),
+                                      _lib.dptr(rates), _lib.dptr(hbar), C.byref(handle)),
+                   "compile(model; backend=:cuda)")
+        self._handle = handle
+        info = _lib.pi_plan_info_t()
+        _lib.check(lib.pi_plan_info(handle, C.byref(info)), "pi_plan_info")
+        self.info = {f: getattr(info, f) for f, _ in info._fields_}
+        if len(self.basis) != info.dim:
+            raise PiDimensionMismatch("library and host bases disagree")
+        if memory_budget is not None and np.isfinite(memory_budget) and info.device_bytes > memory_budget:
+            self.close()
+            raise PiArgumentError("the prepared CUDA plan exceeds memory_budget")
+
+    @property
+    def handle(self):
+        if self._handle is None:
+            raise _lib.PiError("the compiled model has been closed")
+        return self._handle
+
+    def close(self):
+        if getattr(self, "_handle", None) is not None:
+            _lib.load().pi_plan_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.basis)
+
+    @property
+    def shape(self):
+        n = len(self.basis)
+        return (n, n)
+
+    def isautonomous(self):
+        return True
+
+    # -- basis maps straight from the library (bit-exact) --------------------------------
+    def library_sectors(self):
+        lib = _lib.load()
+        S = self.info["nsectors"]
+        ks = np.zeros(S, dtype=np.int32)
+        offs = np.zeros(S, dtype=np.int64)
+        dims = np.zeros(S, dtype=np.int32)
+        _lib.check(lib.pi_plan_sectors(self.handle, _lib.iptr(ks), _lib.llptr(offs), _lib.iptr(dims)),
+                   "pi_plan_sectors")
+        return ks, offs, dims
+
+    def library_patterns(self, sector):
+        lib = _lib.load()
+        n = self.basis.dims[sector]
+        out = np.zeros(3 * n, dtype=np.int32)
+        _lib.check(lib.pi_plan_gt_patterns(self.handle, sector, _lib.iptr(out)), "pi_plan_gt_patterns")
+        return out.reshape(n, 3)
+
+    def library_trace_functional(self):
+        lib = _lib.load()
+        nd = sum(self.basis.dims)
+        idx = np.zeros(nd, dtype=np.int64)
+        val = np.zeros(nd, dtype=np.float64)
+        _lib.check(lib.pi_plan_trace_functional(self.handle, _lib.llptr(idx), _lib.dptr(val)),
+                   "pi_plan_trace_functional")
+        return idx, val
+
+    def sector_scales(self):
+        lib = _lib.load()
+        out = np.zeros(self.info["nsectors"], dtype=np.float64)
+        _lib.check(lib.pi_plan_sector_scales(self.handle, _lib.dptr(out)), "pi_plan_sector_scales")
+        return out
+
+
+def compile(model: PIModel, backend: str = "cuda", memory_budget=_DEFAULT_MEMORY_BUDGET):
+    """compile(model; backend=:cuda) (liouvillian.jl:4040-4098)."""
+    if backend != "cuda":
+        raise PiArgumentError("this package implements backend=:cuda only")
+    if not isinstance(model, PIModel):
+        raise PiArgumentError("compile requires a PIModel")
+    return CompiledPIModel(model, memory_budget)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def apply_(y, compiled: CompiledPIModel, x, t=0.0, p=None, precision="fp64", coords="reference"):
+    """apply!(y, compiled, x, t, p) (liouvillian.jl:4165-4171).
+
+    x, y: torch CUDA tensors (complex128 for fp64, complex64 for fp32) of shape (dim,) or
+    (ncols, dim) -- device-resident, no transfers -- or numpy complex128 arrays (the
+    host-buffer convenience path, fp64 only).  Aliasing of x and y is rejected.
+    """
+    if p is not None:
+        raise PiArgumentError("the CUDA backend applies autonomous generators (parameters=nothing)")
+    lib = _lib.load()
+    n = len(compiled.basis)
+    if isinstance(x, np.ndarray):
+        if precision != "fp64":
+            raise PiArgumentError("host-buffer apply is FP64")
+        if x.dtype != np.complex128 or y.dtype != np.complex128:
+            raise PiArgumentError("host buffers must be complex128")
+        if x.shape != y.shape or x.shape[-1] != n:
+            raise PiDimensionMismatch("Liouvillian vector has the wrong length")
+        if np.shares_memory(x, y):
+            raise PiArgumentError("source and destination must not share storage")
+        xc = np.ascontiguousarray(x)
+        ncols = 1 if x.ndim == 1 else x.shape[0]
+        out = np.empty_like(xc) if not y.flags.c_contiguous else y
+        _lib.check(lib.pi_apply_host_f64(compiled.handle, out.ctypes.data_as(C.c_void_p),
+                                         xc.ctypes.data_as(C.c_void_p), ncols), "apply!")
+        if out is not y:
+            y[...] = out
+        return y
+    torch = _torch()
+    if x.shape != y.shape or x.shape[-1] != n or not x.is_cuda or not y.is_cuda:
+        raise PiDimensionMismatch("Liouvillian vector has the wrong length or is not on the GPU")
+    if not (x.is_contiguous() and y.is_contiguous()):
+        raise PiArgumentError("device vectors must be contiguous")
+    ncols = 1 if x.dim() == 1 else x.shape[0]
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if precision == "fp64":
+        if x.dtype != torch.complex128 or y.dtype != torch.complex128:
+            raise PiArgumentError("fp64 apply needs complex128 tensors")
+        _lib.check(lib.pi_apply_f64(compiled.handle, _ptr(y), _ptr(x), ncols, n, stream), "apply!")
+    elif precision == "fp32":
+        if x.dtype != torch.complex64 or y.dtype != torch.complex64:
+            raise PiArgumentError("fp32 apply needs complex64 tensors")
+        cc = _lib.PI_COORDS_POPULATION if coords == "population" else _lib.PI_COORDS_REFERENCE
+        _lib.check(lib.pi_apply_f32(compiled.handle, _ptr(y), _ptr(x), ncols, n, cc, stream), "apply!")
+    else:
+        raise PiArgumentError("precision must be 'fp64' or 'fp32'")
+    return y
+
+
+def mul(compiled: CompiledPIModel, x):
+    """L * x for a host vector (allocating wrapper of apply!)."""
+    y = np.empty_like(np.asarray(x, dtype=np.complex128))
+    return apply_(y, compiled, np.asarray(x, dtype=np.complex128))
+
+
+# ---------------------------------------------------------------------------------------
+# Algorithms (highlevel.jl:32-125)
+# ---------------------------------------------------------------------------------------
+
+@dataclass(frozen=True)
+class GMRESAlgorithm:
+    """Restarted matrix-free GMRES (highlevel.jl:32-41); precision 'fp64' (the reference's
+    method) or 'mixed' (FP32 inner applies with FP64 refinement)."""
+    krylovdim: int = 30
+    maxiter: int = 500
+    preconditioner: object = None
+    precision: str = "fp64"
+
+    def __post_init__(self):
+        if isinstance(self.krylovdim, bool) or self.krylovdim < 1:
+            raise PiArgumentError("krylovdim must be at least 1")
+        if isinstance(self.maxiter, bool) or self.maxiter < 1:
+            raise PiArgumentError("maxiter must be at least 1")
+        if self.preconditioner is not None:
+            raise PiArgumentError("the CUDA backend runs unpreconditioned GMRES")
+        if self.precision not in ("fp64", "mixed"):
+            raise PiArgumentError("precision must be 'fp64' or 'mixed'")
+
+
+@dataclass(frozen=True)
+class ExpvAlgorithm:
+    """Adaptive restarted-Arnoldi exponential action (highlevel.jl:81-125)."""
+    krylovdim: int = 30
+    atol: float = 1e-10
+    rtol: float = 1e-8
+    initial_step: float | None = None
+    minimum_step: float | None = None
+    maximum_step: float | None = None
+    max_steps: int = 10_000
+    safety: float = 0.9
+    precision: str = "fp64"
+
+    def __post_init__(self):
+        if not (np.isfinite(self.atol) and np.isfinite(self.rtol) and self.atol >= 0 and self.rtol >= 0):
+            raise PiArgumentError("atol and rtol must be finite nonnegative real numbers")
+        if not (0 < self.safety < 1):
+            raise PiArgumentError("safety must lie strictly between zero and one")
+        for name, allow_zero in (("initial_step", False), ("minimum_step", True), ("maximum_step", False)):
+            v = getattr(self, name)
+            if v is not None and (not np.isfinite(v) or (v < 0 if allow_zero else v <= 0)):
+                raise PiArgumentError(f"{name} must be nothing or a finite {'nonnegative' if allow_zero else 'positive'} real number")
+        if self.minimum_step is not None and self.maximum_step is not None and self.minimum_step > self.maximum_step:
+            raise PiArgumentError("minimum_step must not exceed maximum_step")
+        if self.minimum_step is not None and self.initial_step is not None and self.initial_step < self.minimum_step:
+            raise PiArgumentError("initial_step must not be smaller than minimum_step")
+        if self.precision not in ("fp64", "mixed"):
+            raise PiArgumentError("precision must be 'fp64' or 'mixed'")
+
+    def opts(self):
+        o = _lib.pi_expv_opts_t()
+        _lib.load().pi_expv_default_opts(C.byref(o))
+        o.krylovdim = self.krylovdim
+        o.atol = self.atol
+        o.rtol = self.rtol
+        o.initial_step = self.initial_step or 0.0
+        o.minimum_step = self.minimum_step or 0.0
+        o.maximum_step = self.maximum_step or 0.0
+        o.max_steps = self.max_steps
+        o.safety = self.safety
+        o.precision = _lib.PI_FP32 if self.precision == "mixed" else _lib.PI_FP64
+        return o
+
+
+@dataclass
+class SteadyStateResult:
+    """SteadyStateResult: state plus solver information (krylov.jl:876-889)."""
+    state: PIState
+    info: dict
+    algorithm: GMRESAlgorithm
+
+
+@dataclass
+class DynamicsResult:
+    t: list
+    states: list
+    algorithm: str = "expv"
+
+    def __len__(self):
+        return len(self.t)
+
+    def __getitem__(self, i):
+        return self.states[i]
+
+
+@dataclass
+class DynamicsStreamResult:
+    t: list
+    states: list | None
+    values: dict = field(default_factory=dict)
+    algorithm: str = "expv"
+
+
+def _as_compiled(x) -> CompiledPIModel:
+    if isinstance(x, CompiledPIModel):
+        return x
+    if isinstance(x, PIModel):
+        return compile(x, backend="cuda")
+    raise PiArgumentError("expected a PIModel or a CompiledPIModel")
+
+
+def stationary_state(x, algorithm=None, return_info=False, atol=1e-10, rtol=1e-8, operator_scale=None,
+                     initial_state=None, max_refinements=200):
+    """stationary_state(x; algorithm=GMRESAlgorithm(...)) (highlevel.jl:321-371) on the GPU."""
+    torch = _torch()
+    algorithm = algorithm or GMRESAlgorithm()
+    if isinstance(algorithm, str):
+        if algorithm not in ("gmres", "auto"):
+            raise PiArgumentError("the CUDA backend solves stationary states with GMRES")
+        algorithm = GMRESAlgorithm()
+    compiled = _as_compiled(x)
+    n = len(compiled.basis)
+    o = _lib.pi_gmres_opts_t()
+    lib = _lib.load()
+    lib.pi_gmres_default_opts(C.byref(o))
+    o.krylovdim = algorithm.krylovdim
+    o.maxiter = algorithm.maxiter
+    o.atol, o.rtol = atol, rtol
+    o.operator_scale = float(operator_scale) if operator_scale else 0.0
+    o.precision = _lib.PI_FP32 if algorithm.precision == "mixed" else _lib.PI_FP64
+    o.max_refinements = max_refinements
+    xd = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    if initial_state is not None:
+        init = initial_state.data if isinstance(initial_state, PIState) else np.asarray(initial_state)
+        if init.shape != (n,):
+            raise PiDimensionMismatch("initial_state has wrong length")
+        xd.copy_(torch.from_numpy(np.ascontiguousarray(init, dtype=np.complex128)))
+        o.use_initial = 1
+    torch.cuda.synchronize()
+    info = _lib.pi_gmres_info_t()
+    _lib.check(lib.pi_steady_state(compiled.handle, _ptr(xd), C.byref(o), C.byref(info)),
+               "stationary_state")
+    rho = PIState(compiled.basis, xd.cpu().numpy())
+    if not return_info:
+        return rho
+    d = {f: getattr(info, f) for f, _ in info._fields_}
+    d.update(method="krylov", krylov_dimension=algorithm.krylovdim, precision=algorithm.precision,
+             state=rho.data)
+    return SteadyStateResult(rho, d, algorithm)
+
+
+def steady_state(x, method="krylov", **kwargs):
+    """Low-level steady_state(compiled; method=:krylov) (liouvillian.jl:4752-4761)."""
+    if method not in ("krylov", "gmres"):
+        raise PiArgumentError("the CUDA backend supports method=:krylov")
+    alg = GMRESAlgorithm(krylovdim=kwargs.pop("krylovdim", 30), maxiter=kwargs.pop("maxiter", 500),
+                         precision=kwargs.pop("precision", "fp64"))
+    return stationary_state(x, algorithm=alg, **kwargs).data
+
+
+def krylov_expv(compiled, b, t, algorithm: ExpvAlgorithm | None = None, return_info=False):
+    """krylov_expv(A, b, t; ...) (krylov_extensions.jl:1578-1585) on the GPU."""
+    torch = _torch()
+    algorithm = algorithm or ExpvAlgorithm()
+    compiled = _as_compiled(compiled)
+    lib = _lib.load()
+    data = b.data if isinstance(b, PIState) else np.asarray(b)
+    xd = torch.from_numpy(np.ascontiguousarray(data, dtype=np.complex128)).cuda()
+    torch.cuda.synchronize()
+    info = _lib.pi_expv_info_t()
+    o = algorithm.opts()
+    _lib.check(lib.pi_expv(compiled.handle, _ptr(xd), float(t), C.byref(o), C.byref(info)), "krylov_expv")
+    out = xd.cpu().numpy()
+    if return_info:
+        return out, {f: getattr(info, f) for f, _ in info._fields_}
+    return out
+
+
+def saved_times(tspan, saveat):
+    """Saved-time grid (highlevel.jl:434-465)."""
+    t0, t1 = float(tspan[0]), float(tspan[1])
+    if t1 < t0:
+        raise PiArgumentError("tspan must be ordered")
+    if saveat is None:
+        return [t0, t1]
+    if np.isscalar(saveat):
+        step = float(saveat)
+        if not (np.isfinite(step) and step > 0):
+            raise PiArgumentError("saveat must be finite and positive")
+        count = int(np.floor((t1 - t0) / step * (1 + 1e-15))) + 1
+        ts = [t0 + i * step for i in range(count) if t0 + i * step <= t1]
+        if not ts or ts[-1] < t1:
+            ts.append(t1)
+        return ts
+    ts = [float(v) for v in saveat]
+    if not ts:
+        raise PiArgumentError("saveat cannot be empty")
+    if ts[0] != t0 or ts[-1] != t1:
+        raise PiArgumentError("explicit saveat times must include both endpoints of tspan")
+    if any(b < a for a, b in zip(ts, ts[1:])):
+        raise PiArgumentError("saveat times must be nondecreasing")
+    return ts
+
+
+def _observable_data(basis, obs):
+    if isinstance(obs, (PIOperator, PIState)):
+        return obs.data
+    a = np.asarray(obs, dtype=np.complex128)
+    if a.shape == (basis.d, basis.d):
+        return collective_operator(basis, a).data  # a local matrix denotes its collective sum
+    if a.shape == (len(basis),):
+        return a
+    raise PiDimensionMismatch("observable must be a PIOperator, a local d x d matrix or a PI vector")
+
+
+def solve_dynamics(x, rho0: PIState, tspan, algorithm="expv", saveat=None, observables=None,
+                   save_states=True, parameters=None):
+    """solve_dynamics(x, rho0, tspan; algorithm=:expv | ExpvAlgorithm(...)) (highlevel.jl:559-733)."""
+    torch = _torch()
+    if parameters is not None:
+        raise PiArgumentError("Krylov exponential dynamics requires parameters=nothing")
+    if isinstance(algorithm, str):
+        if algorithm in ("expv", "krylov_expv"):
+            algorithm = ExpvAlgorithm()
+        else:
+            raise PiArgumentError("the CUDA backend propagates with algorithm=:expv (ExpvAlgorithm)")
+    if not isinstance(algorithm, ExpvAlgorithm):
+        raise PiArgumentError("algorithm must be :expv or an ExpvAlgorithm")
+    compiled = _as_compiled(x)
+    if rho0.basis.N != compiled.basis.N or rho0.basis.sectors != compiled.basis.sectors:
+        raise PiArgumentError("Liouvillian source and initial state use incompatible PI bases")
+    if observables is None and not save_states:
+        raise PiArgumentError("save_states=false requires at least one observable")
+    ts = saved_times(tspan, saveat)
+    lib = _lib.load()
+    n = len(compiled.basis)
+    xd = torch.from_numpy(np.ascontiguousarray(rho0.data)).cuda()
+    names = []
+    obs_dev = None
+    if observables:
+        items = observables.items() if isinstance(observables, dict) else (
+            [("observable", observables)] if not isinstance(observables, (list, tuple)) else observables)
+        datas = []
+        for k, v in items:
+            names.append(k)
+            datas.append(_observable_data(compiled.basis, v))
+        obs_dev = torch.from_numpy(np.ascontiguousarray(np.stack(datas))).cuda()
+    nobs = len(names)
+    o = algorithm.opts()
+    info = _lib.pi_expv_info_t()
+    torch.cuda.synchronize()
+    if not save_states:
+        times = np.array(ts, dtype=np.float64)
+        vals = np.zeros((len(ts), max(nobs, 1), 2), dtype=np.float64)
+        _lib.check(lib.pi_solve_dynamics(compiled.handle, _ptr(xd), len(ts), _lib.dptr(times), nobs,
+                                         _ptr(obs_dev) if obs_dev is not None else None, _lib.dptr(vals),
+                                         C.byref(o), C.byref(info)), "solve_dynamics")
+        values = {k: vals[:, i, 0] + 1j * vals[:, i, 1] for i, k in enumerate(names)}
+        return DynamicsStreamResult(ts, None, values)
+    states = [rho0.copy()]
+    series = {k: [] for k in names}
+
+    def record(state_dev):
+        # dot(op.data, rho.data) on the device (highlevel.jl:672-677)
+        out = np.zeros(2, dtype=np.float64)
+        for i, k in enumerate(names):
+            _lib.check(lib.pi_dot_f64(compiled.handle, _ptr(obs_dev[i]), _ptr(state_dev), _lib.dptr(out)),
+                       "observable")
+            series[k].append(complex(out[0], out[1]))
+
+    record(xd)
+    for i in range(1, len(ts)):
+        dt = ts[i] - ts[i - 1]
+        if dt != 0:
+            torch.cuda.synchronize()
+            _lib.check(lib.pi_expv(compiled.handle, _ptr(xd), dt, C.byref(o), C.byref(info)), "solve_dynamics")
+        states.append(PIState(compiled.basis, xd.cpu().numpy()))
+        record(xd)
+    if nobs:
+        return DynamicsStreamResult(ts, states, {k: np.array(v) for k, v in series.items()})
+    return DynamicsResult(ts, states)

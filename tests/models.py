@@ -1,0 +1,54 @@
+"""Model cases built twice: once for libpicuda (picuda) and once for the oracle."""
+import numpy as np
+
+import picuda
+from oracle import pi_oracle as O
+
+KIND_NAMES = {0: "H", 1: "LJ", 2: "CJ"}
+
+
+def to_oracle(model: "picuda.PIModel") -> "O.PIModel":
+    b = O.PIBasis(model.basis.N, 2, sectors=model.basis.sectors)
+    terms = [O.Term(KIND_NAMES[t.kind], t.operator, t.rate, t.hbar) for t in model.terms]
+    return O.PIModel(b, terms)
+
+
+def driven_c1(N=8):
+    """Driven qubits, H = Omega Jx, local decay 0.5 (the N=8 CPU-runnable configuration)."""
+    return picuda.Models.driven_qubits(N, drive=1.0, emission=0.5, pumping=0.0)
+
+
+def ensemble_c2(N=120):
+    """H = 0.3 Jz + 1.2 Jx, local decay 0.2, local dephasing 0.1, collective decay 0.05/N."""
+    s = picuda.spin_matrices(2)
+    return picuda.qubit_ensemble_model(N, hamiltonian=0.3 * s["jz"] + 1.2 * s["jx"], emission=0.2,
+                                       dephasing=0.1, collective_emission=0.05 / N)
+
+
+def btc_c3(N=200, omega_over_kappa=1.0):
+    """Boundary-time-crystal-like model on all sectors: H = Omega Jx, collective decay 1/N,
+    local dephasing 0.01, Omega = omega_over_kappa * kappa."""
+    s = picuda.spin_matrices(2)
+    kappa = 1.0 / N
+    return picuda.qubit_ensemble_model(N, hamiltonian=omega_over_kappa * kappa * s["jx"],
+                                       collective_emission=kappa, dephasing=0.01)
+
+
+def general(N=6, seed=0, sectors=None):
+    """Random complex one-body operators for every supported term kind."""
+    rng = np.random.default_rng(seed)
+    b = picuda.PIBasis(N, 2, sectors=sectors)
+    h = rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))
+    h = (h + h.conj().T) / 2
+    L1 = rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))
+    L2 = rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))
+    L3 = rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))
+    return picuda.PIModel(b, [picuda.CollectiveHamiltonian(h, rate=0.7, hbar=1.3),
+                              picuda.LocalJump(L1, rate=0.3), picuda.CollectiveJump(L2, rate=0.2),
+                              picuda.LocalJump(L3, rate=0.11),
+                              picuda.LocalHamiltonian(0.5 * (h + h.T.conj()), rate=0.4)])
+
+
+def random_state_vector(n, seed):
+    rng = np.random.default_rng(seed)
+    return (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)

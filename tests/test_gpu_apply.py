@@ -1,0 +1,151 @@
+"""GPU parity of the fused Schur-block apply (libpicuda, sm_103a) against the oracle."""
+import numpy as np
+import pytest
+
+import picuda
+from oracle import pi_oracle as O
+from tests import models as M
+
+pytestmark = pytest.mark.gpu
+
+# Plain FP64 path: relative error bound against the oracle (max |dy| / max |y|).
+TOL_F64 = 1e-12
+# FP32 apply: FP32 rounding of ~15 accumulated terms.
+TOL_F32 = 2e-6
+
+
+@pytest.fixture(scope="module")
+def torch_cuda(lib_built):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _dev(torch, a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return t if dtype is None else t.to(dtype)
+
+
+def _apply64(torch, compiled, x):
+    xd = _dev(torch, x)
+    yd = torch.empty_like(xd)
+    picuda.apply_(yd, compiled, xd)
+    torch.cuda.synchronize()
+    return yd.cpu().numpy()
+
+
+CASES = [
+    ("driven_c1_N8", lambda: M.driven_c1(8)),
+    ("general_N1", lambda: M.general(1, 1)),
+    ("general_N6", lambda: M.general(6, 4)),
+    ("general_N33", lambda: M.general(33, 8)),
+    ("general_N8_restricted", lambda: M.general(8, 6, sectors=[(8, 0), (6, 2), (4, 4)])),
+    ("ensemble_c2_N40", lambda: M.ensemble_c2(40)),
+    ("btc_c3_N65", lambda: M.btc_c3(65, 0.5)),
+    ("btc_symmetric_N50", lambda: picuda.Models.boundary_time_crystal(50)),
+]
+
+
+@pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
+def test_apply_f64_matches_oracle(torch_cuda, name, make):
+    model = make()
+    compiled = picuda.compile(model)
+    oplan = O.Plan(M.to_oracle(model))
+    for seed in range(2):
+        x = M.random_state_vector(len(model.basis), seed)
+        y = _apply64(torch_cuda, compiled, x)
+        ref = O.apply(oplan, x)
+        assert np.abs(y - ref).max() <= TOL_F64 * np.abs(ref).max(), name
+
+
+@pytest.mark.parametrize("N,make", [(120, M.ensemble_c2), (200, M.btc_c3)], ids=["c2_N120", "c3_N200"])
+def test_apply_f64_full_size(torch_cuda, N, make):
+    model = make(N)
+    compiled = picuda.compile(model)
+    oplan = O.Plan(M.to_oracle(model))
+    x = M.random_state_vector(len(model.basis), 11)
+    y = _apply64(torch_cuda, compiled, x)
+    ref = O.apply(oplan, x)
+    assert np.abs(y - ref).max() <= TOL_F64 * np.abs(ref).max()
+    # trace preservation: t^H (L x) = 0 for every x (liouvillian property tests)
+    idx, val = compiled.library_trace_functional()
+    assert abs(np.sum(val * y[idx])) <= 1e-11 * np.sum(np.abs(val * y[idx]))
+
+
+def test_apply_multi_rhs_and_determinism(torch_cuda):
+    torch = torch_cuda
+    model = M.ensemble_c2(30)
+    compiled = picuda.compile(model)
+    n = len(model.basis)
+    X = np.stack([M.random_state_vector(n, s) for s in range(3)])
+    Xd = _dev(torch, X)
+    Yd = torch.empty_like(Xd)
+    picuda.apply_(Yd, compiled, Xd)
+    Y2 = torch.empty_like(Xd)
+    picuda.apply_(Y2, compiled, Xd)
+    torch.cuda.synchronize()
+    assert torch.equal(Yd, Y2), "apply must be bitwise deterministic"
+    for c in range(3):
+        assert np.array_equal(Yd[c].cpu().numpy(), _apply64(torch, compiled, X[c]))
+    # host-buffer path (H2D + apply + D2H) gives the same bits
+    yh = np.empty_like(X[0])
+    picuda.apply_(yh, compiled, X[0].copy())
+    assert np.array_equal(yh, Yd[0].cpu().numpy())
+
+
+def test_apply_rejects_aliasing_and_bad_shapes(torch_cuda):
+    torch = torch_cuda
+    compiled = picuda.compile(M.driven_c1(4))
+    n = len(compiled.basis)
+    x = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.apply_(x, compiled, x)
+    with pytest.raises(picuda.PiDimensionMismatch):
+        picuda.apply_(torch.zeros(n + 1, dtype=torch.complex128, device="cuda"), compiled,
+                      torch.zeros(n + 1, dtype=torch.complex128, device="cuda"))
+
+
+@pytest.mark.parametrize("N,make", [(40, M.ensemble_c2), (120, M.ensemble_c2), (200, M.btc_c3)])
+def test_apply_f32_both_coordinates(torch_cuda, N, make):
+    torch = torch_cuda
+    model = make(N)
+    compiled = picuda.compile(model)
+    oplan = O.Plan(M.to_oracle(model))
+    n = len(model.basis)
+    x = M.random_state_vector(n, 5)
+    ref = O.apply(oplan, x)
+    # reference coordinates
+    xd = _dev(torch, x, torch.complex64)
+    yd = torch.empty_like(xd)
+    picuda.apply_(yd, compiled, xd, precision="fp32", coords="reference")
+    torch.cuda.synchronize()
+    y = yd.cpu().numpy().astype(np.complex128)
+    assert np.abs(y - ref).max() <= TOL_F32 * np.abs(ref).max()
+    # population coordinates z = sqrt(f) x: feed z, compare sqrt(f) * (L x)
+    scales = compiled.sector_scales()
+    w = np.concatenate([np.full(d * d, s) for d, s in zip(model.basis.dims, scales)])
+    z = M.random_state_vector(n, 6)
+    xz = z / w
+    refz = w * O.apply(oplan, xz)
+    zd = _dev(torch, z, torch.complex64)
+    yz = torch.empty_like(zd)
+    picuda.apply_(yz, compiled, zd, precision="fp32", coords="population")
+    torch.cuda.synchronize()
+    out = yz.cpu().numpy().astype(np.complex128)
+    assert np.abs(out - refz).max() <= TOL_F32 * np.abs(refz).max()
+
+
+def test_library_basis_maps_bit_exact(torch_cuda):
+    for N in (8, 120):
+        compiled = picuda.compile(M.ensemble_c2(N))
+        ob = O.PIBasis(N, 2)
+        ks, offs, dims = compiled.library_sectors()
+        assert [(N - k, k) for k in ks] == ob.sectors
+        assert list(offs) == ob.offsets[:-1]
+        assert list(dims) == [len(p) for p in ob.patterns]
+        for s in (0, len(ks) // 2, len(ks) - 1):
+            assert [tuple(r) for r in compiled.library_patterns(s)] == ob.patterns[s]
+        idx, val = compiled.library_trace_functional()
+        oidx, oval = O.trace_functional(ob)
+        assert np.array_equal(idx, oidx) and np.array_equal(val, oval.real)

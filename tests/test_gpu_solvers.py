@@ -1,0 +1,122 @@
+"""GPU Krylov solvers (steady-state GMRES, expv dynamics) against the oracle and known answers."""
+import math
+
+import numpy as np
+import pytest
+import scipy.linalg as sla
+
+import picuda
+from oracle import pi_oracle as O
+from tests import models as M
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda(lib_built):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def test_steady_state_fp64_matches_oracle_c1(torch_cuda):
+    model = M.driven_c1(8)
+    oplan = O.Plan(M.to_oracle(model))
+    x_ref, info_ref = O.krylov_steady_state(oplan)
+    res = picuda.stationary_state(model, algorithm=picuda.GMRESAlgorithm(), return_info=True,
+                                  operator_scale=info_ref["operator_scale"])
+    assert res.info["converged"]
+    assert res.info["trace_error"] <= 1e-10 + 1e-8
+    assert np.abs(res.state.data - x_ref).max() <= 1e-8 * np.abs(x_ref).max()
+    # the scale estimate itself (own RNG) agrees to tolerance
+    res2 = picuda.stationary_state(model, return_info=True)
+    assert res2.info["operator_scale"] == pytest.approx(info_ref["operator_scale"], rel=0.3)
+    assert np.abs(res2.state.data - x_ref).max() <= 1e-7 * np.abs(x_ref).max()
+
+
+def test_steady_state_known_answer_pump_decay(torch_cuda):
+    """Local pump-decay product steady state (test_published_models.jl:432-447)."""
+    model = picuda.Models.local_pump_decay(4, down=1.0, up=0.3)
+    rho = picuda.stationary_state(model)
+    exc = picuda.collective_operator(model.basis, np.array([[0, 0], [0, 1]]))
+    assert picuda.expectation(exc, rho).real == pytest.approx(4 * 0.3 / 1.3, abs=2e-9)
+    tr = picuda.expectation(picuda.collective_operator(model.basis, np.eye(2)) , rho).real / 4
+    assert tr == pytest.approx(1.0, abs=1e-9)
+
+
+@pytest.mark.parametrize("N", [12, 40])
+def test_steady_state_mixed_matches_fp64(torch_cuda, N):
+    model = M.btc_c3(N, 1.0)
+    r64 = picuda.stationary_state(model, algorithm=picuda.GMRESAlgorithm(krylovdim=50, maxiter=5000),
+                                  return_info=True)
+    rmx = picuda.stationary_state(model, algorithm=picuda.GMRESAlgorithm(krylovdim=50, maxiter=5000,
+                                                                          precision="mixed"),
+                                  return_info=True, operator_scale=r64.info["operator_scale"])
+    assert rmx.info["converged"] and rmx.info["refinements"] >= 1
+    tol = 1e-10 + 1e-8 * max(np.linalg.norm(rmx.state.data), 1.0)
+    assert rmx.info["normalized_residual"] <= tol
+    ref = np.abs(r64.state.data).max()
+    assert np.abs(rmx.state.data - r64.state.data).max() <= 1e-6 * ref
+
+
+def test_expv_matches_dense_exponential(torch_cuda):
+    model = M.general(5, 9)
+    oplan = O.Plan(M.to_oracle(model))
+    L = O.materialize(oplan)
+    b = picuda.iid_pure_state(model.basis, np.array([0.6, 0.8j])).data
+    for t in (0.3, 2.0):
+        y, info = picuda.krylov_expv(model, b, t, return_info=True)
+        ref = sla.expm(t * L) @ b
+        assert np.abs(y - ref).max() <= 3e-9 * max(np.abs(ref).max(), 1.0)
+        assert info["converged"] and info["accepted_steps"] >= 1
+
+
+def test_solve_dynamics_c1_matches_oracle(torch_cuda):
+    """Driven qubits N=8: expv over [0, 4], saveat 0.1, m = 30, tol 1e-10, observables."""
+    model = M.driven_c1(8)
+    b = model.basis
+    rho0 = picuda.computational_product_state(b, 2)
+    s = picuda.spin_matrices(2)
+    obs = {"excited": s["jp"] @ s["jm"], "Jz": s["jz"]}
+    alg = picuda.ExpvAlgorithm(krylovdim=30, atol=1e-10)
+    res = picuda.solve_dynamics(model, rho0, (0.0, 4.0), algorithm=alg, saveat=0.1, observables=obs,
+                                save_states=False)
+    oplan = O.Plan(M.to_oracle(model))
+    ob = oplan.basis
+    oobs = {k: O.collective_operator(ob, v) for k, v in obs.items()}
+    ref = O.solve_dynamics_expv(oplan, O.computational_product_state(ob, 2), (0.0, 4.0), saveat=0.1,
+                                observables=oobs, atol=1e-10, save_states=False)
+    assert len(res.t) == 41 and np.allclose(res.t, ref["t"])
+    for k in obs:
+        assert np.abs(res.values[k] - ref["values"][k]).max() <= 1e-8 * max(1.0, np.abs(ref["values"][k]).max())
+    # excited population starts at N
+    assert res.values["excited"][0].real == pytest.approx(8.0)
+    # the saved-state variant agrees with the streamed one
+    res2 = picuda.solve_dynamics(model, rho0, (0.0, 4.0), algorithm=alg, saveat=0.1, observables=obs)
+    assert np.abs(res2.values["Jz"] - res.values["Jz"]).max() <= 1e-12 * 8
+
+
+def test_dephasing_coherence_law(torch_cuda):
+    """Independent dephasing: <Sx> = N/2 exp(-gamma t) (test_published_models.jl:432-438)."""
+    for N in (1, 3, 5, 30):
+        model = picuda.Models.independent_dephasing(N, gamma=0.4)
+        rho0 = picuda.iid_pure_state(model.basis, np.array([1, 1]) / math.sqrt(2))
+        sx = np.array([[0, 1], [1, 0]]) / 2
+        res = picuda.solve_dynamics(model, rho0, (0.0, 0.8), saveat=[0.0, 0.2, 0.8], observables={"sx": sx},
+                                    save_states=False)
+        for t, v in zip(res.t, res.values["sx"]):
+            assert v.real == pytest.approx(N / 2 * math.exp(-0.4 * t), abs=2e-9 * N)
+
+
+def test_expv_mixed_vs_fp64_c2_small(torch_cuda):
+    model = M.ensemble_c2(40)
+    rho0 = picuda.computational_product_state(model.basis, 2)
+    s = picuda.spin_matrices(2)
+    obs = {"Jz": s["jz"], "JpJm": s["jp"] @ s["jm"]}
+    kw = dict(saveat=0.5, observables=obs, save_states=False)
+    r64 = picuda.solve_dynamics(model, rho0, (0.0, 2.0), algorithm=picuda.ExpvAlgorithm(), **kw)
+    rmx = picuda.solve_dynamics(model, rho0, (0.0, 2.0), algorithm=picuda.ExpvAlgorithm(precision="mixed"), **kw)
+    for k in obs:
+        err = np.abs(rmx.values[k] - r64.values[k]).max() / np.abs(r64.values[k]).max()
+        assert err <= 1e-4, (k, err)
