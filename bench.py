@@ -41,6 +41,59 @@ def model_c2(picuda, N=N_QUBITS):
                                        dephasing=0.1, collective_emission=0.05 / N)
 
 
+def to_oracle(model):
+    """The same model for the CPU oracle (checker / CPU baseline only)."""
+    from oracle import pi_oracle as O
+    names = {0: "H", 1: "LJ", 2: "CJ"}
+    b = O.PIBasis(model.basis.N, 2, sectors=model.basis.sectors)
+    return O.PIModel(b, [O.Term(names[t.kind], t.operator, t.rate, t.hbar) for t in model.terms])
+
+
+def solve_rates(picuda, torch):
+    """Solves/s of the reference's Krylov methods, plain FP64 vs mixed precision.
+
+    steady state: driven qubits N=20 (H = Jx, local decay 0.5; dim 1771), GMRES(50) to
+    atol 1e-10 / rtol 1e-8 -- the largest size of this family that the reference's
+    unpreconditioned restarted GMRES brings to tolerance;
+    dynamics: the N=120 ensemble, expv m=30 over one dt = 0.05 interval from the
+    all-excited state."""
+    out = {}
+    sm = picuda.spin_matrices(2)
+    ss_model = picuda.Models.driven_qubits(20, drive=1.0, emission=0.5, pumping=0.0)
+    cm = picuda.compile(ss_model)
+    for prec in ("fp64", "mixed"):
+        alg = picuda.GMRESAlgorithm(krylovdim=50, maxiter=5000, precision=prec)
+        r = picuda.stationary_state(cm, algorithm=alg, return_info=True)  # warm
+        times = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            r = picuda.stationary_state(cm, algorithm=alg, return_info=True, operator_scale=r.info["operator_scale"])
+            times.append(time.perf_counter() - t0)
+        out[f"steady_{prec}"] = {"solves_per_s": 1.0 / statistics.median(times),
+                                 "p50_ms": statistics.median(times) * 1e3, "p99_ms": max(times) * 1e3,
+                                 "iterations": r.info["iterations"],
+                                 "normalized_residual": r.info["normalized_residual"],
+                                 "trace_error": r.info["trace_error"]}
+    ref = None
+    c2 = picuda.compile(model_c2(picuda))
+    rho0 = picuda.computational_product_state(c2.basis, 2)
+    obs = {"Jz": sm["jz"], "JpJm": sm["jp"] @ sm["jm"]}
+    for prec in ("fp64", "mixed"):
+        alg = picuda.ExpvAlgorithm(krylovdim=30, precision=prec)
+        times = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            res = picuda.solve_dynamics(c2, rho0, (0.0, 0.05), algorithm=alg, observables=obs, save_states=False)
+            times.append(time.perf_counter() - t0)
+        vals = np.array([res.values[k][-1] for k in obs])
+        if prec == "fp64":
+            ref = vals
+        out[f"expv_{prec}"] = {"intervals_per_s": 1.0 / statistics.median(times),
+                               "p50_ms": statistics.median(times) * 1e3, "p99_ms": max(times) * 1e3,
+                               "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref)))}
+    return out
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -153,11 +206,12 @@ def stencil_flops(picuda, model):
     cost = {(0, 0): 10, (0, 1): 10, (0, 2): 10, (1, 0): 4, (1, 1): 4, (1, 2): 8,
             (2, 0): 4, (2, 1): 4, (2, 2): 8, (3, 0): 5, (3, 1): 14, (3, 2): 14}
     total = 0
-    for s, src, kind, cls, dr, dc, *_ in table:
+    for row in table.tolist():
+        s, src, kind, cls, dr, dc = row[:6]
         n, m = dims[s], dims[src]
         rows = max(0, min(n, m - dr) - max(0, -dr))
         cols = max(0, min(n, m - dc) - max(0, -dc))
-        total += cost[(int(kind), int(cls))] * rows * cols
+        total += cost[(kind, cls)] * rows * cols
     return total
 
 
@@ -188,7 +242,6 @@ def run_reference(args, world, rank):
         return 0
     import picuda
     from oracle import pi_oracle as O
-    from tests.models import to_oracle
     model = model_c2(picuda)
     plan = O.Plan(to_oracle(model))
     from oracle import cpu_baseline
@@ -308,10 +361,11 @@ def main():
     e2e_s = max_over_ranks(e2e_s, world)
     e2e_value = world * bytes32 / e2e_s / 1e9
 
+    solves = solve_rates(picuda, torch) if rank == 0 else None
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import pi_oracle as O
-        from tests.models import to_oracle
         gbs, threads, count, dt = cpu_baseline_apply(O.Plan(to_oracle(model)), n)
         cpu = {"value": gbs, "unit": "GB/s", "cores": threads, "kind": "port",
                "sample": f"{count} FP64 applies of one N=120 state vector in {dt:.1f} s "
@@ -339,6 +393,7 @@ def main():
             "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 8 * n * BATCH,
                     "d2h_bytes_per_step": 8 * n * BATCH, "ms_per_step": e2e_s * 1e3,
                     "call": "pi_apply_host_f32 (pinned host buffers)"},
+            "solves": solves,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": cl,

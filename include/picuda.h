@@ -129,7 +129,8 @@ int pi_sector_multiplicity(int N, int k, double* f, double* sqrt_f);
 /* ---- apply!(y, compiled, x, t, p, work) (liouvillian.jl:4165-4171, :3205-3230) ------ */
 
 /* y = L x for ncols right-hand sides with leading dimension ld (elements), device
- * buffers, complex FP64 reference coordinates.  stream may be NULL (the plan's stream).
+ * buffers, complex FP64 reference coordinates, enqueued on `stream` (a cudaStream_t;
+ * NULL is the CUDA default stream) without synchronizing.
  * Aliasing of x and y is rejected (liouvillian.jl:3220-3221). */
 int pi_apply_f64(pi_plan* plan, double* y_dev, const double* x_dev, int ncols, long long ld,
                  void* stream);

@@ -59,6 +59,10 @@ void free_plan(pi_plan* plan) {
   cudaSetDevice(plan->device);
   if (plan->stream) cudaStreamSynchronize(plan->stream);
   for (void* p : plan->allocations) cudaFree(p);
+  if (plan->stage_x) cudaFree(plan->stage_x);
+  if (plan->stage_y) cudaFree(plan->stage_y);
+  for (auto& ps : plan->pipe)
+    if (ps) cudaStreamDestroy(ps);
   if (plan->host_pinned) cudaFreeHost(plan->host_pinned);
   if (plan->stream) cudaStreamDestroy(plan->stream);
   cudaSetDevice(cur);
@@ -333,6 +337,13 @@ int pi_plan_create(int N, int d, int nsectors, const int* sector_ks, int nterms,
     delete plan;
     return cuda_fail(e, "cudaStreamCreate");
   }
+  for (auto& ps : plan->pipe) {
+    e = cudaStreamCreateWithFlags(&ps, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      free_plan(plan);
+      return cuda_fail(e, "cudaStreamCreate");
+    }
+  }
   int rc = upload_plan(plan);
   if (rc != PI_OK) {
     std::string msg = g_last_error;
@@ -415,7 +426,7 @@ int pi_apply_f64(pi_plan* plan, double* y_dev, const double* x_dev, int ncols, l
   int rc = check_apply_args(plan, y_dev, x_dev, ncols, ld, sizeof(double2));
   if (rc) return rc;
   BorderArgs border{1.0, nullptr, 0};
-  cudaStream_t s = stream ? (cudaStream_t)stream : plan->stream;
+  cudaStream_t s = (cudaStream_t)stream;  // NULL is the CUDA default stream
   cudaError_t e = launch_apply_f64(plan->dev, x_dev, y_dev, ncols, ld, border, s);
   if (e != cudaSuccess) return cuda_fail(e, "apply launch");
   return PI_OK;
@@ -428,7 +439,7 @@ int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, lon
   if (coords != PI_COORDS_REFERENCE && coords != PI_COORDS_POPULATION)
     return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
   BorderArgs border{1.0, nullptr, coords};
-  cudaStream_t s = stream ? (cudaStream_t)stream : plan->stream;
+  cudaStream_t s = (cudaStream_t)stream;  // NULL is the CUDA default stream
   cudaError_t e = launch_apply_f32(plan->dev, x_dev, y_dev, ncols, ld, border, s);
   if (e != cudaSuccess) return cuda_fail(e, "apply launch");
   return PI_OK;
@@ -436,39 +447,62 @@ int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, lon
 
 }  // extern "C"
 
+// Host-buffer apply: the columns are split into chunks that cycle through three streams,
+// so the host-to-device copy of one chunk, the apply of the previous one and the
+// device-to-host copy of the one before overlap on the link and the SMs.  Device staging
+// is grow-only and owned by the plan.
 template <typename T>
 static int apply_host(pi_plan* plan, void* y_host, const void* x_host, int ncols, int coords) {
   if (!plan || !y_host || !x_host) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
   if (ncols < 1 || ncols > 65535) return fail(PI_ERR_INVALID_ARGUMENT, "ncols must lie in 1:65535");
   if (coords != PI_COORDS_REFERENCE && coords != PI_COORDS_POPULATION)
     return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
-  const size_t bytes = (size_t)ncols * (size_t)plan->host.dim * 2 * sizeof(T);
+  const size_t col_bytes = (size_t)plan->host.dim * 2 * sizeof(T);
+  const size_t bytes = (size_t)ncols * col_bytes;
   if (overlap(x_host, bytes, y_host, bytes))
     return fail(PI_ERR_INVALID_ARGUMENT, "source and destination must not share storage");
   BusyGuard guard(plan);
   if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
-  cudaStream_t s = plan->stream;
-  void *dx = nullptr, *dy = nullptr;
-  cudaError_t e = cudaMallocAsync(&dx, bytes, s);
-  if (e != cudaSuccess) return cuda_fail(e, "device allocation");
-  e = cudaMallocAsync(&dy, bytes, s);
-  if (e != cudaSuccess) {
-    cudaFreeAsync(dx, s);
-    cudaStreamSynchronize(s);
-    return cuda_fail(e, "device allocation");
+  cudaError_t e = cudaSuccess;
+  if (plan->stage_bytes < bytes) {
+    if (plan->stage_x) cudaFree(plan->stage_x);
+    if (plan->stage_y) cudaFree(plan->stage_y);
+    plan->stage_x = plan->stage_y = nullptr;
+    plan->stage_bytes = 0;
+    e = cudaMalloc(&plan->stage_x, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&plan->stage_y, bytes);
+    if (e != cudaSuccess) {
+      if (plan->stage_x) cudaFree(plan->stage_x);
+      plan->stage_x = nullptr;
+      return cuda_fail(e, "host-apply staging allocation");
+    }
+    plan->stage_bytes = bytes;
   }
+  // about 8 chunks, each at least 1 column
+  const int chunk = std::max(1, (ncols + 7) / 8);
   BorderArgs border{1.0, nullptr, coords};
-  e = cudaMemcpyAsync(dx, x_host, bytes, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) {
-    if (sizeof(T) == sizeof(double))
-      e = launch_apply_f64(plan->dev, (const double*)dx, (double*)dy, ncols, plan->host.dim, border, s);
-    else
-      e = launch_apply_f32(plan->dev, (const float*)dx, (float*)dy, ncols, plan->host.dim, border, s);
+  int k = 0;
+  for (int c0 = 0; c0 < ncols && e == cudaSuccess; c0 += chunk, ++k) {
+    const int nc = std::min(chunk, ncols - c0);
+    cudaStream_t s = plan->pipe[k % 3];
+    char* dx = (char*)plan->stage_x + (size_t)c0 * col_bytes;
+    char* dy = (char*)plan->stage_y + (size_t)c0 * col_bytes;
+    e = cudaMemcpyAsync(dx, (const char*)x_host + (size_t)c0 * col_bytes, (size_t)nc * col_bytes,
+                        cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      if (sizeof(T) == sizeof(double))
+        e = launch_apply_f64(plan->dev, (const double*)dx, (double*)dy, nc, plan->host.dim, border, s);
+      else
+        e = launch_apply_f32(plan->dev, (const float*)dx, (float*)dy, nc, plan->host.dim, border, s);
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync((char*)y_host + (size_t)c0 * col_bytes, dy, (size_t)nc * col_bytes, cudaMemcpyDeviceToHost, s);
   }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(y_host, dy, bytes, cudaMemcpyDeviceToHost, s);
-  cudaFreeAsync(dx, s);
-  cudaFreeAsync(dy, s);
-  cudaError_t e2 = cudaStreamSynchronize(s);
+  cudaError_t e2 = cudaSuccess;
+  for (auto& ps : plan->pipe) {
+    cudaError_t e3 = cudaStreamSynchronize(ps);
+    if (e3 != cudaSuccess && e2 == cudaSuccess) e2 = e3;
+  }
   if (e != cudaSuccess) return cuda_fail(e, "host apply");
   if (e2 != cudaSuccess) return cuda_fail(e2, "host apply synchronize");
   return PI_OK;

@@ -18,6 +18,11 @@ struct pi_plan {
   int device = 0;
   picuda::ReduceScratch rs;        // reduction scratch (device)
   double* host_pinned = nullptr;   // small pinned staging buffer for reductions
+  // Host-buffer applies: grow-only device staging and copy/compute pipeline streams.
+  void* stage_x = nullptr;
+  void* stage_y = nullptr;
+  size_t stage_bytes = 0;
+  cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
   std::atomic<int> busy{0};
 };
 
