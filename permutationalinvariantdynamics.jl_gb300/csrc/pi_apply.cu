@@ -4,10 +4,15 @@
 // copies every sector into dense scratch (:2952-2958) and runs sparse x dense products for
 // the Hamiltonian commutator, the loss anticommutator and the collective gains plus the
 // support-path sandwich loops of the one-body gains (:2486-2561).  Here every output entry
-// (j, m, m') is produced once by one thread as a gather over the separable stencil terms
-// of its sector: no scratch copies, one read stream of x (neighbouring sectors j +- 1 come
-// from L2) and one write of y.  The same kernel serves the plain FP64 path (reference
-// coordinates) and the FP32 path (population coordinates z = sqrt(f) x).
+// (j, m, m') is produced once, as a gather over the separable stencil terms of its sector:
+// no scratch copies, one read stream of x (the neighbouring sectors j +- 1 are served from
+// L1/L2) and one write of y.
+//
+// Work layout: a block owns a 32 x 32 tile of one sector block; lane = row (coalesced,
+// column-major blocks), warp = 4 consecutive columns.  The sector's terms are staged in
+// shared memory grouped by (kind, class), so each group runs one branch-free loop and the
+// alpha[a] coefficient of a term is reused across the thread's 4 columns.  The same kernel
+// serves the plain FP64 path and the FP32 path (reference or population coordinates).
 #include "pi_device.cuh"
 #include "pi_internal.hpp"
 
@@ -24,70 +29,74 @@ struct Vec2<float> {
   using type = float2;
 };
 
-template <typename T, typename T2>
-__device__ __forceinline__ void accumulate_term(const DevTerm& tm, const T2* __restrict__ coef, int a,
-                                                int b, T2 xv, T& accr, T& acci) {
-  switch (tm.kind) {
-    case 0: {  // ADD: (alpha[a] + beta[b]) x[a, b]
-      T2 al = __ldg(coef + tm.alpha_off + a);
-      T2 be = __ldg(coef + tm.beta_off + b);
-      T cr = al.x + be.x, ci = al.y + be.y;
-      accr = fma(cr, xv.x, accr);
-      accr = fma(-ci, xv.y, accr);
-      acci = fma(cr, xv.y, acci);
-      acci = fma(ci, xv.x, acci);
-      break;
+enum Kind { K_ADD, K_LEFT, K_RIGHT, K_SAND };
+enum Cls { C_RE, C_IM, C_CX };
+
+template <typename T>
+struct Acc {
+  T re[kColsPerThread];
+  T im[kColsPerThread];
+};
+
+// One stencil term for the thread's row a and columns b0 .. b0+3.
+template <typename T, typename T2, int KIND, int CLS>
+__device__ __forceinline__ void term(const DevTerm& tm, const T2* __restrict__ coef, const T2* __restrict__ x, int a,
+                                     int b0, int ncol, Acc<T>& acc) {
+  const int r = a + tm.dr;
+  const bool rv = (unsigned)r < (unsigned)tm.src_n;
+  T2 al;
+  if (KIND != K_RIGHT) al = __ldg(coef + tm.alpha_off + a);
+  const int base = tm.src_off + r + (b0 + tm.dc) * tm.src_n;
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) {
+    if (k >= ncol) break;
+    const int c = b0 + k + tm.dc;
+    const bool v = rv && (unsigned)c < (unsigned)tm.src_n;
+    T2 xv;
+    if (v) {
+      xv = __ldg(x + base + k * tm.src_n);
+    } else {
+      xv.x = 0;
+      xv.y = 0;
     }
-    case 1: {  // LEFT: alpha[a] x[a + dr, b]
-      T2 al = __ldg(coef + tm.alpha_off + a);
-      if (tm.cls == 1) {
-        accr = fma(-al.y, xv.y, accr);
-        acci = fma(al.y, xv.x, acci);
-      } else if (tm.cls == 0) {
-        accr = fma(al.x, xv.x, accr);
-        acci = fma(al.x, xv.y, acci);
-      } else {
-        accr = fma(al.x, xv.x, accr);
-        accr = fma(-al.y, xv.y, accr);
-        acci = fma(al.x, xv.y, acci);
-        acci = fma(al.y, xv.x, acci);
-      }
-      break;
+    T2 be;
+    if (KIND != K_LEFT) be = __ldg(coef + tm.beta_off + b0 + k);
+    T cr, ci;  // combined coefficient
+    if (KIND == K_ADD) {
+      cr = al.x + be.x;
+      ci = al.y + be.y;
+    } else if (KIND == K_LEFT) {
+      cr = al.x;
+      ci = al.y;
+    } else if (KIND == K_RIGHT) {
+      cr = be.x;
+      ci = be.y;
+    } else if (CLS == C_RE) {
+      cr = al.x * be.x;
+      ci = 0;
+    } else {
+      cr = al.x * be.x - al.y * be.y;
+      ci = al.x * be.y + al.y * be.x;
     }
-    case 2: {  // RIGHT: beta[b] x[a, b + dc]
-      T2 be = __ldg(coef + tm.beta_off + b);
-      if (tm.cls == 1) {
-        accr = fma(-be.y, xv.y, accr);
-        acci = fma(be.y, xv.x, acci);
-      } else if (tm.cls == 0) {
-        accr = fma(be.x, xv.x, accr);
-        acci = fma(be.x, xv.y, acci);
-      } else {
-        accr = fma(be.x, xv.x, accr);
-        accr = fma(-be.y, xv.y, accr);
-        acci = fma(be.x, xv.y, acci);
-        acci = fma(be.y, xv.x, acci);
-      }
-      break;
-    }
-    default: {  // SAND: alpha[a] beta[b] x[a + dr, b + dc]
-      T2 al = __ldg(coef + tm.alpha_off + a);
-      T2 be = __ldg(coef + tm.beta_off + b);
-      if (tm.cls == 0) {
-        T c = al.x * be.x;
-        accr = fma(c, xv.x, accr);
-        acci = fma(c, xv.y, acci);
-      } else {
-        T cr = al.x * be.x - al.y * be.y;
-        T ci = al.x * be.y + al.y * be.x;
-        accr = fma(cr, xv.x, accr);
-        accr = fma(-ci, xv.y, accr);
-        acci = fma(cr, xv.y, acci);
-        acci = fma(ci, xv.x, acci);
-      }
-      break;
+    if (CLS == C_RE && KIND != K_ADD) {
+      acc.re[k] = fma(cr, xv.x, acc.re[k]);
+      acc.im[k] = fma(cr, xv.y, acc.im[k]);
+    } else if (CLS == C_IM && KIND != K_ADD) {
+      acc.re[k] = fma(-ci, xv.y, acc.re[k]);
+      acc.im[k] = fma(ci, xv.x, acc.im[k]);
+    } else {
+      acc.re[k] = fma(cr, xv.x, acc.re[k]);
+      acc.re[k] = fma(-ci, xv.y, acc.re[k]);
+      acc.im[k] = fma(cr, xv.y, acc.im[k]);
+      acc.im[k] = fma(ci, xv.x, acc.im[k]);
     }
   }
+}
+
+template <typename T, typename T2, int KIND, int CLS>
+__device__ __forceinline__ void group(const DevTerm* st, int g0, int g1, const T2* __restrict__ coef,
+                                      const T2* __restrict__ x, int a, int b0, int ncol, Acc<T>& acc) {
+  for (int t = g0; t < g1; ++t) term<T, T2, KIND, CLS>(st[t], coef, x, a, b0, ncol, acc);
 }
 
 template <typename T>
@@ -97,33 +106,55 @@ __global__ void __launch_bounds__(kApplyThreads)
             const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ y,
             long long ld, BorderArgs border) {
   using T2 = typename Vec2<T>::type;
+  __shared__ DevTerm st[kMaxSectorTerms];
+  __shared__ int ge[G_COUNT + 1];
   const DevTile tile = tiles[blockIdx.x];
+  const DevSector& sec = sectors[tile.sector];
+  const int tb = sec.term_begin;
+  const int nt = sec.group_end[G_COUNT - 1] - tb;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = terms[tb + i];
+  if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
+  __syncthreads();
   const long long col = blockIdx.y;
   x += col * ld;
   y += col * ld;
-  const DevSector sec = sectors[tile.sector];
-  const int a = tile.a0 + (threadIdx.x & (kTileRows - 1));
-  const int b = tile.b0 + (threadIdx.x / kTileRows);
-  if (a >= sec.n || b >= sec.n) return;
-  T accr = 0, acci = 0;
-  const int tend = sec.term_begin + sec.term_count;
-  for (int t = sec.term_begin; t < tend; ++t) {
-    const DevTerm tm = terms[t];
-    const int r = a + tm.dr, c = b + tm.dc;
-    if (r < 0 || r >= tm.src_n || c < 0 || c >= tm.src_n) continue;
-    const T2 xv = __ldg(x + tm.src_off + r + (long long)c * tm.src_n);
-    accumulate_term<T, T2>(tm, coef, a, b, xv, accr, acci);
+  const int n = sec.n;
+  const int a = tile.a0 + (threadIdx.x & 31);
+  const int b0 = tile.b0 + (threadIdx.x >> 5) * kColsPerThread;
+  if (a >= n || b0 >= n) return;
+  const int ncol = min(kColsPerThread, n - b0);
+  Acc<T> acc;
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
+  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], coef, x, a, b0, ncol, acc);
+  const T scale = (T)border.scale;
+  double2 al = make_double2(0.0, 0.0);
+  double v = 0.0;
+  if (border.alpha != nullptr) {
+    al = border.alpha[col];
+    v = border.coords ? sec.border_z : sec.border_x;
   }
-  T2 out;
-  out.x = (T)border.scale * accr;
-  out.y = (T)border.scale * acci;
-  if (border.alpha != nullptr && a == b) {
-    const double2 al = border.alpha[col];
-    const double v = border.coords ? sec.border_z : sec.border_x;
-    out.x += (T)(al.x * v);
-    out.y += (T)(al.y * v);
+  T2* yp = y + sec.offset + a + (long long)b0 * n;
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) {
+    if (k >= ncol) break;
+    T2 out;
+    out.x = scale * acc.re[k];
+    out.y = scale * acc.im[k];
+    if (b0 + k == a && border.alpha != nullptr) {
+      out.x += (T)(al.x * v);
+      out.y += (T)(al.y * v);
+    }
+    yp[(long long)k * n] = out;
   }
-  y[sec.offset + a + (long long)b * sec.n] = out;
 }
 
 template <typename T>

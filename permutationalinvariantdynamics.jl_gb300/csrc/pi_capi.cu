@@ -89,49 +89,59 @@ int upload_plan(pi_plan* plan) {
   std::vector<DevTile> tiles;
   std::vector<int> diag_sector;
   std::vector<long long> diag_index;
+  auto group_of = [](const StencilTerm& t) -> int {
+    switch (t.kind) {
+      case ST_ADD: return G_ADD;
+      case ST_LEFT: return t.cls == CC_IMAG ? G_LEFT_IM : t.cls == CC_REAL ? G_LEFT_RE : G_LEFT_CX;
+      case ST_RIGHT: return t.cls == CC_IMAG ? G_RIGHT_IM : t.cls == CC_REAL ? G_RIGHT_RE : G_RIGHT_CX;
+      default: return t.cls == CC_REAL ? G_SAND_RE : G_SAND_CX;
+    }
+  };
   for (int s = 0; s < S; ++s) {
     const Sector& sec = hp.sectors[s];
     DevSector& ds = sectors[s];
+    std::memset(&ds, 0, sizeof(ds));
     ds.offset = sec.offset;
     ds.n = sec.n;
     ds.term_begin = (int)terms.size();
-    ds.term_count = (int)sec.terms.size();
-    ds.pad = 0;
     ds.border_x = sec.sqrt_f / hp.trace_norm2;
     ds.border_z = sec.f / hp.trace_norm2;
     ds.sqrt_f = sec.sqrt_f;
-    for (const StencilTerm& t : sec.terms) {
-      DevTerm dt;
-      const Sector& src = hp.sectors[t.src];
-      dt.src_off = src.offset;
-      dt.src_n = src.n;
-      dt.kind = t.kind;
-      dt.cls = t.cls;
-      dt.dr = t.e + t.p;
-      dt.dc = t.e + t.q;
-      dt.pad = 0;
-      const double ratio = sec.sqrt_f / src.sqrt_f;  // population-coordinate rescaling
-      dt.alpha_off = -1;
-      dt.beta_off = -1;
-      if (!t.alpha.empty()) {
-        dt.alpha_off = (int)coef64.size();
-        for (const auto& z : t.alpha) {
-          coef64.push_back(make_double2(z.real(), z.imag()));
-          coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
-          coef32z.push_back(make_float2((float)(z.real() * ratio), (float)(z.imag() * ratio)));
+    if ((int)sec.terms.size() > kMaxSectorTerms)
+      return fail(PI_ERR_UNSUPPORTED, "a sector has more stencil terms than the apply kernel stages");
+    for (int g = 0; g < G_COUNT; ++g) {
+      for (const StencilTerm& t : sec.terms) {
+        if (group_of(t) != g) continue;
+        DevTerm dt;
+        const Sector& src = hp.sectors[t.src];
+        dt.src_off = (int)src.offset;
+        dt.src_n = src.n;
+        dt.dr = t.e + t.p;
+        dt.dc = t.e + t.q;
+        const double ratio = sec.sqrt_f / src.sqrt_f;  // population-coordinate rescaling
+        dt.alpha_off = -1;
+        dt.beta_off = -1;
+        if (!t.alpha.empty()) {
+          dt.alpha_off = (int)coef64.size();
+          for (const auto& z : t.alpha) {
+            coef64.push_back(make_double2(z.real(), z.imag()));
+            coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
+            coef32z.push_back(make_float2((float)(z.real() * ratio), (float)(z.imag() * ratio)));
+          }
         }
-      }
-      if (!t.beta.empty()) {
-        dt.beta_off = (int)coef64.size();
-        for (const auto& z : t.beta) {
-          // ratio is applied once, on alpha (or on beta for a RIGHT term, which has no alpha)
-          const double r = t.alpha.empty() ? ratio : 1.0;
-          coef64.push_back(make_double2(z.real(), z.imag()));
-          coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
-          coef32z.push_back(make_float2((float)(z.real() * r), (float)(z.imag() * r)));
+        if (!t.beta.empty()) {
+          dt.beta_off = (int)coef64.size();
+          for (const auto& z : t.beta) {
+            // ratio is applied once, on alpha (or on beta for a RIGHT term, which has no alpha)
+            const double r = t.alpha.empty() ? ratio : 1.0;
+            coef64.push_back(make_double2(z.real(), z.imag()));
+            coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
+            coef32z.push_back(make_float2((float)(z.real() * r), (float)(z.imag() * r)));
+          }
         }
+        terms.push_back(dt);
       }
-      terms.push_back(dt);
+      ds.group_end[g] = (int)terms.size();
     }
     for (int a0 = 0; a0 < sec.n; a0 += kTileRows)
       for (int b0 = 0; b0 < sec.n; b0 += kTileCols) tiles.push_back(DevTile{s, a0, b0, 0});
@@ -165,7 +175,7 @@ int upload_plan(pi_plan* plan) {
   plan->rs.rresult = (double*)plan_alloc(plan, sizeof(double) * 16);
   if (!plan->rs.partial || !plan->rs.result || !plan->rs.rpartial || !plan->rs.rresult)
     return fail(PI_ERR_OUT_OF_MEMORY, "device allocation of reduction scratch failed");
-  cudaError_t e = cudaMallocHost((void**)&plan->host_pinned, sizeof(double) * 4 * kMaxDots);
+  cudaError_t e = cudaMallocHost((void**)&plan->host_pinned, sizeof(double) * 8 * kMaxDots);
   if (e != cudaSuccess) return cuda_fail(e, "pinned staging allocation");
   return PI_OK;
 }

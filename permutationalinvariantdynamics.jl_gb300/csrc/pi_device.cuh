@@ -6,32 +6,46 @@
 
 namespace picuda {
 
+// Stencil term groups, in the order the apply kernel walks them: every group runs one
+// branch-free code path (kind = how the separable coefficient combines, class = whether it
+// is real, imaginary or complex).
+enum TermGroup : int {
+  G_ADD = 0,      // (alpha[a] + beta[b]) x[a, b]
+  G_LEFT_IM,      // i Im(alpha[a]) x[a + dr, b]
+  G_LEFT_RE,      // Re(alpha[a]) x[a + dr, b]
+  G_LEFT_CX,      // alpha[a] x[a + dr, b]
+  G_RIGHT_IM,     // i Im(beta[b]) x[a, b + dc]
+  G_RIGHT_RE,
+  G_RIGHT_CX,
+  G_SAND_RE,      // Re(alpha[a]) Re(beta[b]) x[a + dr, b + dc]
+  G_SAND_CX,      // alpha[a] beta[b] x[a + dr, b + dc]
+  G_COUNT
+};
+
 // One output sector of the stencil plan.
 struct DevSector {
   long long offset;    // 0-based element offset of the column-major block
   int n;               // block dimension
-  int term_begin;      // first stencil term
-  int term_count;      // number of stencil terms
+  int term_begin;      // first stencil term (terms are stored group by group)
+  int group_end[G_COUNT];  // absolute end index of each group
   int pad;
   double border_x;     // normalized trace vector v = t/|t|^2 on the diagonal, x coordinates
   double border_z;     // the same vector in population coordinates (f / |t|^2)
   double sqrt_f;       // sqrt(f^nu): z = sqrt_f * x
 };
 
-// One separable stencil term (see pi_plan.hpp).
+// One separable stencil term (see pi_plan.hpp); its group fixes kind and class.
 struct DevTerm {
-  long long src_off;   // block offset of the source sector
+  int src_off;         // block offset of the source sector (PI dimension < 2^31)
   int src_n;           // block dimension of the source sector
-  int kind;            // 0 ADD, 1 LEFT, 2 RIGHT, 3 SAND
-  int cls;             // 0 real, 1 imaginary, 2 complex combined coefficient
   int dr;              // row offset into the source block: e + p
   int dc;              // column offset into the source block: e + q
-  int alpha_off;       // offset of alpha[0..n) in the coefficient pool
-  int beta_off;        // offset of beta[0..n) in the coefficient pool
-  int pad;
+  int alpha_off;       // offset of alpha[0..n) in the coefficient pool (-1: unused)
+  int beta_off;        // offset of beta[0..n) in the coefficient pool (-1: unused)
 };
 
-// Output tile: 32 rows x TILE_COLS columns of one sector block.
+// Output tile: 32 rows x 32 columns of one sector block; each of the 8 warps owns 4
+// consecutive columns and each lane one row.
 struct DevTile {
   int sector;
   int a0;
@@ -40,8 +54,11 @@ struct DevTile {
 };
 
 constexpr int kTileRows = 32;
-constexpr int kTileCols = 8;
-constexpr int kApplyThreads = kTileRows * kTileCols;
+constexpr int kColsPerThread = 4;
+constexpr int kApplyWarps = 8;
+constexpr int kTileCols = kColsPerThread * kApplyWarps;
+constexpr int kApplyThreads = 32 * kApplyWarps;
+constexpr int kMaxSectorTerms = 128;  // stencil terms of one sector staged in shared memory
 
 // Trace-border epilogue: y = scale * (L x) + border ? alpha * v : 0, where alpha is a
 // device scalar t^H x computed beforehand (krylov.jl:855-860).

@@ -89,21 +89,21 @@ struct ExpvWork {
   }
   size_t esz() const { return mixed ? sizeof(float2) : sizeof(double2); }
   void* col(int j) const { return (char*)V + (size_t)j * (size_t)n * esz(); }
-  // w = L V_j ; returns |w|
-  double apply_col(int j) {
+  // w = L V_j; |w|^2 goes to rresult[1] and is read back with the next orthogonalization
+  void apply_col(int j) {
     BorderArgs b{1.0, nullptr, mixed ? 1 : 0};
     if (mixed) {
       chk(launch_apply_f32(p->dev, (const float*)col(j), (float*)w, 1, n, b, s));
-      chk(norm2_f32((const float2*)w, n, p->rs, 0, s));
+      chk(norm2_f32((const float2*)w, n, p->rs, 1, s));
     } else {
       chk(launch_apply_f64(p->dev, (const double*)col(j), (double*)w, 1, n, b, s));
-      chk(norm2_f64((const double2*)w, n, p->rs, 0, s));
+      chk(norm2_f64((const double2*)w, n, p->rs, 1, s));
     }
     ++applications;
-    return std::sqrt(rresult());
   }
-  // CGS2 of w against V[0..nv): column += h1 + h2, returns |w| after
-  double orthogonalize(int nv, std::vector<cd>& colv) {
+  // CGS2 of w against V[0..nv): column += h1 + h2; returns |w| after and sets *image to
+  // the norm recorded by apply_col.  One synchronization.
+  double orthogonalize(int nv, std::vector<cd>& colv, double* image) {
     if (mixed) {
       chk(mdot_f32((const float2*)V, n, nv, (const float2*)w, n, p->rs, h1, s));
       chk(maxpy_f32((const float2*)V, n, nv, h1, (float2*)w, n, p->rs, -1, s));
@@ -115,12 +115,15 @@ struct ExpvWork {
       chk(mdot_f64((const double2*)V, n, nv, (const double2*)w, n, p->rs, h2, s));
       chk(maxpy_f64((const double2*)V, n, nv, h2, (double2*)w, n, p->rs, 0, s));
     }
-    std::vector<double> a(2 * nv), b(2 * nv);
-    fetch(a.data(), h1, sizeof(double2) * nv);
-    fetch(b.data(), h2, sizeof(double2) * nv);
-    const double r = std::sqrt(rresult());
-    for (int i = 0; i < nv; ++i) colv[i] += cd(a[2 * i], a[2 * i + 1]) + cd(b[2 * i], b[2 * i + 1]);
-    return r;
+    double* hp = p->host_pinned;
+    chk(cudaMemcpyAsync(hp, h1, sizeof(double2) * (kMaxDots + nv), cudaMemcpyDeviceToHost, s));
+    chk(cudaMemcpyAsync(hp + 4 * kMaxDots, p->rs.rresult, sizeof(double) * 2, cudaMemcpyDeviceToHost, s));
+    chk(cudaStreamSynchronize(s));
+    if (!ok()) return 0.0;
+    for (int i = 0; i < nv; ++i)
+      colv[i] += cd(hp[2 * i], hp[2 * i + 1]) + cd(hp[2 * (kMaxDots + i)], hp[2 * (kMaxDots + i) + 1]);
+    if (image) *image = std::sqrt(hp[4 * kMaxDots + 1]);
+    return std::sqrt(hp[4 * kMaxDots]);
   }
   // V_j = src / scale (src is w or, for j = 0, the FP64 current state)
   void set_col_from_w(int j, double scale) {
@@ -170,8 +173,10 @@ Factorization arnoldi(ExpvWork& W) {
   bool exact = false, near = false;
   const double breakfactor = std::sqrt(std::numeric_limits<double>::epsilon());
   for (int j = 0; j < m && W.ok(); ++j) {
-    const double image = W.checked(W.apply_col(j), "exponential-action Arnoldi image");
-    const double rem = W.checked(W.orthogonalize(j + 1, H[j]), "exponential-action Arnoldi remainder");
+    W.apply_col(j);
+    double image = 0.0;
+    const double rem = W.checked(W.orthogonalize(j + 1, H[j], &image), "exponential-action Arnoldi remainder");
+    W.checked(image, "exponential-action Arnoldi image");
     H[j][j + 1] = rem;
     k = j + 1;
     if (rem == 0.0 || (long long)(j + 1) == W.n) {
@@ -190,9 +195,11 @@ Factorization arnoldi(ExpvWork& W) {
   if (!exact && near) {
     f.enlarged = true;
     f.used += 1;
-    W.checked(W.apply_col(q - 1), "exponential-action enlarged Arnoldi image");
+    W.apply_col(q - 1);
     std::vector<cd> extra(q, cd(0, 0));
-    f.next_remainder = W.checked(W.orthogonalize(q, extra), "exponential-action enlarged Arnoldi remainder");
+    double image = 0.0;
+    f.next_remainder = W.checked(W.orthogonalize(q, extra, &image), "exponential-action enlarged Arnoldi remainder");
+    W.checked(image, "exponential-action enlarged Arnoldi image");
     for (int i = 0; i < q; ++i) f.S(i, q - 1) += extra[i];
   }
   f.k = k;
@@ -217,7 +224,6 @@ double project(ExpvWork& W, const Factorization& f, double h) {
     c[i] = make_double2(v.real(), v.imag());
   }
   W.chk(cudaMemcpyAsync(W.coef, c.data(), sizeof(double2) * f.coeff_count, cudaMemcpyHostToDevice, W.s));
-  W.chk(cudaStreamSynchronize(W.s));
   W.combine(f.coeff_count);
   if (f.completed) return 0.0;
   if (f.enlarged) return f.beta * std::abs(h) * f.next_remainder * std::abs(E(f.q - 1, 0));
@@ -354,8 +360,8 @@ bool alloc_work(ExpvWork& W, Bufs& B) {
   W.w = B.get(e * (size_t)W.n);
   W.cur = (double2*)B.get(sizeof(double2) * W.n);
   W.trial = (double2*)B.get(sizeof(double2) * W.n);
-  W.h1 = (double2*)B.get(sizeof(double2) * kMaxDots);
-  W.h2 = (double2*)B.get(sizeof(double2) * kMaxDots);
+  W.h1 = (double2*)B.get(sizeof(double2) * 2 * kMaxDots);  // h2 follows h1 contiguously
+  W.h2 = W.h1 ? W.h1 + kMaxDots : nullptr;
   W.coef = (double2*)B.get(sizeof(double2) * kMaxDots);
   return B.err == cudaSuccess;
 }

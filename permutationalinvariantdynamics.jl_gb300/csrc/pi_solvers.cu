@@ -122,6 +122,23 @@ inline int grid_n(long long n) {
 
 // One CGS2 orthogonalisation of w against V[0..nv) (FP64): H column += h1 + h2 and
 // *rem2 = |w|^2 after both passes.
+template <typename VT>
+void cgs2_fetch(Run& R, int nv, double2* h1d, std::vector<cd>& hcol, double* rem2) {
+  // h1 and h2 are contiguous (h2 = h1 + kMaxDots); one pinned copy of both plus the
+  // remainder norm, then a single synchronization.
+  pi_plan* p = R.p;
+  double* hp = p->host_pinned;
+  R.chk(cudaMemcpyAsync(hp, h1d, sizeof(double2) * (kMaxDots + nv), cudaMemcpyDeviceToHost, R.s));
+  R.chk(cudaMemcpyAsync(hp + 2 * (2 * kMaxDots), p->rs.rresult, sizeof(double) * 2, cudaMemcpyDeviceToHost, R.s));
+  R.chk(cudaStreamSynchronize(R.s));
+  if (!R.ok()) return;
+  for (int i = 0; i < nv; ++i)
+    hcol[i] += cd(hp[2 * i], hp[2 * i + 1]) + cd(hp[2 * (kMaxDots + i)], hp[2 * (kMaxDots + i) + 1]);
+  *rem2 = hp[4 * kMaxDots];
+}
+
+// One CGS2 orthogonalisation of w against V[0..nv) (FP64): H column += h1 + h2 and
+// *rem2 = |w|^2 after both passes.
 void cgs2_f64(Run& R, const double2* V, int nv, double2* w, double2* h1d, double2* h2d, std::vector<cd>& hcol,
               double* rem2) {
   pi_plan* p = R.p;
@@ -129,13 +146,7 @@ void cgs2_f64(Run& R, const double2* V, int nv, double2* w, double2* h1d, double
   R.chk(maxpy_f64(V, R.n, nv, h1d, w, R.n, p->rs, -1, R.s));
   R.chk(mdot_f64(V, R.n, nv, w, R.n, p->rs, h2d, R.s));
   R.chk(maxpy_f64(V, R.n, nv, h2d, w, R.n, p->rs, 0, R.s));
-  std::vector<double> b1(2 * nv), b2(2 * nv);
-  R.fetch(b1.data(), h1d, sizeof(double2) * nv);
-  R.fetch(b2.data(), h2d, sizeof(double2) * nv);
-  double r2 = 0.0;
-  R.fetch(&r2, p->rs.rresult, sizeof(double));
-  for (int i = 0; i < nv; ++i) hcol[i] += cd(b1[2 * i], b1[2 * i + 1]) + cd(b2[2 * i], b2[2 * i + 1]);
-  *rem2 = r2;
+  cgs2_fetch<double2>(R, nv, h1d, hcol, rem2);
 }
 
 void cgs2_f32(Run& R, const float2* V, int nv, float2* w, double2* h1d, double2* h2d, std::vector<cd>& hcol,
@@ -145,13 +156,7 @@ void cgs2_f32(Run& R, const float2* V, int nv, float2* w, double2* h1d, double2*
   R.chk(maxpy_f32(V, R.n, nv, h1d, w, R.n, p->rs, -1, R.s));
   R.chk(mdot_f32(V, R.n, nv, w, R.n, p->rs, h2d, R.s));
   R.chk(maxpy_f32(V, R.n, nv, h2d, w, R.n, p->rs, 0, R.s));
-  std::vector<double> b1(2 * nv), b2(2 * nv);
-  R.fetch(b1.data(), h1d, sizeof(double2) * nv);
-  R.fetch(b2.data(), h2d, sizeof(double2) * nv);
-  double r2 = 0.0;
-  R.fetch(&r2, p->rs.rresult, sizeof(double));
-  for (int i = 0; i < nv; ++i) hcol[i] += cd(b1[2 * i], b1[2 * i + 1]) + cd(b2[2 * i], b2[2 * i + 1]);
-  *rem2 = r2;
+  cgs2_fetch<float2>(R, nv, h1d, hcol, rem2);
 }
 
 void upper_triangular_solve(const std::vector<std::vector<cd>>& H, const std::vector<cd>& g, int k,
