@@ -9,10 +9,15 @@
 // L1/L2) and one write of y.
 //
 // Work layout: a block owns a 32 x 32 tile of one sector block; lane = row (coalesced,
-// column-major blocks), warp = 4 consecutive columns.  The sector's terms are staged in
-// shared memory grouped by (kind, class), so each group runs one branch-free loop and the
-// alpha[a] coefficient of a term is reused across the thread's 4 columns.  The same kernel
-// serves the plain FP64 path and the FP32 path (reference or population coordinates).
+// column-major blocks), warp = 4 consecutive columns.  The block first stages, for each of
+// the (at most three) source sectors j, j +- 1, the zero-padded 36 x 36 window of x that
+// the tile's stencil reaches, plus the sector's term list grouped by (kind, class); every
+// term then reads shared memory without bounds checks in one branch-free loop per group,
+// and the alpha[a] coefficient of a term is reused across the thread's 4 columns.  The
+// same kernel serves the plain FP64 path and the FP32 path (reference or population
+// coordinates).  TMA is not used for the staging: the reference's packed column-major
+// blocks have odd leading dimensions (n = N - 2k + 1), so FP32 rows are not 16-byte
+// strided as tensor maps require.
 #include "pi_device.cuh"
 #include "pi_internal.hpp"
 
@@ -38,29 +43,19 @@ struct Acc {
   T im[kColsPerThread];
 };
 
-// One stencil term for the thread's row a and columns b0 .. b0+3.
+// One stencil term for the thread's row la and columns lb .. lb+3 of the tile, reading the
+// zero-padded source window in shared memory (no bounds checks).
 template <typename T, typename T2, int KIND, int CLS>
-__device__ __forceinline__ void term(const DevTerm& tm, const T2* __restrict__ coef, const T2* __restrict__ x, int a,
-                                     int b0, int ncol, Acc<T>& acc) {
-  const int r = a + tm.dr;
-  const bool rv = (unsigned)r < (unsigned)tm.src_n;
+__device__ __forceinline__ void term(const DevTerm& tm, const T2* __restrict__ coef, const T2* win, int a,
+                                     int la, int lb, int b0, int nm1, Acc<T>& acc) {
   T2 al;
   if (KIND != K_RIGHT) al = __ldg(coef + tm.alpha_off + a);
-  const int base = tm.src_off + r + (b0 + tm.dc) * tm.src_n;
+  const T2* wp = win + tm.slot * kWinElems + (la + tm.p + kHalo) + (lb + tm.q + kHalo) * kWinRows;
 #pragma unroll
   for (int k = 0; k < kColsPerThread; ++k) {
-    if (k >= ncol) break;
-    const int c = b0 + k + tm.dc;
-    const bool v = rv && (unsigned)c < (unsigned)tm.src_n;
-    T2 xv;
-    if (v) {
-      xv = __ldg(x + base + k * tm.src_n);
-    } else {
-      xv.x = 0;
-      xv.y = 0;
-    }
+    const T2 xv = wp[k * kWinRows];
     T2 be;
-    if (KIND != K_LEFT) be = __ldg(coef + tm.beta_off + b0 + k);
+    if (KIND != K_LEFT) be = __ldg(coef + tm.beta_off + min(b0 + k, nm1));
     T cr, ci;  // combined coefficient
     if (KIND == K_ADD) {
       cr = al.x + be.x;
@@ -94,9 +89,9 @@ __device__ __forceinline__ void term(const DevTerm& tm, const T2* __restrict__ c
 }
 
 template <typename T, typename T2, int KIND, int CLS>
-__device__ __forceinline__ void group(const DevTerm* st, int g0, int g1, const T2* __restrict__ coef,
-                                      const T2* __restrict__ x, int a, int b0, int ncol, Acc<T>& acc) {
-  for (int t = g0; t < g1; ++t) term<T, T2, KIND, CLS>(st[t], coef, x, a, b0, ncol, acc);
+__device__ __forceinline__ void group(const DevTerm* st, int g0, int g1, const T2* __restrict__ coef, const T2* win,
+                                      int a, int la, int lb, int b0, int nm1, Acc<T>& acc) {
+  for (int t = g0; t < g1; ++t) term<T, T2, KIND, CLS>(st[t], coef, win, a, la, lb, b0, nm1, acc);
 }
 
 template <typename T>
@@ -106,42 +101,61 @@ __global__ void __launch_bounds__(kApplyThreads)
             const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ y,
             long long ld, BorderArgs border) {
   using T2 = typename Vec2<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* win = reinterpret_cast<T2*>(smem_raw);  // [3][kWinElems] source windows
   __shared__ DevTerm st[kMaxSectorTerms];
   __shared__ int ge[G_COUNT + 1];
   const DevTile tile = tiles[blockIdx.x];
   const DevSector& sec = sectors[tile.sector];
+  const long long col = blockIdx.y;
+  x += col * ld;
+  y += col * ld;
   const int tb = sec.term_begin;
   const int nt = sec.group_end[G_COUNT - 1] - tb;
   for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = terms[tb + i];
   if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
+  // Stage the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every
+  // source sector (e = -1, 0, +1).
+#pragma unroll 1
+  for (int slot = 0; slot < 3; ++slot) {
+    const int s2 = sec.src[slot];
+    if (s2 < 0) continue;
+    const int m = sectors[s2].n;
+    const T2* xs = x + sectors[s2].offset;
+    const int r0 = tile.a0 + slot - 1 - kHalo, c0 = tile.b0 + slot - 1 - kHalo;
+    T2* w = win + slot * kWinElems;
+    for (int idx = threadIdx.x; idx < kWinElems; idx += blockDim.x) {
+      const int i = idx % kWinRows, j = idx / kWinRows;
+      const int R = r0 + i, C = c0 + j;
+      T2 v;
+      v.x = 0;
+      v.y = 0;
+      if ((unsigned)R < (unsigned)m && (unsigned)C < (unsigned)m) v = __ldg(xs + R + C * m);
+      w[idx] = v;
+    }
+  }
   __syncthreads();
-  const long long col = blockIdx.y;
-  x += col * ld;
-  y += col * ld;
   const int n = sec.n;
-  const int a = tile.a0 + (threadIdx.x & 31);
-  const int b0 = tile.b0 + (threadIdx.x >> 5) * kColsPerThread;
+  const int la = threadIdx.x & 31;
+  const int lb = (threadIdx.x >> 5) * kColsPerThread;
+  const int a = tile.a0 + la;
+  const int b0 = tile.b0 + lb;
   if (a >= n || b0 >= n) return;
   const int ncol = min(kColsPerThread, n - b0);
+  const int nm1 = n - 1;
   Acc<T> acc;
 #pragma unroll
   for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
-  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], coef, x, a, b0, ncol, acc);
-  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], coef, x, a, b0, ncol, acc);
+  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], coef, win, a, la, lb, b0, nm1, acc);
+  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], coef, win, a, la, lb, b0, nm1, acc);
   const T scale = (T)border.scale;
-  double2 al = make_double2(0.0, 0.0);
-  double v = 0.0;
-  if (border.alpha != nullptr) {
-    al = border.alpha[col];
-    v = border.coords ? sec.border_z : sec.border_x;
-  }
   T2* yp = y + sec.offset + a + (long long)b0 * n;
 #pragma unroll
   for (int k = 0; k < kColsPerThread; ++k) {
@@ -150,6 +164,8 @@ __global__ void __launch_bounds__(kApplyThreads)
     out.x = scale * acc.re[k];
     out.y = scale * acc.im[k];
     if (b0 + k == a && border.alpha != nullptr) {
+      const double2 al = border.alpha[col];
+      const double v = border.coords ? sec.border_z : sec.border_x;
       out.x += (T)(al.x * v);
       out.y += (T)(al.y * v);
     }
@@ -162,9 +178,16 @@ cudaError_t launch_apply_t(const DevicePlan& dp, const void* coef, const void* x
                            long long ld, const BorderArgs& border, cudaStream_t stream) {
   using T2 = typename Vec2<T>::type;
   if (dp.ntiles == 0 || ncols == 0) return cudaSuccess;
+  const size_t smem = 3 * kWinElems * sizeof(T2);
+  static bool configured = false;  // per template instance, host side
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(k_apply<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
   dim3 grid((unsigned)dp.ntiles, (unsigned)ncols);
-  k_apply<T><<<grid, kApplyThreads, 0, stream>>>(dp.sectors, dp.terms, (const T2*)coef, dp.tiles,
-                                                 (const T2*)x, (T2*)y, ld, border);
+  k_apply<T><<<grid, kApplyThreads, smem, stream>>>(dp.sectors, dp.terms, (const T2*)coef, dp.tiles,
+                                                    (const T2*)x, (T2*)y, ld, border);
   return cudaGetLastError();
 }
 

@@ -109,15 +109,23 @@ int upload_plan(pi_plan* plan) {
     ds.sqrt_f = sec.sqrt_f;
     if ((int)sec.terms.size() > kMaxSectorTerms)
       return fail(PI_ERR_UNSUPPORTED, "a sector has more stencil terms than the apply kernel stages");
+    ds.src[0] = ds.src[1] = ds.src[2] = -1;
+    for (const StencilTerm& t : sec.terms) {
+      if (t.e < -1 || t.e > 1 || t.p < -kHalo || t.p > kHalo || t.q < -kHalo || t.q > kHalo)
+        return fail(PI_ERR_UNSUPPORTED, "stencil term outside the staged band");
+      if (ds.src[t.e + 1] >= 0 && ds.src[t.e + 1] != t.src)
+        return fail(PI_ERR_UNSUPPORTED, "two source sectors share one index shift");
+      ds.src[t.e + 1] = t.src;
+    }
     for (int g = 0; g < G_COUNT; ++g) {
       for (const StencilTerm& t : sec.terms) {
         if (group_of(t) != g) continue;
         DevTerm dt;
         const Sector& src = hp.sectors[t.src];
-        dt.src_off = (int)src.offset;
-        dt.src_n = src.n;
-        dt.dr = t.e + t.p;
-        dt.dc = t.e + t.q;
+        dt.slot = t.e + 1;
+        dt.p = t.p;
+        dt.q = t.q;
+        dt.pad = 0;
         const double ratio = sec.sqrt_f / src.sqrt_f;  // population-coordinate rescaling
         dt.alpha_off = -1;
         dt.beta_off = -1;

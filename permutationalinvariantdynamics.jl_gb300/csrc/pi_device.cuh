@@ -28,20 +28,21 @@ struct DevSector {
   int n;               // block dimension
   int term_begin;      // first stencil term (terms are stored group by group)
   int group_end[G_COUNT];  // absolute end index of each group
-  int pad;
+  int src[3];          // source sector for index shift e = j_src - j_out = -1, 0, +1 (-1: none)
   double border_x;     // normalized trace vector v = t/|t|^2 on the diagonal, x coordinates
   double border_z;     // the same vector in population coordinates (f / |t|^2)
   double sqrt_f;       // sqrt(f^nu): z = sqrt_f * x
 };
 
-// One separable stencil term (see pi_plan.hpp); its group fixes kind and class.
+// One separable stencil term (see pi_plan.hpp); its group fixes kind and class.  The
+// source entry x_src[a + e + p, b + e + q] is read from the staged window of slot e + 1.
 struct DevTerm {
-  int src_off;         // block offset of the source sector (PI dimension < 2^31)
-  int src_n;           // block dimension of the source sector
-  int dr;              // row offset into the source block: e + p
-  int dc;              // column offset into the source block: e + q
+  int slot;            // e + 1: which staged source window
+  int p;               // row offset within the band, -2..2
+  int q;               // column offset within the band, -2..2
   int alpha_off;       // offset of alpha[0..n) in the coefficient pool (-1: unused)
   int beta_off;        // offset of beta[0..n) in the coefficient pool (-1: unused)
+  int pad;
 };
 
 // Output tile: 32 rows x 32 columns of one sector block; each of the 8 warps owns 4
@@ -59,6 +60,10 @@ constexpr int kApplyWarps = 8;
 constexpr int kTileCols = kColsPerThread * kApplyWarps;
 constexpr int kApplyThreads = 32 * kApplyWarps;
 constexpr int kMaxSectorTerms = 128;  // stencil terms of one sector staged in shared memory
+constexpr int kHalo = 2;                // band half-width of every stencil term
+constexpr int kWinRows = kTileRows + 2 * kHalo;
+constexpr int kWinCols = kTileCols + 2 * kHalo;
+constexpr int kWinElems = kWinRows * kWinCols;
 
 // Trace-border epilogue: y = scale * (L x) + border ? alpha * v : 0, where alpha is a
 // device scalar t^H x computed beforehand (krylov.jl:855-860).
