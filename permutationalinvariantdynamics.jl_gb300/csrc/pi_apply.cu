@@ -43,35 +43,50 @@ struct Acc {
   T im[kColsPerThread];
 };
 
-// One stencil term for the thread's row la and columns lb .. lb+3 of the tile, reading the
-// zero-padded source window in shared memory (no bounds checks).
+// beta[b0 .. b0+3] of one term: b0 and every beta array start are multiples of 4, so the
+// four coefficients are read with aligned vector loads.
+__device__ __forceinline__ void load4(const float2* p, float2 (&v)[4]) {
+  const float4 u0 = __ldg(reinterpret_cast<const float4*>(p));
+  const float4 u1 = __ldg(reinterpret_cast<const float4*>(p) + 1);
+  v[0] = make_float2(u0.x, u0.y);
+  v[1] = make_float2(u0.z, u0.w);
+  v[2] = make_float2(u1.x, u1.y);
+  v[3] = make_float2(u1.z, u1.w);
+}
+__device__ __forceinline__ void load4(const double2* p, double2 (&v)[4]) {
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = __ldg(p + k);
+}
+
+// One stencil term for the thread's row and 4 columns, reading the zero-padded source
+// windows in shared memory (no bounds checks).  ca points at coef + a, cb at coef + b0.
 template <typename T, typename T2, int KIND, int CLS>
-__device__ __forceinline__ void term(const DevTerm& tm, const T2* __restrict__ coef, const T2* win, int a,
-                                     int la, int lb, int b0, int nm1, Acc<T>& acc) {
+__device__ __forceinline__ void term(const int4 tm, const T2* __restrict__ ca, const T2* __restrict__ cb,
+                                     const T2* wbase, Acc<T>& acc) {
   T2 al;
-  if (KIND != K_RIGHT) al = __ldg(coef + tm.alpha_off + a);
-  const T2* wp = win + tm.slot * kWinElems + (la + tm.p + kHalo) + (lb + tm.q + kHalo) * kWinRows;
+  if (KIND != K_RIGHT) al = __ldg(ca + tm.y);
+  T2 be[4];
+  if (KIND != K_LEFT) load4(cb + tm.z, be);
+  const T2* wp = wbase + tm.x;
 #pragma unroll
   for (int k = 0; k < kColsPerThread; ++k) {
     const T2 xv = wp[k * kWinRows];
-    T2 be;
-    if (KIND != K_LEFT) be = __ldg(coef + tm.beta_off + min(b0 + k, nm1));
     T cr, ci;  // combined coefficient
     if (KIND == K_ADD) {
-      cr = al.x + be.x;
-      ci = al.y + be.y;
+      cr = al.x + be[k].x;
+      ci = al.y + be[k].y;
     } else if (KIND == K_LEFT) {
       cr = al.x;
       ci = al.y;
     } else if (KIND == K_RIGHT) {
-      cr = be.x;
-      ci = be.y;
+      cr = be[k].x;
+      ci = be[k].y;
     } else if (CLS == C_RE) {
-      cr = al.x * be.x;
+      cr = al.x * be[k].x;
       ci = 0;
     } else {
-      cr = al.x * be.x - al.y * be.y;
-      ci = al.x * be.y + al.y * be.x;
+      cr = al.x * be[k].x - al.y * be[k].y;
+      ci = al.x * be[k].y + al.y * be[k].x;
     }
     if (CLS == C_RE && KIND != K_ADD) {
       acc.re[k] = fma(cr, xv.x, acc.re[k]);
@@ -89,9 +104,9 @@ __device__ __forceinline__ void term(const DevTerm& tm, const T2* __restrict__ c
 }
 
 template <typename T, typename T2, int KIND, int CLS>
-__device__ __forceinline__ void group(const DevTerm* st, int g0, int g1, const T2* __restrict__ coef, const T2* win,
-                                      int a, int la, int lb, int b0, int nm1, Acc<T>& acc) {
-  for (int t = g0; t < g1; ++t) term<T, T2, KIND, CLS>(st[t], coef, win, a, la, lb, b0, nm1, acc);
+__device__ __forceinline__ void group(const int4* st, int g0, int g1, const T2* __restrict__ ca,
+                                      const T2* __restrict__ cb, const T2* wbase, Acc<T>& acc) {
+  for (int t = g0; t < g1; ++t) term<T, T2, KIND, CLS>(st[t], ca, cb, wbase, acc);
 }
 
 template <typename T>
@@ -103,7 +118,7 @@ __global__ void __launch_bounds__(kApplyThreads)
   using T2 = typename Vec2<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T2* win = reinterpret_cast<T2*>(smem_raw);  // [3][kWinElems] source windows
-  __shared__ DevTerm st[kMaxSectorTerms];
+  __shared__ int4 st[kMaxSectorTerms];
   __shared__ int ge[G_COUNT + 1];
   const DevTile tile = tiles[blockIdx.x];
   const DevSector& sec = sectors[tile.sector];
@@ -112,10 +127,13 @@ __global__ void __launch_bounds__(kApplyThreads)
   y += col * ld;
   const int tb = sec.term_begin;
   const int nt = sec.group_end[G_COUNT - 1] - tb;
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = terms[tb + i];
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
   if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
+  const int la = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   // Stage the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every
-  // source sector (e = -1, 0, +1).
+  // source sector (e = -1, 0, +1): lane = window row (plus rows 32..35 on lanes 0..3),
+  // warps stride over the 36 window columns.
 #pragma unroll 1
   for (int slot = 0; slot < 3; ++slot) {
     const int s2 = sec.src[slot];
@@ -124,45 +142,56 @@ __global__ void __launch_bounds__(kApplyThreads)
     const T2* xs = x + sectors[s2].offset;
     const int r0 = tile.a0 + slot - 1 - kHalo, c0 = tile.b0 + slot - 1 - kHalo;
     T2* w = win + slot * kWinElems;
-    for (int idx = threadIdx.x; idx < kWinElems; idx += blockDim.x) {
-      const int i = idx % kWinRows, j = idx / kWinRows;
-      const int R = r0 + i, C = c0 + j;
-      T2 v;
-      v.x = 0;
-      v.y = 0;
-      if ((unsigned)R < (unsigned)m && (unsigned)C < (unsigned)m) v = __ldg(xs + R + C * m);
-      w[idx] = v;
+    const int R = r0 + la, R2 = r0 + 32 + la;
+    const bool rv = (unsigned)R < (unsigned)m, rv2 = la < kWinRows - 32 && (unsigned)R2 < (unsigned)m;
+    for (int j = warp; j < kWinCols; j += kApplyWarps) {
+      const int C = c0 + j;
+      const bool cv = (unsigned)C < (unsigned)m;
+      T2 v, v2;
+      v.x = v.y = v2.x = v2.y = 0;
+      if (rv && cv) v = __ldg(xs + R + C * m);
+      if (rv2 && cv) v2 = __ldg(xs + R2 + C * m);
+      w[la + j * kWinRows] = v;
+      if (la < kWinRows - 32) w[32 + la + j * kWinRows] = v2;
     }
   }
   __syncthreads();
   const int n = sec.n;
-  const int la = threadIdx.x & 31;
-  const int lb = (threadIdx.x >> 5) * kColsPerThread;
+  const int lb = warp * kColsPerThread;
   const int a = tile.a0 + la;
   const int b0 = tile.b0 + lb;
   if (a >= n || b0 >= n) return;
   const int ncol = min(kColsPerThread, n - b0);
-  const int nm1 = n - 1;
   Acc<T> acc;
 #pragma unroll
   for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
-  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], coef, win, a, la, lb, b0, nm1, acc);
-  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], coef, win, a, la, lb, b0, nm1, acc);
-  const T scale = (T)border.scale;
+  const T2* ca = coef + a;
+  const T2* cb = coef + b0;
+  const T2* wbase = win + (la + kHalo) + (lb + kHalo) * kWinRows;  // + woff selects slot, p, q
+  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], ca, cb, wbase, acc);
+  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], ca, cb, wbase, acc);
+  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], ca, cb, wbase, acc);
+  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], ca, cb, wbase, acc);
+  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], ca, cb, wbase, acc);
+  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], ca, cb, wbase, acc);
+  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], ca, cb, wbase, acc);
+  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], ca, cb, wbase, acc);
+  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], ca, cb, wbase, acc);
+  if (border.scale != 1.0) {
+    const T scale = (T)border.scale;
+#pragma unroll
+    for (int k = 0; k < kColsPerThread; ++k) {
+      acc.re[k] *= scale;
+      acc.im[k] *= scale;
+    }
+  }
   T2* yp = y + sec.offset + a + (long long)b0 * n;
 #pragma unroll
   for (int k = 0; k < kColsPerThread; ++k) {
     if (k >= ncol) break;
     T2 out;
-    out.x = scale * acc.re[k];
-    out.y = scale * acc.im[k];
+    out.x = acc.re[k];
+    out.y = acc.im[k];
     if (b0 + k == a && border.alpha != nullptr) {
       const double2 al = border.alpha[col];
       const double v = border.coords ? sec.border_z : sec.border_x;

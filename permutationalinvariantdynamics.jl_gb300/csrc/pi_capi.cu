@@ -122,13 +122,21 @@ int upload_plan(pi_plan* plan) {
         if (group_of(t) != g) continue;
         DevTerm dt;
         const Sector& src = hp.sectors[t.src];
-        dt.slot = t.e + 1;
-        dt.p = t.p;
-        dt.q = t.q;
+        dt.woff = (t.e + 1) * kWinElems + t.p + t.q * kWinRows;
         dt.pad = 0;
         const double ratio = sec.sqrt_f / src.sqrt_f;  // population-coordinate rescaling
-        dt.alpha_off = -1;
-        dt.beta_off = -1;
+        dt.alpha_off = 0;
+        dt.beta_off = 0;
+        // every coefficient array starts on a 4-element boundary and is padded to a
+        // multiple of 4, so the kernel reads beta[b0 .. b0+3] with aligned vector loads
+        auto pad4 = [&]() {
+          while (coef64.size() % 4) {
+            coef64.push_back(make_double2(0, 0));
+            coef32x.push_back(make_float2(0, 0));
+            coef32z.push_back(make_float2(0, 0));
+          }
+        };
+        pad4();
         if (!t.alpha.empty()) {
           dt.alpha_off = (int)coef64.size();
           for (const auto& z : t.alpha) {
@@ -136,6 +144,7 @@ int upload_plan(pi_plan* plan) {
             coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
             coef32z.push_back(make_float2((float)(z.real() * ratio), (float)(z.imag() * ratio)));
           }
+          pad4();
         }
         if (!t.beta.empty()) {
           dt.beta_off = (int)coef64.size();
@@ -146,6 +155,7 @@ int upload_plan(pi_plan* plan) {
             coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
             coef32z.push_back(make_float2((float)(z.real() * r), (float)(z.imag() * r)));
           }
+          pad4();
         }
         terms.push_back(dt);
       }

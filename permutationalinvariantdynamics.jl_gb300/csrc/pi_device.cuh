@@ -37,11 +37,9 @@ struct DevSector {
 // One separable stencil term (see pi_plan.hpp); its group fixes kind and class.  The
 // source entry x_src[a + e + p, b + e + q] is read from the staged window of slot e + 1.
 struct DevTerm {
-  int slot;            // e + 1: which staged source window
-  int p;               // row offset within the band, -2..2
-  int q;               // column offset within the band, -2..2
-  int alpha_off;       // offset of alpha[0..n) in the coefficient pool (-1: unused)
-  int beta_off;        // offset of beta[0..n) in the coefficient pool (-1: unused)
+  int woff;            // (e+1)*kWinElems + p + q*kWinRows: offset into the staged windows
+  int alpha_off;       // offset of alpha[0..n) in the coefficient pool (0 when unused)
+  int beta_off;        // offset of beta[0..n) in the coefficient pool, a multiple of 4
   int pad;
 };
 
