@@ -285,6 +285,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-apply", action="store_true",
                     help="time only the device applies (used for ncu captures)")
+    ap.add_argument("--only-solves", action="store_true",
+                    help="run only the solve-rate section (used for ncu launch lists)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -298,6 +300,9 @@ def main():
     __graft_entry__.build()
     import picuda
     torch.cuda.set_device(local)
+    if args.only_solves:
+        print(json.dumps({"only_solves": True, "solves": solve_rates(picuda, torch)}))
+        return 0
     model = model_c2(picuda)
     compiled = picuda.compile(model)
     n = len(model.basis)

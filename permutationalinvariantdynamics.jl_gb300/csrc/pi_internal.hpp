@@ -62,7 +62,8 @@ cudaError_t combine_f64(const double2* V, long long ldv, int nv, const double2* 
 cudaError_t trace_dot(const DevicePlan& dp, const void* x, int is_f32, int coords, double2* out,
                       cudaStream_t stream);
 
-// Mixed precision (population coordinates, FP32 storage).
+// Mixed precision (FP32 storage): dots and norms accumulate in double-float (FP32 pairs,
+// ~48-bit significand) on the FP32 pipes; basis updates run in FP32.
 cudaError_t mdot_f32(const float2* V, long long ldv, int nv, const float2* w, long long n,
                      ReduceScratch& rs, double2* h_out, cudaStream_t stream);
 cudaError_t maxpy_f32(const float2* V, long long ldv, int nv, const double2* h, float2* w, long long n,

@@ -81,6 +81,110 @@ __global__ void __launch_bounds__(kReduceThreads)
   }
 }
 
+// Double-float accumulator: the pair (hi, lo) carries a ~48-bit significand on the FP32
+// pipes.  Products of two FP32 numbers are split exactly with an FMA (a*b = p + e) and
+// added with Knuth's TwoSum, so a dot of FP32 vectors is accumulated to FP64-class accuracy
+// without the GB300 FP64 pipe (1/64 of the FP32 rate).
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ void df_add_prod(DF& acc, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  const float s = acc.hi + p;
+  const float bb = s - acc.hi;
+  const float err = (acc.hi - (s - bb)) + (p - bb);
+  acc.hi = s;
+  acc.lo += err + e;
+}
+
+// Stage 1 of a multi-dot for FP32 vectors with double-float accumulation.
+__global__ void __launch_bounds__(kReduceThreads)
+    k_mdot_partial_df(const float2* __restrict__ V, long long ldv, int nv, const float2* __restrict__ w, long long n,
+                      double2* __restrict__ partial) {
+  __shared__ double smem[32 * 8];
+  long long beg, end;
+  chunk_bounds(n, beg, end);
+  for (int g = 0; g < nv; g += 4) {
+    DF re[4], im[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) re[k] = im[k] = DF{0.f, 0.f};
+    const int cnt = min(4, nv - g);
+    for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+      const float2 wv = __ldg(w + e);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (k < cnt) {
+          const float2 v = __ldg(V + (long long)(g + k) * ldv + e);
+          df_add_prod(re[k], v.x, wv.x);
+          df_add_prod(re[k], v.y, wv.y);
+          df_add_prod(im[k], v.x, wv.y);
+          df_add_prod(im[k], -v.y, wv.x);
+        }
+      }
+    }
+    double acc[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      acc[2 * k] = (double)re[k].hi + (double)re[k].lo;
+      acc[2 * k + 1] = (double)im[k].hi + (double)im[k].lo;
+    }
+    block_sum<8>(acc, smem);
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < cnt; ++k)
+        partial[(long long)blockIdx.x * kMaxDots + g + k] = make_double2(acc[2 * k], acc[2 * k + 1]);
+    }
+  }
+}
+
+// w -= sum_i V_i h_i in FP32 (h rounded once), optional |w|^2 partials in double-float.
+__global__ void __launch_bounds__(kReduceThreads)
+    k_maxpy_f32(const float2* __restrict__ V, long long ldv, int nv, const double2* __restrict__ h,
+                float2* __restrict__ w, long long n, double* __restrict__ rpartial) {
+  __shared__ float2 hs[kMaxDots];
+  __shared__ double smem[32];
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) hs[i] = make_float2((float)h[i].x, (float)h[i].y);
+  __syncthreads();
+  long long beg, end;
+  chunk_bounds(n, beg, end);
+  DF nrm{0.f, 0.f};
+  for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+    float2 wv = w[e];
+    for (int i = 0; i < nv; ++i) {
+      const float2 v = __ldg(V + (long long)i * ldv + e);
+      const float2 c = hs[i];
+      wv.x = fmaf(-v.x, c.x, wv.x);
+      wv.x = fmaf(v.y, c.y, wv.x);
+      wv.y = fmaf(-v.x, c.y, wv.y);
+      wv.y = fmaf(-v.y, c.x, wv.y);
+    }
+    w[e] = wv;
+    df_add_prod(nrm, wv.x, wv.x);
+    df_add_prod(nrm, wv.y, wv.y);
+  }
+  if (rpartial != nullptr) {
+    double acc[1] = {(double)nrm.hi + (double)nrm.lo};
+    block_sum<1>(acc, smem);
+    if (threadIdx.x == 0) rpartial[blockIdx.x] = acc[0];
+  }
+}
+
+__global__ void __launch_bounds__(kReduceThreads)
+    k_norm2_df(const float2* __restrict__ w, long long n, double* __restrict__ rpartial) {
+  __shared__ double smem[32];
+  long long beg, end;
+  chunk_bounds(n, beg, end);
+  DF nrm{0.f, 0.f};
+  for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+    const float2 v = __ldg(w + e);
+    df_add_prod(nrm, v.x, v.x);
+    df_add_prod(nrm, v.y, v.y);
+  }
+  double acc[1] = {(double)nrm.hi + (double)nrm.lo};
+  block_sum<1>(acc, smem);
+  if (threadIdx.x == 0) rpartial[blockIdx.x] = acc[0];
+}
+
 // Stage 2: one block per dot, fixed-order sum over the partials.
 __global__ void __launch_bounds__(kReduceThreads)
     k_mdot_final(const double2* __restrict__ partial, int nblocks, double2* __restrict__ out) {
@@ -303,7 +407,7 @@ cudaError_t mdot_f32(const float2* V, long long ldv, int nv, const float2* w, lo
                      double2* h_out, cudaStream_t stream) {
   if (nv <= 0) return cudaSuccess;
   if (nv > kMaxDots) return cudaErrorInvalidValue;
-  k_mdot_partial<float2><<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, w, n, rs.partial);
+  k_mdot_partial_df<<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, w, n, rs.partial);
   k_mdot_final<<<nv, kReduceThreads, 0, stream>>>(rs.partial, kReduceBlocks, h_out);
   return cudaGetLastError();
 }
@@ -320,8 +424,8 @@ cudaError_t maxpy_f64(const double2* V, long long ldv, int nv, const double2* h,
 cudaError_t maxpy_f32(const float2* V, long long ldv, int nv, const double2* h, float2* w, long long n,
                       ReduceScratch& rs, int norm_slot, cudaStream_t stream) {
   if (nv > kMaxDots) return cudaErrorInvalidValue;
-  k_maxpy<float2><<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, h, w, n,
-                                                                norm_slot >= 0 ? rs.rpartial : nullptr);
+  k_maxpy_f32<<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, h, w, n,
+                                                            norm_slot >= 0 ? rs.rpartial : nullptr);
   if (norm_slot >= 0) k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, kReduceBlocks, rs.rresult + norm_slot);
   return cudaGetLastError();
 }
@@ -333,7 +437,7 @@ cudaError_t norm2_f64(const double2* w, long long n, ReduceScratch& rs, int slot
 }
 
 cudaError_t norm2_f32(const float2* w, long long n, ReduceScratch& rs, int slot, cudaStream_t stream) {
-  k_norm2<float2><<<kReduceBlocks, kReduceThreads, 0, stream>>>(w, n, rs.rpartial);
+  k_norm2_df<<<kReduceBlocks, kReduceThreads, 0, stream>>>(w, n, rs.rpartial);
   k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, kReduceBlocks, rs.rresult + slot);
   return cudaGetLastError();
 }
