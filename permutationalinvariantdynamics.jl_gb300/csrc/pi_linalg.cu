@@ -5,6 +5,8 @@
 // Replaces the orthogonalisation loops of the reference (MGS x2: src/krylov.jl:762-766,
 // src/krylov_extensions.jl:1358-1363), the basis combinations (krylov.jl:779,
 // krylov_extensions.jl:1415-1416) and the trace functional dot (krylov.jl:855-860).
+#include <algorithm>
+
 #include "pi_internal.hpp"
 
 namespace picuda {
@@ -49,35 +51,39 @@ __device__ __forceinline__ double2 load_c(const T2* p) {
   return make_double2((double)v.x, (double)v.y);
 }
 
-// Stage 1 of a multi-dot: partial[blk][i] for a group of up to 4 vectors.
+// Stage 1 of a multi-dot: block (bx, by) reduces vectors by*8 .. by*8+7 over element chunk
+// bx and writes partial[bx][i].  One block-wide sum per block.
+constexpr int kDotGroup = 8;
+
 template <typename T2>
 __global__ void __launch_bounds__(kReduceThreads)
     k_mdot_partial(const T2* __restrict__ V, long long ldv, int nv, const T2* __restrict__ w, long long n,
                    double2* __restrict__ partial) {
-  __shared__ double smem[32 * 8];
+  __shared__ double smem[32 * 2 * kDotGroup];
   long long beg, end;
   chunk_bounds(n, beg, end);
-  for (int g = 0; g < nv; g += 4) {
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int cnt = min(4, nv - g);
-    for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
-      const double2 wv = load_c(w + e);
+  const int g = blockIdx.y * kDotGroup;
+  const int cnt = min(kDotGroup, nv - g);
+  double acc[2 * kDotGroup];
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (k < cnt) {
-          const double2 v = load_c(V + (long long)(g + k) * ldv + e);
-          acc[2 * k] = fma(v.x, wv.x, acc[2 * k]);
-          acc[2 * k] = fma(v.y, wv.y, acc[2 * k]);
-          acc[2 * k + 1] = fma(v.x, wv.y, acc[2 * k + 1]);
-          acc[2 * k + 1] = fma(-v.y, wv.x, acc[2 * k + 1]);
-        }
+  for (int k = 0; k < 2 * kDotGroup; ++k) acc[k] = 0.0;
+  for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+    const double2 wv = load_c(w + e);
+#pragma unroll
+    for (int k = 0; k < kDotGroup; ++k) {
+      if (k < cnt) {
+        const double2 v = load_c(V + (long long)(g + k) * ldv + e);
+        acc[2 * k] = fma(v.x, wv.x, acc[2 * k]);
+        acc[2 * k] = fma(v.y, wv.y, acc[2 * k]);
+        acc[2 * k + 1] = fma(v.x, wv.y, acc[2 * k + 1]);
+        acc[2 * k + 1] = fma(-v.y, wv.x, acc[2 * k + 1]);
       }
     }
-    block_sum<8>(acc, smem);
-    if (threadIdx.x == 0) {
-      for (int k = 0; k < cnt; ++k)
-        partial[(long long)blockIdx.x * kMaxDots + g + k] = make_double2(acc[2 * k], acc[2 * k + 1]);
-    }
+  }
+  block_sum<2 * kDotGroup>(acc, smem);
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < cnt; ++k)
+      partial[(long long)blockIdx.x * kMaxDots + g + k] = make_double2(acc[2 * k], acc[2 * k + 1]);
   }
 }
 
@@ -98,42 +104,41 @@ __device__ __forceinline__ void df_add_prod(DF& acc, float a, float b) {
   acc.lo += err + e;
 }
 
-// Stage 1 of a multi-dot for FP32 vectors with double-float accumulation.
+// Stage 1 of a multi-dot for FP32 vectors with double-float accumulation (grid as above).
 __global__ void __launch_bounds__(kReduceThreads)
     k_mdot_partial_df(const float2* __restrict__ V, long long ldv, int nv, const float2* __restrict__ w, long long n,
                       double2* __restrict__ partial) {
-  __shared__ double smem[32 * 8];
+  __shared__ double smem[32 * 2 * kDotGroup];
   long long beg, end;
   chunk_bounds(n, beg, end);
-  for (int g = 0; g < nv; g += 4) {
-    DF re[4], im[4];
+  const int g = blockIdx.y * kDotGroup;
+  const int cnt = min(kDotGroup, nv - g);
+  DF re[kDotGroup], im[kDotGroup];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) re[k] = im[k] = DF{0.f, 0.f};
-    const int cnt = min(4, nv - g);
-    for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
-      const float2 wv = __ldg(w + e);
+  for (int k = 0; k < kDotGroup; ++k) re[k] = im[k] = DF{0.f, 0.f};
+  for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+    const float2 wv = __ldg(w + e);
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        if (k < cnt) {
-          const float2 v = __ldg(V + (long long)(g + k) * ldv + e);
-          df_add_prod(re[k], v.x, wv.x);
-          df_add_prod(re[k], v.y, wv.y);
-          df_add_prod(im[k], v.x, wv.y);
-          df_add_prod(im[k], -v.y, wv.x);
-        }
+    for (int k = 0; k < kDotGroup; ++k) {
+      if (k < cnt) {
+        const float2 v = __ldg(V + (long long)(g + k) * ldv + e);
+        df_add_prod(re[k], v.x, wv.x);
+        df_add_prod(re[k], v.y, wv.y);
+        df_add_prod(im[k], v.x, wv.y);
+        df_add_prod(im[k], -v.y, wv.x);
       }
     }
-    double acc[8];
+  }
+  double acc[2 * kDotGroup];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      acc[2 * k] = (double)re[k].hi + (double)re[k].lo;
-      acc[2 * k + 1] = (double)im[k].hi + (double)im[k].lo;
-    }
-    block_sum<8>(acc, smem);
-    if (threadIdx.x == 0) {
-      for (int k = 0; k < cnt; ++k)
-        partial[(long long)blockIdx.x * kMaxDots + g + k] = make_double2(acc[2 * k], acc[2 * k + 1]);
-    }
+  for (int k = 0; k < kDotGroup; ++k) {
+    acc[2 * k] = (double)re[k].hi + (double)re[k].lo;
+    acc[2 * k + 1] = (double)im[k].hi + (double)im[k].lo;
+  }
+  block_sum<2 * kDotGroup>(acc, smem);
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < cnt; ++k)
+      partial[(long long)blockIdx.x * kMaxDots + g + k] = make_double2(acc[2 * k], acc[2 * k + 1]);
   }
 }
 
@@ -385,6 +390,14 @@ __global__ void __launch_bounds__(kReduceThreads)
   if (threadIdx.x == 0) rpartial[blockIdx.x] = acc[0];
 }
 
+// Element-chunk blocks for a reduction over n entries: at least ~4 entries per thread,
+// at most kReduceBlocks in total across the vector-group dimension.
+inline int reduce_blocks(long long n, int ygroups) {
+  long long b = (n + 4LL * kReduceThreads - 1) / (4LL * kReduceThreads);
+  long long cap = std::max(1, kReduceBlocks / std::max(1, ygroups));
+  return (int)std::max(1LL, std::min(b, cap));
+}
+
 inline int grid_for(long long n) {
   long long g = (n + 255) / 256;
   if (g > 4 * 152) g = 4 * 152;
@@ -398,8 +411,10 @@ cudaError_t mdot_f64(const double2* V, long long ldv, int nv, const double2* w, 
                      double2* h_out, cudaStream_t stream) {
   if (nv <= 0) return cudaSuccess;
   if (nv > kMaxDots) return cudaErrorInvalidValue;
-  k_mdot_partial<double2><<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, w, n, rs.partial);
-  k_mdot_final<<<nv, kReduceThreads, 0, stream>>>(rs.partial, kReduceBlocks, h_out);
+  const int gy = (nv + kDotGroup - 1) / kDotGroup;
+  const int gx = reduce_blocks(n, gy);
+  k_mdot_partial<double2><<<dim3(gx, gy), kReduceThreads, 0, stream>>>(V, ldv, nv, w, n, rs.partial);
+  k_mdot_final<<<nv, kReduceThreads, 0, stream>>>(rs.partial, gx, h_out);
   return cudaGetLastError();
 }
 
@@ -407,38 +422,42 @@ cudaError_t mdot_f32(const float2* V, long long ldv, int nv, const float2* w, lo
                      double2* h_out, cudaStream_t stream) {
   if (nv <= 0) return cudaSuccess;
   if (nv > kMaxDots) return cudaErrorInvalidValue;
-  k_mdot_partial_df<<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, w, n, rs.partial);
-  k_mdot_final<<<nv, kReduceThreads, 0, stream>>>(rs.partial, kReduceBlocks, h_out);
+  const int gy = (nv + kDotGroup - 1) / kDotGroup;
+  const int gx = reduce_blocks(n, gy);
+  k_mdot_partial_df<<<dim3(gx, gy), kReduceThreads, 0, stream>>>(V, ldv, nv, w, n, rs.partial);
+  k_mdot_final<<<nv, kReduceThreads, 0, stream>>>(rs.partial, gx, h_out);
   return cudaGetLastError();
 }
 
 cudaError_t maxpy_f64(const double2* V, long long ldv, int nv, const double2* h, double2* w, long long n,
                       ReduceScratch& rs, int norm_slot, cudaStream_t stream) {
   if (nv > kMaxDots) return cudaErrorInvalidValue;
-  k_maxpy<double2><<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, h, w, n,
-                                                                 norm_slot >= 0 ? rs.rpartial : nullptr);
-  if (norm_slot >= 0) k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, kReduceBlocks, rs.rresult + norm_slot);
+  const int gx = reduce_blocks(n, 1);
+  k_maxpy<double2><<<gx, kReduceThreads, 0, stream>>>(V, ldv, nv, h, w, n, norm_slot >= 0 ? rs.rpartial : nullptr);
+  if (norm_slot >= 0) k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, gx, rs.rresult + norm_slot);
   return cudaGetLastError();
 }
 
 cudaError_t maxpy_f32(const float2* V, long long ldv, int nv, const double2* h, float2* w, long long n,
                       ReduceScratch& rs, int norm_slot, cudaStream_t stream) {
   if (nv > kMaxDots) return cudaErrorInvalidValue;
-  k_maxpy_f32<<<kReduceBlocks, kReduceThreads, 0, stream>>>(V, ldv, nv, h, w, n,
-                                                            norm_slot >= 0 ? rs.rpartial : nullptr);
-  if (norm_slot >= 0) k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, kReduceBlocks, rs.rresult + norm_slot);
+  const int gx = reduce_blocks(n, 1);
+  k_maxpy_f32<<<gx, kReduceThreads, 0, stream>>>(V, ldv, nv, h, w, n, norm_slot >= 0 ? rs.rpartial : nullptr);
+  if (norm_slot >= 0) k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, gx, rs.rresult + norm_slot);
   return cudaGetLastError();
 }
 
 cudaError_t norm2_f64(const double2* w, long long n, ReduceScratch& rs, int slot, cudaStream_t stream) {
-  k_norm2<double2><<<kReduceBlocks, kReduceThreads, 0, stream>>>(w, n, rs.rpartial);
-  k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, kReduceBlocks, rs.rresult + slot);
+  const int gx = reduce_blocks(n, 1);
+  k_norm2<double2><<<gx, kReduceThreads, 0, stream>>>(w, n, rs.rpartial);
+  k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, gx, rs.rresult + slot);
   return cudaGetLastError();
 }
 
 cudaError_t norm2_f32(const float2* w, long long n, ReduceScratch& rs, int slot, cudaStream_t stream) {
-  k_norm2_df<<<kReduceBlocks, kReduceThreads, 0, stream>>>(w, n, rs.rpartial);
-  k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, kReduceBlocks, rs.rresult + slot);
+  const int gx = reduce_blocks(n, 1);
+  k_norm2_df<<<gx, kReduceThreads, 0, stream>>>(w, n, rs.rpartial);
+  k_rfinal<<<1, kReduceThreads, 0, stream>>>(rs.rpartial, gx, rs.rresult + slot);
   return cudaGetLastError();
 }
 
