@@ -18,6 +18,8 @@
 // coordinates).  TMA is not used for the staging: the reference's packed column-major
 // blocks have odd leading dimensions (n = N - 2k + 1), so FP32 rows are not 16-byte
 // strided as tensor maps require.
+#include <algorithm>
+
 #include "pi_device.cuh"
 #include "pi_internal.hpp"
 
@@ -109,96 +111,151 @@ __device__ __forceinline__ void group(const int4* st, int g0, int g1, const T2* 
   for (int t = g0; t < g1; ++t) term<T, T2, KIND, CLS>(st[t], ca, cb, wbase, acc);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kApplyThreads)
-    k_apply(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
-            const typename Vec2<T>::type* __restrict__ coef, const DevTile* __restrict__ tiles,
-            const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ y,
-            long long ld, BorderArgs border) {
-  using T2 = typename Vec2<T>::type;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T2* win = reinterpret_cast<T2*>(smem_raw);  // [3][kWinElems] source windows
-  __shared__ int4 st[kMaxSectorTerms];
-  __shared__ int ge[G_COUNT + 1];
-  const DevTile tile = tiles[blockIdx.x];
+// Asynchronous global -> shared copies (cp.async) with hardware zero fill: a source size of
+// 0 writes zeros and reads nothing, which pads the halo and the block edges for free.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_zfill(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int sz = valid ? BYTES : 0;
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(BYTES), "r"(sz)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Shared-memory state of one pipeline stage: the three source windows of a work item, its
+// sector's grouped term list and group boundaries.
+template <typename T2>
+struct Stage {
+  T2 win[3 * kWinElems];
+  int4 st[kMaxSectorTerms];
+  int ge[G_COUNT + 1];
+};
+
+// Issues the copies of work item `item` = (tile, column) into stage `S` (cp.async for the
+// windows, plain loads for the term list) and commits one cp.async group.
+template <typename T2>
+__device__ __forceinline__ void issue_stage(Stage<T2>& S, const DevSector* __restrict__ sectors,
+                                            const DevTerm* __restrict__ terms, const DevTile* __restrict__ tiles,
+                                            const T2* __restrict__ x, long long ld, int ncols, int item) {
+  const int tile_id = item / ncols;
+  const int col = item - tile_id * ncols;
+  const DevTile tile = tiles[tile_id];
   const DevSector& sec = sectors[tile.sector];
-  const long long col = blockIdx.y;
-  x += col * ld;
-  y += col * ld;
-  const int tb = sec.term_begin;
-  const int nt = sec.group_end[G_COUNT - 1] - tb;
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
-  if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
+  const T2* xc = x + (long long)col * ld;
   const int la = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  // Stage the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every
-  // source sector (e = -1, 0, +1): lane = window row (plus rows 32..35 on lanes 0..3),
-  // warps stride over the 36 window columns.
 #pragma unroll 1
   for (int slot = 0; slot < 3; ++slot) {
     const int s2 = sec.src[slot];
     if (s2 < 0) continue;
     const int m = sectors[s2].n;
-    const T2* xs = x + sectors[s2].offset;
+    const T2* xs = xc + sectors[s2].offset;
     const int r0 = tile.a0 + slot - 1 - kHalo, c0 = tile.b0 + slot - 1 - kHalo;
-    T2* w = win + slot * kWinElems;
+    T2* w = S.win + slot * kWinElems;
     const int R = r0 + la, R2 = r0 + 32 + la;
-    const bool rv = (unsigned)R < (unsigned)m, rv2 = la < kWinRows - 32 && (unsigned)R2 < (unsigned)m;
+    const bool rv = (unsigned)R < (unsigned)m;
+    const bool extra = la < kWinRows - 32;
+    const bool rv2 = extra && (unsigned)R2 < (unsigned)m;
     for (int j = warp; j < kWinCols; j += kApplyWarps) {
       const int C = c0 + j;
       const bool cv = (unsigned)C < (unsigned)m;
-      T2 v, v2;
-      v.x = v.y = v2.x = v2.y = 0;
-      if (rv && cv) v = __ldg(xs + R + C * m);
-      if (rv2 && cv) v2 = __ldg(xs + R2 + C * m);
-      w[la + j * kWinRows] = v;
-      if (la < kWinRows - 32) w[32 + la + j * kWinRows] = v2;
+      const bool v1 = rv && cv, v2 = rv2 && cv;
+      cp_async_zfill<sizeof(T2)>(w + la + j * kWinRows, v1 ? xs + R + C * m : xs, v1);
+      if (extra) cp_async_zfill<sizeof(T2)>(w + 32 + la + j * kWinRows, v2 ? xs + R2 + C * m : xs, v2);
     }
   }
-  __syncthreads();
-  const int n = sec.n;
-  const int lb = warp * kColsPerThread;
-  const int a = tile.a0 + la;
-  const int b0 = tile.b0 + lb;
-  if (a >= n || b0 >= n) return;
-  const int ncol = min(kColsPerThread, n - b0);
-  Acc<T> acc;
+  cp_async_commit();
+  const int tb = sec.term_begin;
+  const int nt = sec.group_end[G_COUNT - 1] - tb;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) S.st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
+  if (threadIdx.x <= G_COUNT) S.ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
+}
+
+// Persistent apply: each block walks a contiguous range of work items (tile-major, column
+// minor, so one tile is reused across many right-hand sides) with a two-stage cp.async
+// pipeline -- the windows of item i+1 are in flight while item i is computed.
+template <typename T>
+__global__ void __launch_bounds__(kApplyThreads)
+    k_apply(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
+            const typename Vec2<T>::type* __restrict__ coef, const DevTile* __restrict__ tiles, int ntiles,
+            int ncols, const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ y,
+            long long ld, BorderArgs border) {
+  using T2 = typename Vec2<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Stage<T2>* stages = reinterpret_cast<Stage<T2>*>(smem_raw);
+  const long long total = (long long)ntiles * ncols;
+  const int begin = (int)((long long)blockIdx.x * total / gridDim.x);
+  const int end = (int)((long long)(blockIdx.x + 1) * total / gridDim.x);
+  if (begin >= end) return;
+  const int la = threadIdx.x & 31;
+  const int lb = (threadIdx.x >> 5) * kColsPerThread;
+  issue_stage<T2>(stages[0], sectors, terms, tiles, x, ld, ncols, begin);
+  for (int item = begin; item < end; ++item) {
+    const int buf = (item - begin) & 1;
+    if (item + 1 < end)
+      issue_stage<T2>(stages[buf ^ 1], sectors, terms, tiles, x, ld, ncols, item + 1);
+    else
+      cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const Stage<T2>& S = stages[buf];
+    const int tile_id = item / ncols;
+    const int col = item - tile_id * ncols;
+    const DevTile tile = tiles[tile_id];
+    const DevSector& sec = sectors[tile.sector];
+    const int n = sec.n;
+    const int a = tile.a0 + la;
+    const int b0 = tile.b0 + lb;
+    if (a < n && b0 < n) {
+      const int ncol = min(kColsPerThread, n - b0);
+      Acc<T> acc;
 #pragma unroll
-  for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
-  const T2* ca = coef + a;
-  const T2* cb = coef + b0;
-  const T2* wbase = win + (la + kHalo) + (lb + kHalo) * kWinRows;  // + woff selects slot, p, q
-  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], ca, cb, wbase, acc);
-  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], ca, cb, wbase, acc);
-  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], ca, cb, wbase, acc);
-  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], ca, cb, wbase, acc);
-  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], ca, cb, wbase, acc);
-  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], ca, cb, wbase, acc);
-  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], ca, cb, wbase, acc);
-  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], ca, cb, wbase, acc);
-  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], ca, cb, wbase, acc);
-  if (border.scale != 1.0) {
-    const T scale = (T)border.scale;
+      for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
+      const T2* ca = coef + a;
+      const T2* cb = coef + b0;
+      const T2* wbase = S.win + (la + kHalo) + (lb + kHalo) * kWinRows;  // + woff selects slot, p, q
+      const int4* st = S.st;
+      group<T, T2, K_ADD, C_CX>(st, S.ge[G_ADD], S.ge[G_ADD + 1], ca, cb, wbase, acc);
+      group<T, T2, K_LEFT, C_IM>(st, S.ge[G_LEFT_IM], S.ge[G_LEFT_IM + 1], ca, cb, wbase, acc);
+      group<T, T2, K_LEFT, C_RE>(st, S.ge[G_LEFT_RE], S.ge[G_LEFT_RE + 1], ca, cb, wbase, acc);
+      group<T, T2, K_LEFT, C_CX>(st, S.ge[G_LEFT_CX], S.ge[G_LEFT_CX + 1], ca, cb, wbase, acc);
+      group<T, T2, K_RIGHT, C_IM>(st, S.ge[G_RIGHT_IM], S.ge[G_RIGHT_IM + 1], ca, cb, wbase, acc);
+      group<T, T2, K_RIGHT, C_RE>(st, S.ge[G_RIGHT_RE], S.ge[G_RIGHT_RE + 1], ca, cb, wbase, acc);
+      group<T, T2, K_RIGHT, C_CX>(st, S.ge[G_RIGHT_CX], S.ge[G_RIGHT_CX + 1], ca, cb, wbase, acc);
+      group<T, T2, K_SAND, C_RE>(st, S.ge[G_SAND_RE], S.ge[G_SAND_RE + 1], ca, cb, wbase, acc);
+      group<T, T2, K_SAND, C_CX>(st, S.ge[G_SAND_CX], S.ge[G_SAND_CX + 1], ca, cb, wbase, acc);
+      if (border.scale != 1.0) {
+        const T scale = (T)border.scale;
 #pragma unroll
-    for (int k = 0; k < kColsPerThread; ++k) {
-      acc.re[k] *= scale;
-      acc.im[k] *= scale;
+        for (int k = 0; k < kColsPerThread; ++k) {
+          acc.re[k] *= scale;
+          acc.im[k] *= scale;
+        }
+      }
+      T2* yp = y + (long long)col * ld + sec.offset + a + (long long)b0 * n;
+#pragma unroll
+      for (int k = 0; k < kColsPerThread; ++k) {
+        if (k >= ncol) break;
+        T2 out;
+        out.x = acc.re[k];
+        out.y = acc.im[k];
+        if (b0 + k == a && border.alpha != nullptr) {
+          const double2 al = border.alpha[col];
+          const double v = border.coords ? sec.border_z : sec.border_x;
+          out.x += (T)(al.x * v);
+          out.y += (T)(al.y * v);
+        }
+        yp[(long long)k * n] = out;
+      }
     }
-  }
-  T2* yp = y + sec.offset + a + (long long)b0 * n;
-#pragma unroll
-  for (int k = 0; k < kColsPerThread; ++k) {
-    if (k >= ncol) break;
-    T2 out;
-    out.x = acc.re[k];
-    out.y = acc.im[k];
-    if (b0 + k == a && border.alpha != nullptr) {
-      const double2 al = border.alpha[col];
-      const double v = border.coords ? sec.border_z : sec.border_x;
-      out.x += (T)(al.x * v);
-      out.y += (T)(al.y * v);
-    }
-    yp[(long long)k * n] = out;
+    __syncthreads();  // every thread is done with stage `buf` before it is refilled
   }
 }
 
@@ -207,16 +264,24 @@ cudaError_t launch_apply_t(const DevicePlan& dp, const void* coef, const void* x
                            long long ld, const BorderArgs& border, cudaStream_t stream) {
   using T2 = typename Vec2<T>::type;
   if (dp.ntiles == 0 || ncols == 0) return cudaSuccess;
-  const size_t smem = 3 * kWinElems * sizeof(T2);
-  static bool configured = false;  // per template instance, host side
-  if (!configured) {
+  const size_t smem = 2 * sizeof(Stage<T2>);
+  static int blocks_per_sm = 0;  // per template instance; the kernel and device are fixed
+  static int sms = 0;
+  if (blocks_per_sm == 0) {
     cudaError_t e = cudaFuncSetAttribute(k_apply<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    configured = true;
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int occ = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_apply<T>, kApplyThreads, smem);
+    if (e != cudaSuccess) return e;
+    blocks_per_sm = occ > 0 ? occ : 1;
   }
-  dim3 grid((unsigned)dp.ntiles, (unsigned)ncols);
-  k_apply<T><<<grid, kApplyThreads, smem, stream>>>(dp.sectors, dp.terms, (const T2*)coef, dp.tiles,
-                                                    (const T2*)x, (T2*)y, ld, border);
+  const long long total = (long long)dp.ntiles * ncols;
+  const long long grid = std::min<long long>(total, (long long)sms * blocks_per_sm);
+  k_apply<T><<<(unsigned)grid, kApplyThreads, smem, stream>>>(dp.sectors, dp.terms, (const T2*)coef, dp.tiles,
+                                                               dp.ntiles, ncols, (const T2*)x, (T2*)y, ld, border);
   return cudaGetLastError();
 }
 
