@@ -129,123 +129,270 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Shared-memory state of one pipeline stage: the three source windows of a work item, its
-// sector's grouped term list and group boundaries.
-template <typename T2>
-struct Stage {
-  T2 win[3 * kWinElems];
-  int4 st[kMaxSectorTerms];
-  int ge[G_COUNT + 1];
-};
-
-// Issues the copies of work item `item` = (tile, column) into stage `S` (cp.async for the
-// windows, plain loads for the term list) and commits one cp.async group.
-template <typename T2>
-__device__ __forceinline__ void issue_stage(Stage<T2>& S, const DevSector* __restrict__ sectors,
-                                            const DevTerm* __restrict__ terms, const DevTile* __restrict__ tiles,
-                                            const T2* __restrict__ x, long long ld, int ncols, int item) {
-  const int tile_id = item / ncols;
-  const int col = item - tile_id * ncols;
-  const DevTile tile = tiles[tile_id];
+template <typename T>
+__global__ void __launch_bounds__(kApplyThreads)
+    k_apply(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
+            const typename Vec2<T>::type* __restrict__ coef, const DevTile* __restrict__ tiles,
+            const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ y,
+            long long ld, BorderArgs border) {
+  using T2 = typename Vec2<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T2* win = reinterpret_cast<T2*>(smem_raw);  // [3][kWinElems] source windows
+  __shared__ int4 st[kMaxSectorTerms];
+  __shared__ int ge[G_COUNT + 1];
+  const DevTile tile = tiles[blockIdx.x];
   const DevSector& sec = sectors[tile.sector];
-  const T2* xc = x + (long long)col * ld;
+  const long long col = blockIdx.y;
+  x += col * ld;
+  y += col * ld;
+  const int tb = sec.term_begin;
+  const int nt = sec.group_end[G_COUNT - 1] - tb;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
+  if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
   const int la = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
+  // Stage the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every
+  // source sector (e = -1, 0, +1): lane = window row (plus rows 32..35 on lanes 0..3),
+  // warps stride over the 36 window columns.
 #pragma unroll 1
   for (int slot = 0; slot < 3; ++slot) {
     const int s2 = sec.src[slot];
     if (s2 < 0) continue;
     const int m = sectors[s2].n;
-    const T2* xs = xc + sectors[s2].offset;
+    const T2* xs = x + sectors[s2].offset;
     const int r0 = tile.a0 + slot - 1 - kHalo, c0 = tile.b0 + slot - 1 - kHalo;
-    T2* w = S.win + slot * kWinElems;
+    T2* w = win + slot * kWinElems;
     const int R = r0 + la, R2 = r0 + 32 + la;
-    const bool rv = (unsigned)R < (unsigned)m;
-    const bool extra = la < kWinRows - 32;
-    const bool rv2 = extra && (unsigned)R2 < (unsigned)m;
+    const bool rv = (unsigned)R < (unsigned)m, rv2 = la < kWinRows - 32 && (unsigned)R2 < (unsigned)m;
     for (int j = warp; j < kWinCols; j += kApplyWarps) {
       const int C = c0 + j;
       const bool cv = (unsigned)C < (unsigned)m;
-      const bool v1 = rv && cv, v2 = rv2 && cv;
-      cp_async_zfill<sizeof(T2)>(w + la + j * kWinRows, v1 ? xs + R + C * m : xs, v1);
-      if (extra) cp_async_zfill<sizeof(T2)>(w + 32 + la + j * kWinRows, v2 ? xs + R2 + C * m : xs, v2);
+      T2 v, v2;
+      v.x = v.y = v2.x = v2.y = 0;
+      if (rv && cv) v = __ldg(xs + R + C * m);
+      if (rv2 && cv) v2 = __ldg(xs + R2 + C * m);
+      w[la + j * kWinRows] = v;
+      if (la < kWinRows - 32) w[32 + la + j * kWinRows] = v2;
     }
   }
-  cp_async_commit();
-  const int tb = sec.term_begin;
-  const int nt = sec.group_end[G_COUNT - 1] - tb;
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) S.st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
-  if (threadIdx.x <= G_COUNT) S.ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
+  __syncthreads();
+  const int n = sec.n;
+  const int lb = warp * kColsPerThread;
+  const int a = tile.a0 + la;
+  const int b0 = tile.b0 + lb;
+  if (a >= n || b0 >= n) return;
+  const int ncol = min(kColsPerThread, n - b0);
+  Acc<T> acc;
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
+  const T2* ca = coef + a;
+  const T2* cb = coef + b0;
+  const T2* wbase = win + (la + kHalo) + (lb + kHalo) * kWinRows;  // + woff selects slot, p, q
+  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], ca, cb, wbase, acc);
+  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], ca, cb, wbase, acc);
+  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], ca, cb, wbase, acc);
+  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], ca, cb, wbase, acc);
+  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], ca, cb, wbase, acc);
+  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], ca, cb, wbase, acc);
+  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], ca, cb, wbase, acc);
+  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], ca, cb, wbase, acc);
+  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], ca, cb, wbase, acc);
+  if (border.scale != 1.0) {
+    const T scale = (T)border.scale;
+#pragma unroll
+    for (int k = 0; k < kColsPerThread; ++k) {
+      acc.re[k] *= scale;
+      acc.im[k] *= scale;
+    }
+  }
+  T2* yp = y + sec.offset + a + (long long)b0 * n;
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) {
+    if (k >= ncol) break;
+    T2 out;
+    out.x = acc.re[k];
+    out.y = acc.im[k];
+    if (b0 + k == a && border.alpha != nullptr) {
+      const double2 al = border.alpha[col];
+      const double v = border.coords ? sec.border_z : sec.border_x;
+      out.x += (T)(al.x * v);
+      out.y += (T)(al.y * v);
+    }
+    yp[(long long)k * n] = out;
+  }
 }
 
-// Persistent apply: each block walks a contiguous range of work items (tile-major, column
-// minor, so one tile is reused across many right-hand sides) with a two-stage cp.async
-// pipeline -- the windows of item i+1 are in flight while item i is computed.
-template <typename T>
-__global__ void __launch_bounds__(kApplyThreads)
-    k_apply(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
-            const typename Vec2<T>::type* __restrict__ coef, const DevTile* __restrict__ tiles, int ntiles,
-            int ncols, const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ y,
-            long long ld, BorderArgs border) {
+// ---------------------------------------------------------------------------------------
+// Batched apply for stencils made of one ADD term, LEFT/RIGHT terms with imaginary
+// coefficients (the Hamiltonian off-diagonals) and real sandwich terms (collective and local
+// gains) -- every qubit model with real one-body operators and diagonal losses.  The term
+// counts are compile-time (sectors with fewer terms are padded with zero terms on the host),
+// so each thread keeps its coefficient products alpha[a]*beta[b] in registers and reuses them
+// for a chunk of right-hand sides; only the x windows stream through a two-stage cp.async
+// pipeline.  Per output entry and right-hand side this leaves one shared load and two FMAs
+// per term.
+// ---------------------------------------------------------------------------------------
+template <typename T, int LI, int RI, int SR>
+__global__ void __launch_bounds__(kApplyThreads, sizeof(T) == 4 ? 2 : 1)
+    k_apply_rhs(const DevSector* __restrict__ sectors, const int4* __restrict__ fterms,
+                const typename Vec2<T>::type* __restrict__ coef, const DevTile* __restrict__ tiles, int ntiles,
+                int ncols, int rc, const typename Vec2<T>::type* __restrict__ x, typename Vec2<T>::type* __restrict__ y,
+                long long ld, BorderArgs border) {
   using T2 = typename Vec2<T>::type;
+  constexpr int NT = 1 + LI + RI + SR;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Stage<T2>* stages = reinterpret_cast<Stage<T2>*>(smem_raw);
-  const long long total = (long long)ntiles * ncols;
-  const int begin = (int)((long long)blockIdx.x * total / gridDim.x);
-  const int end = (int)((long long)(blockIdx.x + 1) * total / gridDim.x);
-  if (begin >= end) return;
+  T2* win = reinterpret_cast<T2*>(smem_raw);  // [2][3 * kWinElems]
+  const int chunk = blockIdx.x / ntiles;
+  const int tile_id = blockIdx.x - chunk * ntiles;
+  const int c0 = chunk * rc, c1 = min(c0 + rc, ncols);
+  const DevTile tile = tiles[tile_id];
+  const DevSector& sec = sectors[tile.sector];
+  const int n = sec.n;
   const int la = threadIdx.x & 31;
-  const int lb = (threadIdx.x >> 5) * kColsPerThread;
-  issue_stage<T2>(stages[0], sectors, terms, tiles, x, ld, ncols, begin);
-  for (int item = begin; item < end; ++item) {
-    const int buf = (item - begin) & 1;
-    if (item + 1 < end)
-      issue_stage<T2>(stages[buf ^ 1], sectors, terms, tiles, x, ld, ncols, item + 1);
+  const int warp = threadIdx.x >> 5;
+  const int lb = warp * kColsPerThread;
+  const int a = tile.a0 + la;
+  const int b0 = tile.b0 + lb;
+  const bool active = a < n && b0 < n;
+  const int ac = active ? a : 0, bq = active ? b0 : 0;
+
+  // Coefficients of the sector's terms for this thread's entries, kept in registers.
+  const int4* tt = fterms + (long long)tile.sector * NT;
+  int woff[NT];
+  T car[4], cai[4], lim[LI > 0 ? LI : 1], rim[RI > 0 ? RI : 1][4], sre[SR > 0 ? SR : 1][4];
+  {
+    const int4 t = tt[0];
+    woff[0] = t.x;
+    const T2 al = __ldg(coef + t.y + ac);
+    T2 be[4];
+    load4(coef + t.z + bq, be);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      car[k] = al.x + be[k].x;
+      cai[k] = al.y + be[k].y;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < LI; ++i) {
+    const int4 t = tt[1 + i];
+    woff[1 + i] = t.x;
+    lim[i] = __ldg(coef + t.y + ac).y;
+  }
+#pragma unroll
+  for (int i = 0; i < RI; ++i) {
+    const int4 t = tt[1 + LI + i];
+    woff[1 + LI + i] = t.x;
+    T2 be[4];
+    load4(coef + t.z + bq, be);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) rim[i][k] = be[k].y;
+  }
+#pragma unroll
+  for (int i = 0; i < SR; ++i) {
+    const int4 t = tt[1 + LI + RI + i];
+    woff[1 + LI + RI + i] = t.x;
+    const T al = __ldg(coef + t.y + ac).x;
+    T2 be[4];
+    load4(coef + t.z + bq, be);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) sre[i][k] = al * be[k].x;
+  }
+
+  // Staging plan of this thread: rows la and 32 + la of each source window.
+  int sR[3], sm[3], sc0[3];
+  long long soff[3];
+  bool srv[3], srv2[3];
+#pragma unroll
+  for (int slot = 0; slot < 3; ++slot) {
+    const int s2 = sec.src[slot];
+    sm[slot] = s2 >= 0 ? sectors[s2].n : 0;
+    soff[slot] = s2 >= 0 ? sectors[s2].offset : 0;
+    const int r0 = tile.a0 + slot - 1 - kHalo;
+    sc0[slot] = tile.b0 + slot - 1 - kHalo;
+    sR[slot] = r0 + la;
+    srv[slot] = (unsigned)(r0 + la) < (unsigned)sm[slot];
+    srv2[slot] = la < kWinRows - 32 && (unsigned)(r0 + 32 + la) < (unsigned)sm[slot];
+  }
+  auto stage = [&](int col, T2* w) {
+    const T2* xc = x + (long long)col * ld;
+#pragma unroll
+    for (int slot = 0; slot < 3; ++slot) {
+      if (sm[slot] == 0) continue;
+      const T2* xs = xc + soff[slot];
+      T2* ws = w + slot * kWinElems;
+      const int m = sm[slot];
+      for (int j = warp; j < kWinCols; j += kApplyWarps) {
+        const int C = sc0[slot] + j;
+        const bool cv = (unsigned)C < (unsigned)m;
+        const bool v1 = srv[slot] && cv, v2 = srv2[slot] && cv;
+        const T2* g = xs + sR[slot] + C * m;
+        cp_async_zfill<sizeof(T2)>(ws + la + j * kWinRows, v1 ? g : xs, v1);
+        if (la < kWinRows - 32) cp_async_zfill<sizeof(T2)>(ws + 32 + la + j * kWinRows, v2 ? g + 32 : xs, v2);
+      }
+    }
+    cp_async_commit();
+  };
+
+  stage(c0, win);
+  for (int col = c0; col < c1; ++col) {
+    const int buf = (col - c0) & 1;
+    if (col + 1 < c1)
+      stage(col + 1, win + (buf ^ 1) * 3 * kWinElems);
     else
       cp_async_commit();
     cp_async_wait<1>();
     __syncthreads();
-    const Stage<T2>& S = stages[buf];
-    const int tile_id = item / ncols;
-    const int col = item - tile_id * ncols;
-    const DevTile tile = tiles[tile_id];
-    const DevSector& sec = sectors[tile.sector];
-    const int n = sec.n;
-    const int a = tile.a0 + la;
-    const int b0 = tile.b0 + lb;
-    if (a < n && b0 < n) {
-      const int ncol = min(kColsPerThread, n - b0);
-      Acc<T> acc;
+    if (active) {
+      const T2* wb = win + buf * 3 * kWinElems + (la + kHalo) + (lb + kHalo) * kWinRows;
+      T accr[4], acci[4];
 #pragma unroll
-      for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
-      const T2* ca = coef + a;
-      const T2* cb = coef + b0;
-      const T2* wbase = S.win + (la + kHalo) + (lb + kHalo) * kWinRows;  // + woff selects slot, p, q
-      const int4* st = S.st;
-      group<T, T2, K_ADD, C_CX>(st, S.ge[G_ADD], S.ge[G_ADD + 1], ca, cb, wbase, acc);
-      group<T, T2, K_LEFT, C_IM>(st, S.ge[G_LEFT_IM], S.ge[G_LEFT_IM + 1], ca, cb, wbase, acc);
-      group<T, T2, K_LEFT, C_RE>(st, S.ge[G_LEFT_RE], S.ge[G_LEFT_RE + 1], ca, cb, wbase, acc);
-      group<T, T2, K_LEFT, C_CX>(st, S.ge[G_LEFT_CX], S.ge[G_LEFT_CX + 1], ca, cb, wbase, acc);
-      group<T, T2, K_RIGHT, C_IM>(st, S.ge[G_RIGHT_IM], S.ge[G_RIGHT_IM + 1], ca, cb, wbase, acc);
-      group<T, T2, K_RIGHT, C_RE>(st, S.ge[G_RIGHT_RE], S.ge[G_RIGHT_RE + 1], ca, cb, wbase, acc);
-      group<T, T2, K_RIGHT, C_CX>(st, S.ge[G_RIGHT_CX], S.ge[G_RIGHT_CX + 1], ca, cb, wbase, acc);
-      group<T, T2, K_SAND, C_RE>(st, S.ge[G_SAND_RE], S.ge[G_SAND_RE + 1], ca, cb, wbase, acc);
-      group<T, T2, K_SAND, C_CX>(st, S.ge[G_SAND_CX], S.ge[G_SAND_CX + 1], ca, cb, wbase, acc);
+      for (int k = 0; k < 4; ++k) {
+        const T2 xv = wb[woff[0] + k * kWinRows];
+        accr[k] = car[k] * xv.x - cai[k] * xv.y;
+        acci[k] = car[k] * xv.y + cai[k] * xv.x;
+      }
+#pragma unroll
+      for (int i = 0; i < LI; ++i) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const T2 xv = wb[woff[1 + i] + k * kWinRows];
+          accr[k] = fma(-lim[i], xv.y, accr[k]);
+          acci[k] = fma(lim[i], xv.x, acci[k]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < RI; ++i) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const T2 xv = wb[woff[1 + LI + i] + k * kWinRows];
+          accr[k] = fma(-rim[i][k], xv.y, accr[k]);
+          acci[k] = fma(rim[i][k], xv.x, acci[k]);
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < SR; ++i) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const T2 xv = wb[woff[1 + LI + RI + i] + k * kWinRows];
+          accr[k] = fma(sre[i][k], xv.x, accr[k]);
+          acci[k] = fma(sre[i][k], xv.y, acci[k]);
+        }
+      }
       if (border.scale != 1.0) {
         const T scale = (T)border.scale;
 #pragma unroll
-        for (int k = 0; k < kColsPerThread; ++k) {
-          acc.re[k] *= scale;
-          acc.im[k] *= scale;
+        for (int k = 0; k < 4; ++k) {
+          accr[k] *= scale;
+          acci[k] *= scale;
         }
       }
       T2* yp = y + (long long)col * ld + sec.offset + a + (long long)b0 * n;
 #pragma unroll
-      for (int k = 0; k < kColsPerThread; ++k) {
-        if (k >= ncol) break;
+      for (int k = 0; k < 4; ++k) {
+        if (b0 + k >= n) break;
         T2 out;
-        out.x = acc.re[k];
-        out.y = acc.im[k];
+        out.x = accr[k];
+        out.y = acci[k];
         if (b0 + k == a && border.alpha != nullptr) {
           const double2 al = border.alpha[col];
           const double v = border.coords ? sec.border_z : sec.border_x;
@@ -255,7 +402,40 @@ __global__ void __launch_bounds__(kApplyThreads)
         yp[(long long)k * n] = out;
       }
     }
-    __syncthreads();  // every thread is done with stage `buf` before it is refilled
+    __syncthreads();  // stage `buf` is refilled two columns later
+  }
+}
+
+template <typename T, int LI, int RI, int SR>
+cudaError_t launch_apply_rhs(const DevicePlan& dp, const void* coef, const void* x, void* y, int ncols,
+                             long long ld, const BorderArgs& border, cudaStream_t stream) {
+  using T2 = typename Vec2<T>::type;
+  const size_t smem = 2 * 3 * kWinElems * sizeof(T2);
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e =
+        cudaFuncSetAttribute(k_apply_rhs<T, LI, RI, SR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  // chunks of right-hand sides per block: enough blocks to fill the GPU, many columns per
+  // block to amortize the coefficient setup
+  const int rc = ncols >= 64 ? 16 : (ncols >= 16 ? 8 : (ncols >= 4 ? 4 : 1));
+  const long long chunks = (ncols + rc - 1) / rc;
+  const long long grid = chunks * dp.ntiles;
+  k_apply_rhs<T, LI, RI, SR><<<(unsigned)grid, kApplyThreads, smem, stream>>>(
+      dp.sectors, (const int4*)dp.fterms, (const T2*)coef, dp.tiles, dp.ntiles, ncols, rc, (const T2*)x, (T2*)y,
+      ld, border);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_apply_fast(const DevicePlan& dp, const void* coef, const void* x, void* y, int ncols,
+                              long long ld, const BorderArgs& border, cudaStream_t stream) {
+  switch (dp.fast_sr) {
+    case 5: return launch_apply_rhs<T, 2, 2, 5>(dp, coef, x, y, ncols, ld, border, stream);
+    case 9: return launch_apply_rhs<T, 2, 2, 9>(dp, coef, x, y, ncols, ld, border, stream);
+    default: return launch_apply_rhs<T, 2, 2, 13>(dp, coef, x, y, ncols, ld, border, stream);
   }
 }
 
@@ -264,35 +444,31 @@ cudaError_t launch_apply_t(const DevicePlan& dp, const void* coef, const void* x
                            long long ld, const BorderArgs& border, cudaStream_t stream) {
   using T2 = typename Vec2<T>::type;
   if (dp.ntiles == 0 || ncols == 0) return cudaSuccess;
-  const size_t smem = 2 * sizeof(Stage<T2>);
-  static int blocks_per_sm = 0;  // per template instance; the kernel and device are fixed
-  static int sms = 0;
-  if (blocks_per_sm == 0) {
+  const size_t smem = 3 * kWinElems * sizeof(T2);
+  static bool configured = false;  // per template instance, host side
+  if (!configured) {
     cudaError_t e = cudaFuncSetAttribute(k_apply<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int dev = 0;
-    e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int occ = 0;
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_apply<T>, kApplyThreads, smem);
-    if (e != cudaSuccess) return e;
-    blocks_per_sm = occ > 0 ? occ : 1;
+    configured = true;
   }
-  const long long total = (long long)dp.ntiles * ncols;
-  const long long grid = std::min<long long>(total, (long long)sms * blocks_per_sm);
-  k_apply<T><<<(unsigned)grid, kApplyThreads, smem, stream>>>(dp.sectors, dp.terms, (const T2*)coef, dp.tiles,
-                                                               dp.ntiles, ncols, (const T2*)x, (T2*)y, ld, border);
+  dim3 grid((unsigned)dp.ntiles, (unsigned)ncols);
+  k_apply<T><<<grid, kApplyThreads, smem, stream>>>(dp.sectors, dp.terms, (const T2*)coef, dp.tiles,
+                                                    (const T2*)x, (T2*)y, ld, border);
   return cudaGetLastError();
 }
 
 cudaError_t launch_apply_f64(const DevicePlan& dp, const double* x, double* y, int ncols, long long ld,
                              const BorderArgs& border, cudaStream_t stream) {
+  if (dp.fast_sr > 0 && ncols >= kFastMinCols)
+    return launch_apply_fast<double>(dp, dp.coef64, x, y, ncols, ld, border, stream);
   return launch_apply_t<double>(dp, dp.coef64, x, y, ncols, ld, border, stream);
 }
 
 cudaError_t launch_apply_f32(const DevicePlan& dp, const float* x, float* y, int ncols, long long ld,
                              const BorderArgs& border, cudaStream_t stream) {
-  return launch_apply_t<float>(dp, border.coords ? dp.coef32z : dp.coef32x, x, y, ncols, ld, border, stream);
+  const void* coef = border.coords ? dp.coef32z : dp.coef32x;
+  if (dp.fast_sr > 0 && ncols >= kFastMinCols) return launch_apply_fast<float>(dp, coef, x, y, ncols, ld, border, stream);
+  return launch_apply_t<float>(dp, coef, x, y, ncols, ld, border, stream);
 }
 
 }  // namespace picuda

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -97,6 +98,8 @@ int upload_plan(pi_plan* plan) {
       default: return t.cls == CC_REAL ? G_SAND_RE : G_SAND_CX;
     }
   };
+  // grouped terms of every sector, kept for the fixed-structure table below
+  std::vector<std::array<std::vector<DevTerm>, G_COUNT>> by_group(S);
   for (int s = 0; s < S; ++s) {
     const Sector& sec = hp.sectors[s];
     DevSector& ds = sectors[s];
@@ -158,6 +161,7 @@ int upload_plan(pi_plan* plan) {
           pad4();
         }
         terms.push_back(dt);
+        by_group[s][g].push_back(dt);
       }
       ds.group_end[g] = (int)terms.size();
     }
@@ -166,6 +170,46 @@ int upload_plan(pi_plan* plan) {
     for (int a = 0; a < sec.n; ++a) {
       diag_sector.push_back(s);
       diag_index.push_back(sec.offset + a + (long long)a * sec.n);
+    }
+  }
+  // Fixed-structure table for the batched kernel: one ADD, two imaginary LEFT, two
+  // imaginary RIGHT and fast_sr real sandwich terms per sector, padded with zero terms.
+  std::vector<DevTerm> fterms;
+  int fast_sr = 0;
+  {
+    bool ok = true;
+    int max_sr = 0;
+    for (int s = 0; s < S && ok; ++s) {
+      const auto& g = by_group[s];
+      ok = g[G_LEFT_RE].empty() && g[G_LEFT_CX].empty() && g[G_RIGHT_RE].empty() && g[G_RIGHT_CX].empty() &&
+           g[G_SAND_CX].empty() && g[G_ADD].size() <= 1 && g[G_LEFT_IM].size() <= 2 && g[G_RIGHT_IM].size() <= 2;
+      max_sr = std::max(max_sr, (int)g[G_SAND_RE].size());
+    }
+    if (ok && max_sr <= 13) {
+      fast_sr = max_sr <= 5 ? 5 : (max_sr <= 9 ? 9 : 13);
+      while (coef64.size() % 4) {
+        coef64.push_back(make_double2(0, 0));
+        coef32x.push_back(make_float2(0, 0));
+        coef32z.push_back(make_float2(0, 0));
+      }
+      const int zero_off = (int)coef64.size();
+      const int zlen = ((hp.max_n + 3) / 4) * 4 + 4;
+      for (int i = 0; i < zlen; ++i) {
+        coef64.push_back(make_double2(0, 0));
+        coef32x.push_back(make_float2(0, 0));
+        coef32z.push_back(make_float2(0, 0));
+      }
+      const DevTerm zero{kWinElems, zero_off, zero_off, 0};  // centre of the own-sector window
+      auto put = [&](const std::vector<DevTerm>& v, int count) {
+        for (int i = 0; i < count; ++i) fterms.push_back(i < (int)v.size() ? v[i] : zero);
+      };
+      for (int s = 0; s < S; ++s) {
+        const auto& g = by_group[s];
+        put(g[G_ADD], 1);
+        put(g[G_LEFT_IM], 2);
+        put(g[G_RIGHT_IM], 2);
+        put(g[G_SAND_RE], fast_sr);
+      }
     }
   }
   // Largest sectors first: their tiles are the longest-running.
@@ -181,6 +225,12 @@ int upload_plan(pi_plan* plan) {
   if ((rc = upload(plan, coef32x, &plan->dev.coef32x))) return rc;
   if ((rc = upload(plan, coef32z, &plan->dev.coef32z))) return rc;
   if ((rc = upload(plan, diag_sector, &plan->dev.diag_sector))) return rc;
+  if (fast_sr > 0) {
+    const DevTerm* ft = nullptr;
+    if ((rc = upload(plan, fterms, &ft))) return rc;
+    plan->dev.fterms = reinterpret_cast<const int4*>(ft);
+    plan->dev.fast_sr = fast_sr;
+  }
   if ((rc = upload(plan, diag_index, &plan->dev.diag_index))) return rc;
   plan->dev.nsectors = S;
   plan->dev.ntiles = (int)tiles.size();

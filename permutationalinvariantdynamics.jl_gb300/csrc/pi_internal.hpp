@@ -20,11 +20,17 @@ struct DevicePlan {
   const float2* coef32z = nullptr;   // FP32 coefficients in population coordinates
   const int* diag_sector = nullptr;  // per diagonal entry: its sector
   const long long* diag_index = nullptr;  // per diagonal entry: its element index
+  const int4* fterms = nullptr;     // padded fixed-structure term table (batched apply)
+  int fast_sr = 0;                   // real sandwich terms per sector of the fixed structure (0: none)
   int nsectors = 0;
   int ntiles = 0;
   int ndiag = 0;
   long long dim = 0;
 };
+
+// Applies with at least this many right-hand sides use the fixed-structure batched kernel
+// when the plan has one.
+constexpr int kFastMinCols = 2;
 
 // Apply kernels (pi_apply.cu).
 cudaError_t launch_apply_f64(const DevicePlan& dp, const double* x, double* y, int ncols, long long ld,
