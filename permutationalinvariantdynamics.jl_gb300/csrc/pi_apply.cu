@@ -298,36 +298,51 @@ __global__ void __launch_bounds__(kApplyThreads, sizeof(T) == 4 ? 2 : 1)
     for (int k = 0; k < 4; ++k) sre[i][k] = al * be[k].x;
   }
 
-  // Staging plan of this thread: rows la and 32 + la of each source window.
-  int sR[3], sm[3], sc0[3];
-  long long soff[3];
-  bool srv[3], srv2[3];
+  // Staging plan of this thread, fixed for the tile: rows la and 32 + la of window columns
+  // warp, warp + 8, ..., of each source window.  Validity is a bitmask and the source
+  // pointers advance by a constant per column, so staging one right-hand side costs a
+  // pointer bump and one cp.async per element.
+  constexpr int kIters = (kWinCols + kApplyWarps - 1) / kApplyWarps;  // 5
+  const bool extra = la < kWinRows - 32;
+  unsigned long long vmask = 0;
+  long long gbase[3];
+  int gstep[3];
+  bool have[3];
 #pragma unroll
   for (int slot = 0; slot < 3; ++slot) {
     const int s2 = sec.src[slot];
-    sm[slot] = s2 >= 0 ? sectors[s2].n : 0;
-    soff[slot] = s2 >= 0 ? sectors[s2].offset : 0;
-    const int r0 = tile.a0 + slot - 1 - kHalo;
-    sc0[slot] = tile.b0 + slot - 1 - kHalo;
-    sR[slot] = r0 + la;
-    srv[slot] = (unsigned)(r0 + la) < (unsigned)sm[slot];
-    srv2[slot] = la < kWinRows - 32 && (unsigned)(r0 + 32 + la) < (unsigned)sm[slot];
+    have[slot] = s2 >= 0;
+    const int m = have[slot] ? sectors[s2].n : 0;
+    const int R = tile.a0 + slot - 1 - kHalo + la;
+    const int C0 = tile.b0 + slot - 1 - kHalo + warp;
+    gbase[slot] = (have[slot] ? sectors[s2].offset : 0) + R + (long long)C0 * m;
+    gstep[slot] = kApplyWarps * m;
+    const bool rv = (unsigned)R < (unsigned)m, rv2 = extra && (unsigned)(R + 32) < (unsigned)m;
+#pragma unroll
+    for (int it = 0; it < kIters; ++it) {
+      const int j = warp + it * kApplyWarps;
+      const bool cv = j < kWinCols && (unsigned)(C0 + it * kApplyWarps) < (unsigned)m;
+      if (rv && cv) vmask |= 1ull << (slot * 2 * kIters + 2 * it);
+      if (rv2 && cv) vmask |= 1ull << (slot * 2 * kIters + 2 * it + 1);
+    }
   }
   auto stage = [&](int col, T2* w) {
     const T2* xc = x + (long long)col * ld;
 #pragma unroll
     for (int slot = 0; slot < 3; ++slot) {
-      if (sm[slot] == 0) continue;
-      const T2* xs = xc + soff[slot];
-      T2* ws = w + slot * kWinElems;
-      const int m = sm[slot];
-      for (int j = warp; j < kWinCols; j += kApplyWarps) {
-        const int C = sc0[slot] + j;
-        const bool cv = (unsigned)C < (unsigned)m;
-        const bool v1 = srv[slot] && cv, v2 = srv2[slot] && cv;
-        const T2* g = xs + sR[slot] + C * m;
-        cp_async_zfill<sizeof(T2)>(ws + la + j * kWinRows, v1 ? g : xs, v1);
-        if (la < kWinRows - 32) cp_async_zfill<sizeof(T2)>(ws + 32 + la + j * kWinRows, v2 ? g + 32 : xs, v2);
+      if (!have[slot]) continue;
+      const T2* g = xc + gbase[slot];
+      T2* ws = w + slot * kWinElems + la + warp * kWinRows;
+#pragma unroll
+      for (int it = 0; it < kIters; ++it) {
+        if (warp + it * kApplyWarps < kWinCols) {
+          const bool v1 = (vmask >> (slot * 2 * kIters + 2 * it)) & 1ull;
+          const bool v2 = (vmask >> (slot * 2 * kIters + 2 * it + 1)) & 1ull;
+          cp_async_zfill<sizeof(T2)>(ws, v1 ? g : xc, v1);
+          if (extra) cp_async_zfill<sizeof(T2)>(ws + 32, v2 ? g + 32 : xc, v2);
+        }
+        g += gstep[slot];
+        ws += kApplyWarps * kWinRows;
       }
     }
     cp_async_commit();
