@@ -348,6 +348,11 @@ __global__ void __launch_bounds__(kApplyThreads, sizeof(T) == 4 ? 2 : 1)
     cp_async_commit();
   };
 
+  // FP64 comparisons and conversions run on GB300's narrow FP64 pipe: decide once per block
+  const bool do_scale = border.scale != 1.0;
+  const T scale = (T)border.scale;
+  const bool has_border = border.alpha != nullptr;
+  const bool diag_tile = tile.a0 == tile.b0;
   stage(c0, win);
   for (int col = c0; col < c1; ++col) {
     const int buf = (col - c0) & 1;
@@ -393,8 +398,7 @@ __global__ void __launch_bounds__(kApplyThreads, sizeof(T) == 4 ? 2 : 1)
           acci[k] = fma(sre[i][k], xv.y, acci[k]);
         }
       }
-      if (border.scale != 1.0) {
-        const T scale = (T)border.scale;
+      if (do_scale) {
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
           accr[k] *= scale;
@@ -408,7 +412,7 @@ __global__ void __launch_bounds__(kApplyThreads, sizeof(T) == 4 ? 2 : 1)
         T2 out;
         out.x = accr[k];
         out.y = acci[k];
-        if (b0 + k == a && border.alpha != nullptr) {
+        if (has_border && diag_tile && b0 + k == a) {
           const double2 al = border.alpha[col];
           const double v = border.coords ? sec.border_z : sec.border_x;
           out.x += (T)(al.x * v);
