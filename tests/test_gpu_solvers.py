@@ -121,3 +121,26 @@ def test_expv_mixed_vs_fp64_c2_small(torch_cuda):
     for k in obs:
         err = np.abs(rmx.values[k] - r64.values[k]).max() / np.abs(r64.values[k]).max()
         assert err <= 1e-4, (k, err)
+
+
+def test_golden_fixtures_on_gpu(torch_cuda):
+    """Committed oracle fixtures (tests/golden/driven_qubits_N8.npz) reproduced on the GPU."""
+    from pathlib import Path
+    g = np.load(Path(__file__).resolve().parent / "golden" / "driven_qubits_N8.npz")
+    model = M.driven_c1(8)
+    compiled = picuda.compile(model)
+    _, offs, _ = compiled.library_sectors()
+    assert np.array_equal(offs, g["offsets"][:-1])
+    idx, val = compiled.library_trace_functional()
+    assert np.array_equal(idx, g["trace_idx"]) and np.array_equal(val, g["trace_val"])
+    y = np.empty_like(g["x"])
+    picuda.apply_(y, compiled, g["x"].copy())
+    assert np.abs(y - g["Lx"]).max() <= 1e-12 * np.abs(g["Lx"]).max()
+    ss = picuda.stationary_state(compiled, operator_scale=float(g["steady_operator_scale"]))
+    assert np.abs(ss.data - g["steady"]).max() <= 1e-9
+    s = picuda.spin_matrices(2)
+    res = picuda.solve_dynamics(compiled, picuda.computational_product_state(model.basis, 2), (0.0, 4.0),
+                                saveat=0.1, observables={"excited": s["jp"] @ s["jm"], "Jz": s["jz"]},
+                                save_states=False)
+    assert np.allclose(res.values["excited"], g["excited"], atol=1e-8)
+    assert np.allclose(res.values["Jz"], g["Jz"], atol=1e-8)
