@@ -149,6 +149,19 @@ int pi_apply_host_f32(pi_plan* plan, float* y_host, const float* x_host, int nco
 /* Device dot(a, b) = sum conj(a) b, FP64, deterministic two-stage reduction. */
 int pi_dot_f64(pi_plan* plan, const double* a_dev, const double* b_dev, double* out_host2);
 
+/* Allocation-free multi-dot: h_dev[i] = sum_e conj(V_i[e]) w[e] for i < nv, with V the nv
+ * columns of length n at leading dimension ldv (complex FP64, device).  No counterpart in
+ * the reference.  For callers that cannot call cudaMalloc when they need a reduction --
+ * device memory owned by another pool (a Julia caller's CUDA.jl allocator), serving loops
+ * that fix their memory at start-up, enqueueing while a stream is captured -- its partial
+ * sums live in a static device array inside this library (128 KiB, kept on every GPU that
+ * loads the library until exit), so it allocates nothing.  nv is limited to 32 (larger nv
+ * is rejected).  The first call on a device looks up the array's device address and should
+ * come before any stream capture.  Calls share the array: two calls that overlap on the GPU
+ * race.  Asynchronous on `stream` (NULL = default stream). */
+int pi_mdot_f64_noalloc(const double* V_dev, long long ldv, int nv, const double* w_dev, long long n,
+                        double* h_dev, void* stream);
+
 /* ---- steady state: krylov_steady_state (krylov.jl:797-891) -------------------------- */
 
 typedef struct {

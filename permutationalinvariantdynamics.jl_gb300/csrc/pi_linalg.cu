@@ -529,3 +529,123 @@ cudaError_t weighted_norm2_z(const DevicePlan& dp, const double2* z, ReduceScrat
 }
 
 }  // namespace picuda
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free multi-dot.
+//
+// Some callers cannot allocate device memory at the time they need a reduction: a Julia
+// package whose device memory is owned by its own pool (CUDA.jl) and must not see foreign
+// cudaMalloc/cudaFree calls, a serving loop that forbids allocation after start-up so its
+// memory budget cannot move, or code that enqueues work while a stream is being captured
+// (cudaMalloc is not allowed inside a capture).  For them, pi_mdot_f64_noalloc computes
+// h[i] = sum_e conj(V_i[e]) w[e] with its partial sums in a fixed device array that lives in
+// this library image: kNoAllocBlocks x kNoAllocMaxDots complex doubles (128 KiB), held on
+// every GPU that loads the library until the process exits.
+// ---------------------------------------------------------------------------------------
+namespace picuda {
+namespace {
+
+constexpr int kNoAllocBlocks = 256;
+constexpr int kNoAllocMaxDots = 32;
+
+static __device__ __align__(256) double2 g_noalloc_partials[kNoAllocBlocks * kNoAllocMaxDots];
+
+// Same arithmetic as the plan-owned multi-dot, with the partial stride of the static array.
+__global__ void __launch_bounds__(kReduceThreads)
+    k_mdot_partial_noalloc(const double2* __restrict__ V, long long ldv, int nv, const double2* __restrict__ w,
+                           long long n, double2* __restrict__ partial) {
+  __shared__ double smem[32 * 2 * kDotGroup];
+  long long beg, end;
+  chunk_bounds(n, beg, end);
+  const int g = blockIdx.y * kDotGroup;
+  const int cnt = min(kDotGroup, nv - g);
+  double acc[2 * kDotGroup];
+#pragma unroll
+  for (int k = 0; k < 2 * kDotGroup; ++k) acc[k] = 0.0;
+  for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+    const double2 wv = w[e];
+#pragma unroll
+    for (int k = 0; k < kDotGroup; ++k) {
+      if (k < cnt) {
+        const double2 v = V[(long long)(g + k) * ldv + e];
+        acc[2 * k] = fma(v.x, wv.x, acc[2 * k]);
+        acc[2 * k] = fma(v.y, wv.y, acc[2 * k]);
+        acc[2 * k + 1] = fma(v.x, wv.y, acc[2 * k + 1]);
+        acc[2 * k + 1] = fma(-v.y, wv.x, acc[2 * k + 1]);
+      }
+    }
+  }
+  block_sum<2 * kDotGroup>(acc, smem);
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < cnt; ++k)
+      partial[(long long)blockIdx.x * kNoAllocMaxDots + g + k] = make_double2(acc[2 * k], acc[2 * k + 1]);
+  }
+}
+
+__global__ void __launch_bounds__(kReduceThreads)
+    k_mdot_final_noalloc(const double2* __restrict__ partial, int nblocks, double2* __restrict__ out) {
+  __shared__ double smem[32 * 2];
+  const int i = blockIdx.x;
+  double acc[2] = {0, 0};
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    const double2 p = partial[(long long)b * kNoAllocMaxDots + i];
+    acc[0] += p.x;
+    acc[1] += p.y;
+  }
+  block_sum<2>(acc, smem);
+  if (threadIdx.x == 0) out[i] = make_double2(acc[0], acc[1]);
+}
+
+}  // namespace
+
+}  // namespace picuda
+
+#include <mutex>
+
+#include "../../include/picuda.h"
+
+namespace picuda {
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+}  // namespace picuda
+
+extern "C" int pi_mdot_f64_noalloc(const double* V_dev, long long ldv, int nv, const double* w_dev, long long n,
+                                   double* h_dev, void* stream) {
+  using namespace picuda;
+  if (!V_dev || !w_dev || !h_dev) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  if (nv < 1 || nv > kNoAllocMaxDots)
+    return fail(PI_ERR_INVALID_ARGUMENT,
+                "nv must lie in 1:32, the capacity of the static scratch of pi_mdot_f64_noalloc");
+  if (n < 1 || ldv < n) return fail(PI_ERR_DIMENSION, "need n >= 1 and ldv >= n");
+  // The address of the static array on the current device, looked up once per device with
+  // that device current (the host-side symbol is only a stand-in, not a device address).
+  static std::mutex mu;
+  static double2* addr[64] = {nullptr};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return fail(PI_ERR_UNSUPPORTED, "device ordinal beyond 63");
+  double2* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the static scratch");
+      addr[dev] = (double2*)p;
+    }
+    scratch = addr[dev];
+  }
+  const int gy = (nv + kDotGroup - 1) / kDotGroup;
+  long long gx = (n + 4LL * kReduceThreads - 1) / (4LL * kReduceThreads);
+  gx = std::max(1LL, std::min(gx, (long long)(kNoAllocBlocks / gy)));
+  cudaStream_t s = (cudaStream_t)stream;
+  // Every partial that the final pass reads is written by the first pass of the same call,
+  // so nothing needs clearing; two calls that overlap on the GPU share the array and race.
+  k_mdot_partial_noalloc<<<dim3((unsigned)gx, gy), kReduceThreads, 0, s>>>(
+      (const double2*)V_dev, ldv, nv, (const double2*)w_dev, n, scratch);
+  k_mdot_final_noalloc<<<nv, kReduceThreads, 0, s>>>(scratch, (int)gx, (double2*)h_dev);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "pi_mdot_f64_noalloc launch");
+  return PI_OK;
+}

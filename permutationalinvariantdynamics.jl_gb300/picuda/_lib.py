@@ -115,6 +115,7 @@ PROTOTYPES = {
     "pi_apply_host_f64": (C.c_int, [_P, _P, _P, C.c_int]),
     "pi_apply_host_f32": (C.c_int, [_P, _P, _P, C.c_int, C.c_int]),
     "pi_dot_f64": (C.c_int, [_P, _P, _P, _D]),
+    "pi_mdot_f64_noalloc": (C.c_int, [_P, C.c_longlong, C.c_int, _P, C.c_longlong, _P, _P]),
     "pi_gmres_default_opts": (None, [C.POINTER(pi_gmres_opts_t)]),
     "pi_steady_state": (C.c_int, [_P, _P, C.POINTER(pi_gmres_opts_t), C.POINTER(pi_gmres_info_t)]),
     "pi_expv_default_opts": (None, [C.POINTER(pi_expv_opts_t)]),
