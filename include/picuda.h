@@ -229,6 +229,114 @@ int pi_solve_dynamics(pi_plan* plan, double* rho_dev, int nt, const double* time
                       int nobs, const double* obs_dev, double* values_host,
                       const pi_expv_opts_t* opts, pi_expv_info_t* info);
 
+/* ---- batched solves over many plans (parameter scans, mixed particle numbers) --------
+ * One engine advances every instance together: each Arnoldi step of all instances is one
+ * launch per kernel over an (instance, sector-tile) or (instance, element-chunk) work list,
+ * each Krylov cycle runs as one CUDA graph with the step index and stop flags in device
+ * memory, and the host runs the reference's controller per instance between cycles.  An
+ * instance's arithmetic does not depend on the other instances in the batch.  The plans
+ * are only read (several instances may share one plan); state buffers must be distinct.
+ * The reference has no batched entry point: these replace a loop over parameter points
+ * that calls solve_dynamics / stationary_state (scans.jl:1457 parameter_scan) per point.
+ * krylovdim is limited to 1..120.  Returns PI_OK when every instance succeeded, else the
+ * first failing instance's status (its message names the instance); infos[i] is filled
+ * for every instance either way. */
+
+/* Batched krylov_expv!: x_devs[i] <- exp(t[i] L_i) x_devs[i]. */
+int pi_expv_batch(int ninst, pi_plan* const* plans, double* const* x_devs, const double* t,
+                  const pi_expv_opts_t* opts, pi_expv_info_t* infos);
+
+/* One job of pi_dynamics_batch: pi_solve_dynamics's arguments for one instance. */
+typedef struct {
+  pi_plan* plan;
+  double* state_dev;      /* in: initial state, out: state at times[nt-1] (device) */
+  int nt;                 /* saved times (>= 1), nondecreasing */
+  const double* times;    /* host */
+  int nobs;               /* 0..16 observables */
+  const double* obs_dev;  /* nobs x dim complex (device) */
+  double* values_host;    /* nt x nobs complex: values[(it*nobs + o)*2 + {0,1}] */
+} pi_dynamics_job_t;
+
+/* Batched solve_dynamics(...; algorithm=ExpvAlgorithm, saveat, observables,
+ * save_states=false) (highlevel.jl:559-733). */
+int pi_dynamics_batch(int njobs, const pi_dynamics_job_t* jobs, const pi_expv_opts_t* opts,
+                      pi_expv_info_t* infos);
+
+/* Batched stationary states (krylov.jl:797-891) into x_devs[i].  The operator-scale
+ * probes come from a counter-based generator on the device (seeded per call), so the
+ * estimated scale agrees with pi_steady_state's to tolerance, not bitwise. */
+int pi_steady_state_batch(int ninst, pi_plan* const* plans, double* const* x_devs,
+                          const pi_gmres_opts_t* opts, pi_gmres_info_t* infos);
+
+/* ---- serving: continuous batching of time-evolution and steady-state requests --------
+ * A server owns one batched engine and a worker thread.  Requests are admitted in arrival
+ * order between engine ticks while their device footprint (Krylov basis, image and state
+ * vectors; the plan tables belong to the caller) fits memory_budget and fewer than
+ * max_active requests run; admitted requests join the next tick's batched launches and
+ * keep their states and Krylov bases resident until they finish.  A request's arithmetic
+ * does not depend on the other requests it shares ticks with.  The reference has no
+ * serving layer; a request is the work of one solve_dynamics(...; saveat=dt) call
+ * (highlevel.jl:559-733) or one stationary_state call (krylov.jl:797-891).
+ * The caller keeps the plan, the state buffer and any observable buffers alive and
+ * untouched until the request's completion has been polled; the state is complete when
+ * the completion is posted. */
+typedef struct pi_server pi_server;
+
+typedef struct {
+  int krylovdim;         /* Krylov dimension of every request (default 30, <= 120) */
+  int precision;         /* PI_FP64, or PI_FP32 (FP32 applies and basis, FP64 rest) */
+  double memory_budget;  /* device bytes admitted requests may hold (default 160e9) */
+  int max_active;        /* concurrent requests, 0 = unlimited */
+  int use_graphs;        /* capture each Krylov cycle as a CUDA graph (default 1) */
+} pi_server_opts_t;
+
+enum { PI_REQUEST_DYNAMICS = 0, PI_REQUEST_STEADY = 1 };
+
+typedef struct {
+  int kind;                  /* PI_REQUEST_DYNAMICS or PI_REQUEST_STEADY */
+  pi_plan* plan;
+  double* state_dev;         /* dynamics: initial state in, final state out; steady: output */
+  double t_final;            /* dynamics: saved times 0:dt:t_final (+ t_final) */
+  double dt;
+  double atol, rtol;         /* <= 0: the solver defaults (1e-10, 1e-8) */
+  int maxiter;               /* steady: <= 0 default 500 */
+  int nobs;                  /* dynamics: 0..16 observables, values at every saved time */
+  const double* obs_dev;
+  double* values_host;       /* nt x nobs complex (nt from the saved-time grid) */
+  unsigned long long tag;    /* caller's request id, returned in the completion */
+} pi_request_t;
+
+typedef struct {
+  unsigned long long tag;
+  int kind;
+  int status;                /* PI_OK or the request's error code */
+  double submit_time;        /* seconds since pi_server_create */
+  double start_time;         /* admission */
+  double finish_time;
+  int iterations;            /* dynamics: accepted steps; steady: GMRES iterations */
+  int operator_applications;
+  double residual;           /* dynamics: summed error estimate; steady: normalized residual */
+  double trace_error;        /* steady */
+  char message[160];
+} pi_completion_t;
+
+typedef struct {
+  long long submitted, admitted, completed, queued, active;
+  double bytes_in_use;
+  long long ticks, cycles, arnoldi_steps;
+  double elapsed;
+} pi_server_stats_t;
+
+void pi_server_default_opts(pi_server_opts_t* opts);
+int pi_server_create(const pi_server_opts_t* opts, int device, pi_server** out);
+/* Thread-safe, non-blocking.  PI_ERR_OUT_OF_MEMORY when the request alone exceeds the budget. */
+int pi_server_submit(pi_server* server, const pi_request_t* request);
+/* Returns up to max completions; waits up to timeout_ms (< 0: until one is available). */
+int pi_server_poll(pi_server* server, pi_completion_t* out, int max, int* count, int timeout_ms);
+int pi_server_stats(pi_server* server, pi_server_stats_t* stats);
+/* Stops after the current tick; unfinished requests are abandoned. */
+int pi_server_destroy(pi_server* server);
+
 #ifdef __cplusplus
 }
 #endif

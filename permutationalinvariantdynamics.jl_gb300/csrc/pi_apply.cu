@@ -20,114 +20,11 @@
 // strided as tensor maps require.
 #include <algorithm>
 
+#include "pi_apply_impl.cuh"
 #include "pi_device.cuh"
 #include "pi_internal.hpp"
 
 namespace picuda {
-
-template <typename T>
-struct Vec2;
-template <>
-struct Vec2<double> {
-  using type = double2;
-};
-template <>
-struct Vec2<float> {
-  using type = float2;
-};
-
-enum Kind { K_ADD, K_LEFT, K_RIGHT, K_SAND };
-enum Cls { C_RE, C_IM, C_CX };
-
-template <typename T>
-struct Acc {
-  T re[kColsPerThread];
-  T im[kColsPerThread];
-};
-
-// beta[b0 .. b0+3] of one term: b0 and every beta array start are multiples of 4, so the
-// four coefficients are read with aligned vector loads.
-__device__ __forceinline__ void load4(const float2* p, float2 (&v)[4]) {
-  const float4 u0 = __ldg(reinterpret_cast<const float4*>(p));
-  const float4 u1 = __ldg(reinterpret_cast<const float4*>(p) + 1);
-  v[0] = make_float2(u0.x, u0.y);
-  v[1] = make_float2(u0.z, u0.w);
-  v[2] = make_float2(u1.x, u1.y);
-  v[3] = make_float2(u1.z, u1.w);
-}
-__device__ __forceinline__ void load4(const double2* p, double2 (&v)[4]) {
-#pragma unroll
-  for (int k = 0; k < 4; ++k) v[k] = __ldg(p + k);
-}
-
-// One stencil term for the thread's row and 4 columns, reading the zero-padded source
-// windows in shared memory (no bounds checks).  ca points at coef + a, cb at coef + b0.
-template <typename T, typename T2, int KIND, int CLS>
-__device__ __forceinline__ void term(const int4 tm, const T2* __restrict__ ca, const T2* __restrict__ cb,
-                                     const T2* wbase, Acc<T>& acc) {
-  T2 al;
-  if (KIND != K_RIGHT) al = __ldg(ca + tm.y);
-  T2 be[4];
-  if (KIND != K_LEFT) load4(cb + tm.z, be);
-  const T2* wp = wbase + tm.x;
-#pragma unroll
-  for (int k = 0; k < kColsPerThread; ++k) {
-    const T2 xv = wp[k * kWinRows];
-    T cr, ci;  // combined coefficient
-    if (KIND == K_ADD) {
-      cr = al.x + be[k].x;
-      ci = al.y + be[k].y;
-    } else if (KIND == K_LEFT) {
-      cr = al.x;
-      ci = al.y;
-    } else if (KIND == K_RIGHT) {
-      cr = be[k].x;
-      ci = be[k].y;
-    } else if (CLS == C_RE) {
-      cr = al.x * be[k].x;
-      ci = 0;
-    } else {
-      cr = al.x * be[k].x - al.y * be[k].y;
-      ci = al.x * be[k].y + al.y * be[k].x;
-    }
-    if (CLS == C_RE && KIND != K_ADD) {
-      acc.re[k] = fma(cr, xv.x, acc.re[k]);
-      acc.im[k] = fma(cr, xv.y, acc.im[k]);
-    } else if (CLS == C_IM && KIND != K_ADD) {
-      acc.re[k] = fma(-ci, xv.y, acc.re[k]);
-      acc.im[k] = fma(ci, xv.x, acc.im[k]);
-    } else {
-      acc.re[k] = fma(cr, xv.x, acc.re[k]);
-      acc.re[k] = fma(-ci, xv.y, acc.re[k]);
-      acc.im[k] = fma(cr, xv.y, acc.im[k]);
-      acc.im[k] = fma(ci, xv.x, acc.im[k]);
-    }
-  }
-}
-
-template <typename T, typename T2, int KIND, int CLS>
-__device__ __forceinline__ void group(const int4* st, int g0, int g1, const T2* __restrict__ ca,
-                                      const T2* __restrict__ cb, const T2* wbase, Acc<T>& acc) {
-  for (int t = g0; t < g1; ++t) term<T, T2, KIND, CLS>(st[t], ca, cb, wbase, acc);
-}
-
-// Asynchronous global -> shared copies (cp.async) with hardware zero fill: a source size of
-// 0 writes zeros and reads nothing, which pads the halo and the block edges for free.
-template <int BYTES>
-__device__ __forceinline__ void cp_async_zfill(void* smem, const void* gmem, bool valid) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  const int sz = valid ? BYTES : 0;
-  if (BYTES == 16)
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gmem), "n"(BYTES), "r"(sz)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
 
 template <typename T>
 __global__ void __launch_bounds__(kApplyThreads)
@@ -140,86 +37,9 @@ __global__ void __launch_bounds__(kApplyThreads)
   T2* win = reinterpret_cast<T2*>(smem_raw);  // [3][kWinElems] source windows
   __shared__ int4 st[kMaxSectorTerms];
   __shared__ int ge[G_COUNT + 1];
-  const DevTile tile = tiles[blockIdx.x];
-  const DevSector& sec = sectors[tile.sector];
   const long long col = blockIdx.y;
-  x += col * ld;
-  y += col * ld;
-  const int tb = sec.term_begin;
-  const int nt = sec.group_end[G_COUNT - 1] - tb;
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
-  if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
-  const int la = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  // Stage the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every
-  // source sector (e = -1, 0, +1): lane = window row (plus rows 32..35 on lanes 0..3),
-  // warps stride over the 36 window columns.
-#pragma unroll 1
-  for (int slot = 0; slot < 3; ++slot) {
-    const int s2 = sec.src[slot];
-    if (s2 < 0) continue;
-    const int m = sectors[s2].n;
-    const T2* xs = x + sectors[s2].offset;
-    const int r0 = tile.a0 + slot - 1 - kHalo, c0 = tile.b0 + slot - 1 - kHalo;
-    T2* w = win + slot * kWinElems;
-    const int R = r0 + la, R2 = r0 + 32 + la;
-    const bool rv = (unsigned)R < (unsigned)m, rv2 = la < kWinRows - 32 && (unsigned)R2 < (unsigned)m;
-    for (int j = warp; j < kWinCols; j += kApplyWarps) {
-      const int C = c0 + j;
-      const bool cv = (unsigned)C < (unsigned)m;
-      T2 v, v2;
-      v.x = v.y = v2.x = v2.y = 0;
-      if (rv && cv) v = __ldg(xs + R + C * m);
-      if (rv2 && cv) v2 = __ldg(xs + R2 + C * m);
-      w[la + j * kWinRows] = v;
-      if (la < kWinRows - 32) w[32 + la + j * kWinRows] = v2;
-    }
-  }
-  __syncthreads();
-  const int n = sec.n;
-  const int lb = warp * kColsPerThread;
-  const int a = tile.a0 + la;
-  const int b0 = tile.b0 + lb;
-  if (a >= n || b0 >= n) return;
-  const int ncol = min(kColsPerThread, n - b0);
-  Acc<T> acc;
-#pragma unroll
-  for (int k = 0; k < kColsPerThread; ++k) acc.re[k] = acc.im[k] = 0;
-  const T2* ca = coef + a;
-  const T2* cb = coef + b0;
-  const T2* wbase = win + (la + kHalo) + (lb + kHalo) * kWinRows;  // + woff selects slot, p, q
-  group<T, T2, K_ADD, C_CX>(st, ge[G_ADD], ge[G_ADD + 1], ca, cb, wbase, acc);
-  group<T, T2, K_LEFT, C_IM>(st, ge[G_LEFT_IM], ge[G_LEFT_IM + 1], ca, cb, wbase, acc);
-  group<T, T2, K_LEFT, C_RE>(st, ge[G_LEFT_RE], ge[G_LEFT_RE + 1], ca, cb, wbase, acc);
-  group<T, T2, K_LEFT, C_CX>(st, ge[G_LEFT_CX], ge[G_LEFT_CX + 1], ca, cb, wbase, acc);
-  group<T, T2, K_RIGHT, C_IM>(st, ge[G_RIGHT_IM], ge[G_RIGHT_IM + 1], ca, cb, wbase, acc);
-  group<T, T2, K_RIGHT, C_RE>(st, ge[G_RIGHT_RE], ge[G_RIGHT_RE + 1], ca, cb, wbase, acc);
-  group<T, T2, K_RIGHT, C_CX>(st, ge[G_RIGHT_CX], ge[G_RIGHT_CX + 1], ca, cb, wbase, acc);
-  group<T, T2, K_SAND, C_RE>(st, ge[G_SAND_RE], ge[G_SAND_RE + 1], ca, cb, wbase, acc);
-  group<T, T2, K_SAND, C_CX>(st, ge[G_SAND_CX], ge[G_SAND_CX + 1], ca, cb, wbase, acc);
-  if (border.scale != 1.0) {
-    const T scale = (T)border.scale;
-#pragma unroll
-    for (int k = 0; k < kColsPerThread; ++k) {
-      acc.re[k] *= scale;
-      acc.im[k] *= scale;
-    }
-  }
-  T2* yp = y + sec.offset + a + (long long)b0 * n;
-#pragma unroll
-  for (int k = 0; k < kColsPerThread; ++k) {
-    if (k >= ncol) break;
-    T2 out;
-    out.x = acc.re[k];
-    out.y = acc.im[k];
-    if (b0 + k == a && border.alpha != nullptr) {
-      const double2 al = border.alpha[col];
-      const double v = border.coords ? sec.border_z : sec.border_x;
-      out.x += (T)(al.x * v);
-      out.y += (T)(al.y * v);
-    }
-    yp[(long long)k * n] = out;
-  }
+  apply_tile<T>(sectors, terms, coef, tiles[blockIdx.x], x + col * ld, y + col * ld, border,
+                border.alpha != nullptr ? border.alpha + col : nullptr, win, st, ge);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -89,6 +89,44 @@ class pi_expv_info_t(C.Structure):
                 ("trial_evaluations", C.c_int), ("estimated_error", C.c_double)]
 
 
+class pi_dynamics_job_t(C.Structure):
+    _fields_ = [("plan", C.c_void_p), ("state_dev", C.c_void_p), ("nt", C.c_int),
+                ("times", C.POINTER(C.c_double)), ("nobs", C.c_int), ("obs_dev", C.c_void_p),
+                ("values_host", C.POINTER(C.c_double))]
+
+
+class pi_server_opts_t(C.Structure):
+    _fields_ = [("krylovdim", C.c_int), ("precision", C.c_int), ("memory_budget", C.c_double),
+                ("max_active", C.c_int), ("use_graphs", C.c_int)]
+
+
+PI_REQUEST_DYNAMICS = 0
+PI_REQUEST_STEADY = 1
+
+
+class pi_request_t(C.Structure):
+    _fields_ = [("kind", C.c_int), ("plan", C.c_void_p), ("state_dev", C.c_void_p),
+                ("t_final", C.c_double), ("dt", C.c_double), ("atol", C.c_double),
+                ("rtol", C.c_double), ("maxiter", C.c_int), ("nobs", C.c_int),
+                ("obs_dev", C.c_void_p), ("values_host", C.POINTER(C.c_double)),
+                ("tag", C.c_ulonglong)]
+
+
+class pi_completion_t(C.Structure):
+    _fields_ = [("tag", C.c_ulonglong), ("kind", C.c_int), ("status", C.c_int),
+                ("submit_time", C.c_double), ("start_time", C.c_double),
+                ("finish_time", C.c_double), ("iterations", C.c_int),
+                ("operator_applications", C.c_int), ("residual", C.c_double),
+                ("trace_error", C.c_double), ("message", C.c_char * 160)]
+
+
+class pi_server_stats_t(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("admitted", C.c_longlong),
+                ("completed", C.c_longlong), ("queued", C.c_longlong), ("active", C.c_longlong),
+                ("bytes_in_use", C.c_double), ("ticks", C.c_longlong), ("cycles", C.c_longlong),
+                ("arnoldi_steps", C.c_longlong), ("elapsed", C.c_double)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -123,6 +161,19 @@ PROTOTYPES = {
                           C.POINTER(pi_expv_info_t)]),
     "pi_solve_dynamics": (C.c_int, [_P, _P, C.c_int, _D, C.c_int, _P, _D,
                                     C.POINTER(pi_expv_opts_t), C.POINTER(pi_expv_info_t)]),
+    "pi_expv_batch": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P), _D,
+                                C.POINTER(pi_expv_opts_t), C.POINTER(pi_expv_info_t)]),
+    "pi_dynamics_batch": (C.c_int, [C.c_int, C.POINTER(pi_dynamics_job_t),
+                                    C.POINTER(pi_expv_opts_t), C.POINTER(pi_expv_info_t)]),
+    "pi_steady_state_batch": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P),
+                                        C.POINTER(pi_gmres_opts_t),
+                                        C.POINTER(pi_gmres_info_t)]),
+    "pi_server_default_opts": (None, [C.POINTER(pi_server_opts_t)]),
+    "pi_server_create": (C.c_int, [C.POINTER(pi_server_opts_t), C.c_int, C.POINTER(_P)]),
+    "pi_server_submit": (C.c_int, [_P, C.POINTER(pi_request_t)]),
+    "pi_server_poll": (C.c_int, [_P, C.POINTER(pi_completion_t), C.c_int, _I, C.c_int]),
+    "pi_server_stats": (C.c_int, [_P, C.POINTER(pi_server_stats_t)]),
+    "pi_server_destroy": (C.c_int, [_P]),
 }
 
 _lib = None

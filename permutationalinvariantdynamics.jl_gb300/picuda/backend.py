@@ -522,3 +522,135 @@ def solve_dynamics(x, rho0: PIState, tspan, algorithm="expv", saveat=None, obser
     if nobs:
         return DynamicsStreamResult(ts, states, {k: np.array(v) for k, v in series.items()})
     return DynamicsResult(ts, states)
+
+
+# ---------------------------------------------------------------------------------------
+# Batched solves: many plans advance together in one engine (pi_*_batch).  The reference
+# runs such workloads as a loop over parameter points (scans.jl:1457 parameter_scan); each
+# batched result equals the single-instance result to solver tolerance.
+# ---------------------------------------------------------------------------------------
+
+def _device_states(compiled_list, states):
+    torch = _torch()
+    out = []
+    for c, s in zip(compiled_list, states):
+        data = s.data if isinstance(s, PIState) else np.asarray(s)
+        if data.shape != (len(c.basis),):
+            raise PiDimensionMismatch("batch state has the wrong length for its model")
+        out.append(torch.from_numpy(np.ascontiguousarray(data, dtype=np.complex128)).cuda())
+    return out
+
+
+def _ptr_array(ptrs):
+    arr = (C.c_void_p * len(ptrs))()
+    for i, p in enumerate(ptrs):
+        arr[i] = p
+    return arr
+
+
+def krylov_expv_batch(models, states, t, algorithm: ExpvAlgorithm | None = None, return_info=False):
+    """exp(t_i L_i) b_i for every instance in one batched engine run."""
+    torch = _torch()
+    algorithm = algorithm or ExpvAlgorithm()
+    compiled = [_as_compiled(m) for m in models]
+    if len(states) != len(compiled):
+        raise PiDimensionMismatch("one state per model is required")
+    ts = np.broadcast_to(np.asarray(t, dtype=np.float64), (len(compiled),)).copy()
+    xs = _device_states(compiled, states)
+    torch.cuda.synchronize()
+    infos = (_lib.pi_expv_info_t * len(compiled))()
+    o = algorithm.opts()
+    lib = _lib.load()
+    _lib.check(lib.pi_expv_batch(len(compiled), _ptr_array([c.handle for c in compiled]),
+                                 _ptr_array([_ptr(x) for x in xs]), _lib.dptr(ts), C.byref(o), infos),
+               "krylov_expv_batch")
+    out = [x.cpu().numpy() for x in xs]
+    if return_info:
+        return out, [{f: getattr(i, f) for f, _ in i._fields_} for i in infos]
+    return out
+
+
+def solve_dynamics_batch(models, rho0s, tspans, algorithm: ExpvAlgorithm | None = None, saveat=None,
+                         observables=None, return_info=False):
+    """solve_dynamics(...; save_states=false) for many models in one batched engine run.
+
+    tspans and saveat may be one value for all instances or one per instance (a list of n
+    tspans; a list of n saveat grids, each None or a sequence).  Returns one
+    DynamicsStreamResult per instance (values per observable name) plus the final states.
+    """
+    torch = _torch()
+    algorithm = algorithm or ExpvAlgorithm()
+    compiled = [_as_compiled(m) for m in models]
+    n = len(compiled)
+    if len(rho0s) != n:
+        raise PiDimensionMismatch("one initial state per model is required")
+    if isinstance(tspans, tuple) and len(tspans) == 2 and np.isscalar(tspans[0]):
+        tspans = [tspans] * n
+    per_instance = isinstance(saveat, list) and len(saveat) == n and all(
+        v is None or not np.isscalar(v) for v in saveat)
+    saves = saveat if per_instance else [saveat] * n
+    grids = [np.array(saved_times(ts, sv), dtype=np.float64) for ts, sv in zip(tspans, saves)]
+    xs = _device_states(compiled, rho0s)
+    names, obs_dev = [], []
+    if observables:
+        items = list(observables.items()) if isinstance(observables, dict) else list(observables)
+        names = [k for k, _ in items]
+        for c in compiled:
+            datas = [_observable_data(c.basis, v) for _, v in items]
+            obs_dev.append(torch.from_numpy(np.ascontiguousarray(np.stack(datas))).cuda())
+    nobs = len(names)
+    vals = [np.zeros((len(g), max(nobs, 1), 2), dtype=np.float64) for g in grids]
+    jobs = (_lib.pi_dynamics_job_t * n)()
+    for i in range(n):
+        jobs[i].plan = compiled[i].handle
+        jobs[i].state_dev = _ptr(xs[i])
+        jobs[i].nt = len(grids[i])
+        jobs[i].times = _lib.dptr(grids[i])
+        jobs[i].nobs = nobs
+        jobs[i].obs_dev = _ptr(obs_dev[i]) if nobs else None
+        jobs[i].values_host = _lib.dptr(vals[i])
+    infos = (_lib.pi_expv_info_t * n)()
+    o = algorithm.opts()
+    torch.cuda.synchronize()
+    _lib.check(_lib.load().pi_dynamics_batch(n, jobs, C.byref(o), infos), "solve_dynamics_batch")
+    results = []
+    for i in range(n):
+        values = {k: vals[i][:, j, 0] + 1j * vals[i][:, j, 1] for j, k in enumerate(names)}
+        results.append(DynamicsStreamResult(list(grids[i]), None, values))
+    finals = [x.cpu().numpy() for x in xs]
+    if return_info:
+        return results, finals, [{f: getattr(i, f) for f, _ in i._fields_} for i in infos]
+    return results, finals
+
+
+def stationary_state_batch(models, algorithm: GMRESAlgorithm | None = None, atol=1e-10, rtol=1e-8,
+                           operator_scale=None, max_refinements=200, return_info=False,
+                           raise_on_failure=True):
+    """stationary_state for many models in one batched engine run.
+
+    With raise_on_failure=False a non-converged instance does not raise: its info carries
+    converged=False (a scan keeps the points that did converge)."""
+    torch = _torch()
+    algorithm = algorithm or GMRESAlgorithm()
+    compiled = [_as_compiled(m) for m in models]
+    n = len(compiled)
+    o = _lib.pi_gmres_opts_t()
+    lib = _lib.load()
+    lib.pi_gmres_default_opts(C.byref(o))
+    o.krylovdim = algorithm.krylovdim
+    o.maxiter = algorithm.maxiter
+    o.atol, o.rtol = atol, rtol
+    o.operator_scale = float(operator_scale) if operator_scale else 0.0
+    o.precision = _lib.PI_FP32 if algorithm.precision == "mixed" else _lib.PI_FP64
+    o.max_refinements = max_refinements
+    xs = [torch.zeros(len(c.basis), dtype=torch.complex128, device="cuda") for c in compiled]
+    torch.cuda.synchronize()
+    infos = (_lib.pi_gmres_info_t * n)()
+    rc = lib.pi_steady_state_batch(n, _ptr_array([c.handle for c in compiled]),
+                                   _ptr_array([_ptr(x) for x in xs]), C.byref(o), infos)
+    if raise_on_failure or rc != _lib.PI_ERR_NOT_CONVERGED:
+        _lib.check(rc, "stationary_state_batch")
+    states = [PIState(c.basis, x.cpu().numpy()) for c, x in zip(compiled, xs)]
+    if return_info:
+        return states, [{f: getattr(i, f) for f, _ in i._fields_} for i in infos]
+    return states

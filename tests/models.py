@@ -52,3 +52,22 @@ def general(N=6, seed=0, sectors=None):
 def random_state_vector(n, seed):
     rng = np.random.default_rng(seed)
     return (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+
+
+def scan_model(N, omega, gdown, gphi):
+    """Parameter-scan family: H = Omega Jx, local decay gdown, local dephasing gphi,
+    collective decay 1/N on J-."""
+    s = picuda.spin_matrices(2)
+    return picuda.qubit_ensemble_model(N, hamiltonian=omega * s["jx"], emission=gdown, dephasing=gphi,
+                                       collective_emission=1.0 / N)
+
+
+def scan_draws(count, seed=0, nmin=20, nmax=160):
+    """Seeded draws (N, Omega, gdown, gphi): N ~ U{nmin..nmax}, Omega ~ U[0.2, 2],
+    gdown ~ U[0.05, 0.5], gphi ~ U[0, 0.2]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        N = int(rng.integers(nmin, nmax + 1))
+        out.append((N, float(rng.uniform(0.2, 2.0)), float(rng.uniform(0.05, 0.5)), float(rng.uniform(0.0, 0.2))))
+    return out

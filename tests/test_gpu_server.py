@@ -1,0 +1,113 @@
+"""Continuous-batching server (pi_server_*): results against the batched/single entry points,
+independence of a request's result from the requests it shares the engine with, and
+memory-budget admission."""
+import time
+
+import numpy as np
+import pytest
+
+import picuda
+from picuda import _lib
+from tests import models as M
+
+pytestmark = pytest.mark.gpu
+
+EXC = np.array([[0, 0], [0, 1]])
+
+
+@pytest.fixture(scope="module")
+def torch_cuda(lib_built):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _excited(m):
+    return picuda.computational_product_state(m.basis, 2)
+
+
+def test_server_dynamics_and_steady_match_direct_calls(torch_cuda):
+    dyn = [M.scan_model(12, 1.1, 0.2, 0.05), M.driven_c1(8), M.ensemble_c2(16)]
+    std = [M.driven_c1(8), picuda.Models.local_pump_decay(6, down=1.0, up=0.3)]
+    with picuda.Server() as srv:
+        tags = {}
+        for i, m in enumerate(dyn):
+            tags[srv.submit_dynamics(m, _excited(m), 0.4 + 0.1 * i, 0.05, observables={"exc": EXC})] = ("d", i)
+        for i, m in enumerate(std):
+            tags[srv.submit_steady(m, maxiter=3000)] = ("s", i)
+        done = srv.drain()
+    assert len(done) == len(tags)
+    for c in done:
+        kind, i = tags[c.tag]
+        assert c.ok, c.message
+        assert c.finish_time >= c.start_time >= c.submit_time
+        if kind == "d":
+            m = dyn[i]
+            ref = picuda.solve_dynamics(m, _excited(m), (0.0, 0.4 + 0.1 * i), saveat=0.05, save_states=False,
+                                        observables={"exc": EXC})
+            assert c.times == ref.t
+            assert np.abs(c.values["exc"] - ref.values["exc"]).max() <= 1e-10 * np.abs(ref.values["exc"]).max()
+        else:
+            ref = picuda.stationary_state(std[i], algorithm=picuda.GMRESAlgorithm(maxiter=3000))
+            assert np.abs(c.state - ref.data).max() <= 1e-7 * np.abs(ref.data).max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_server_result_same_alone_and_in_mix(torch_cuda, precision):
+    """A request served alone and the same request arriving into a busy server give the
+    same state and observables, bit for bit (tolerance 0)."""
+    target = M.scan_model(18, 0.7, 0.25, 0.1)
+    with picuda.Server(precision=precision) as srv:
+        srv.submit_dynamics(target, _excited(target), 1.0, 0.05, observables={"exc": EXC}, tag=1)
+        alone = srv.drain()[0]
+    others = [M.scan_model(int(n), om, gd, gp) for n, om, gd, gp in M.scan_draws(6, seed=5, nmin=10, nmax=40)]
+    with picuda.Server(precision=precision) as srv:
+        for k, m in enumerate(others[:3]):
+            srv.submit_dynamics(m, _excited(m), 0.5 + 0.25 * k, 0.05, tag=100 + k)
+        srv.submit_steady(M.driven_c1(8), maxiter=2000, tag=200)
+        time.sleep(0.05)  # the target arrives while the others are being served
+        srv.submit_dynamics(target, _excited(target), 1.0, 0.05, observables={"exc": EXC}, tag=1)
+        for k, m in enumerate(others[3:]):
+            srv.submit_dynamics(m, _excited(m), 0.3, 0.05, tag=300 + k)
+        done = {c.tag: c for c in srv.drain()}
+    mixed = done[1]
+    assert alone.ok and mixed.ok
+    assert np.array_equal(alone.state, mixed.state)
+    assert np.array_equal(alone.values["exc"], mixed.values["exc"])
+    assert all(c.ok for c in done.values())
+
+
+def test_server_memory_budget_serializes_admission(torch_cuda):
+    models = [M.scan_model(30, 1.0, 0.2, 0.1) for _ in range(3)]
+    dim = len(models[0].basis)
+    one = 16 * dim * (30 + 3) + 2 * 16 * dim  # fp64 footprint of one dynamics request
+    with picuda.Server(memory_budget=1.5 * one) as srv:
+        for i, m in enumerate(models):
+            srv.submit_dynamics(m, _excited(m), 0.2, 0.05, tag=i + 1)
+        done = sorted(srv.drain(fetch_state=False), key=lambda c: c.tag)
+        st = srv.stats()
+    assert all(c.ok for c in done)
+    for a, b in zip(done, done[1:]):
+        assert b.start_time >= a.finish_time - 1e-3  # one at a time
+    assert st["completed"] == 3 and st["active"] == 0 and st["bytes_in_use"] == 0
+
+
+def test_server_rejects_oversized_request(torch_cuda):
+    m = M.scan_model(20, 1.0, 0.2, 0.1)
+    with picuda.Server(memory_budget=1e5) as srv:
+        with pytest.raises(picuda.PiError):
+            srv.submit_dynamics(m, _excited(m), 0.2, 0.05)
+
+
+def test_server_mixed_close_to_fp64(torch_cuda):
+    models = [M.scan_model(int(n), om, gd, gp) for n, om, gd, gp in M.scan_draws(4, seed=9, nmin=10, nmax=30)]
+    res = {}
+    for prec in ("fp64", "mixed"):
+        with picuda.Server(precision=prec) as srv:
+            for i, m in enumerate(models):
+                srv.submit_dynamics(m, _excited(m), 1.0, 0.05, tag=i + 1)
+            res[prec] = {c.tag: c.state for c in srv.drain()}
+    for k in res["fp64"]:
+        ref = res["fp64"][k]
+        assert np.abs(res["mixed"][k] - ref).max() <= 2e-5 * np.abs(ref).max()
