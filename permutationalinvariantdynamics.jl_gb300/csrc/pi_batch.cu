@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kRT) k_s1_combine(const DevInst* __restrict__ 
   long long beg, end;
   chunk_range(S, blockIdx.x, beg, end);
   const T2* V = (const T2*)S.V;
-  const long long dim = S.dim;
+  const long long dim = S.ldv;
   const int acc = S.cacc;
   for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
     double yx = 0, yy = 0;
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(kApplyThreads)
     if (S.done) return;
     const DevTile tile = S.tiles[tile_local[blockIdx.x]];
     BorderArgs b{S.scale, nullptr, S.coords};
-    apply_tile<T>(S.sectors, S.terms, (const T2*)S.coefb, tile, (const T2*)S.V + (long long)S.j * S.dim, (T2*)S.w, b,
+    apply_tile<T>(S.sectors, S.terms, (const T2*)S.coefb, tile, (const T2*)S.V + (long long)S.j * S.ldv, (T2*)S.w, b,
                   S.border ? &S.alpha : nullptr, win, sterms, ge);
   }
 }
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(kRT) k_step_trace(DevInst* __restrict__ st) {
   __shared__ double smem[32 * 2];
   DevInst& S = st[blockIdx.x];
   if (S.done || !S.border) return;
-  const T2* x = (const T2*)S.V + (long long)S.j * S.dim;
+  const T2* x = (const T2*)S.V + (long long)S.j * S.ldv;
   double acc[2] = {0, 0};
   for (int i = threadIdx.x; i < S.ndiag; i += blockDim.x) {
     const double w = S.coords ? 1.0 : S.sectors[S.diag_sector[i]].sqrt_f;
@@ -406,7 +406,7 @@ __global__ void __launch_bounds__(kRT)
   const int cnt = min(8, nv - g0);
   long long beg, end;
   chunk_range(S, blockIdx.x, beg, end);
-  const long long dim = S.dim;
+  const long long dim = S.ldv;
   const T2* V = (const T2*)S.V + (long long)g0 * dim;
   const T2* w = (const T2*)S.w;
   double acc[16];
@@ -484,7 +484,7 @@ __global__ void __launch_bounds__(kRT)
   __syncthreads();
   long long beg, end;
   chunk_range(S, blockIdx.x, beg, end);
-  const long long dim = S.dim;
+  const long long dim = S.ldv;
   const T2* V = (const T2*)S.V;
   T2* w = (T2*)S.w;
   constexpr bool F32 = sizeof(T2) == sizeof(float2);
@@ -534,10 +534,280 @@ __global__ void __launch_bounds__(kRT) k_step_normalize(const DevInst* __restric
   long long beg, end;
   chunk_range(S, blockIdx.x, beg, end);
   const T2* w = (const T2*)S.w;
-  T2* out = (T2*)S.V + (long long)(S.j + 1) * S.dim;
+  T2* out = (T2*)S.V + (long long)(S.j + 1) * S.ldv;
   for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
     const double2 v = ld2(w + e);
     st2(out + e, f * v.x, f * v.y);
+  }
+}
+
+// ---- FP32-basis CGS2 kernels: pairs of complex elements per 16-byte load ---------------
+// Basis columns and the image vector have an even, zero-padded stride, so element pairs
+// never straddle a column; padding entries stay zero through every update.
+
+__device__ __forceinline__ void pair_range(const DevInst& S, int c, long long& beg, long long& end) {
+  beg = (long long)(c - S.chunk_begin) * (kBatchChunk / 2);
+  end = min(beg + (long long)(kBatchChunk / 2), (S.dim + 1) / 2);
+}
+
+// a += t, the rounding error of the addition carried in a.lo (TwoSum).
+__device__ __forceinline__ void df_add(DF& a, float t) {
+  const float s = a.hi + t;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (t - bb);
+  a.hi = s;
+  a.lo += err;
+}
+
+// a + b for double-float values (TwoSum of the leading parts).
+__device__ __forceinline__ DF df_sum(DF a, DF b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b.hi - bb);
+  return DF{s, (a.lo + b.lo) + err};
+}
+
+// Warp sum of double-float values in FP32 arithmetic (GB300's FP64 pipe is narrow: the
+// per-column reductions stay off it); the result is valid in lane 0.
+__device__ __forceinline__ DF warp_df_sum(DF v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const DF o{__shfl_down_sync(0xffffffffu, v.hi, off), __shfl_down_sync(0xffffffffu, v.lo, off)};
+    v = df_sum(v, o);
+  }
+  return v;
+}
+
+// Block sum of one double-float value; the FP64 result is valid in thread 0.
+__device__ __forceinline__ double block_df_sum(DF v, float2* smem) {
+  v = warp_df_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) smem[warp] = make_float2(v.hi, v.lo);
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+    DF t{0.f, 0.f};
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t = df_sum(t, DF{smem[i].x, smem[i].y});
+    r = (double)t.hi + (double)t.lo;
+  }
+  return r;
+}
+
+// CGS2 projections for an FP32 basis: partv[c][i] = conj(V_i) . w over chunk c for every
+// i <= j.  Each thread keeps its kPairs element pairs of w in registers and streams every
+// basis column once: per column it forms each pair term (two complex products) in FP32 and
+// accumulates the terms in double-float (no rounding error in the accumulation), then the
+// warp sums its lanes in FP64 into shared memory.
+constexpr int kPairs = kBatchChunk / 2 / kRT;  // element pairs per thread and chunk
+
+__device__ __forceinline__ void pair_terms(const float4 a, const float4 b, DF& re, DF& im) {
+  df_add(re, fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, a.w * b.w))));
+  df_add(im, fmaf(a.x, b.y, fmaf(-a.y, b.x, fmaf(a.z, b.w, -(a.w * b.z)))));
+}
+
+__global__ void __launch_bounds__(kRT, 3)
+    k_step_mdot_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv) {
+  __shared__ float4 wsm[kBatchChunk / 2];
+  __shared__ float4 red[kMaxDots][kRT / 32];  // per warp: (re.hi, re.lo, im.hi, im.lo)
+  const DevInst& S = st[chunk_inst[blockIdx.x]];
+  if (S.done) return;
+  const int nv = S.j + 1;
+  long long beg, end;
+  pair_range(S, blockIdx.x, beg, end);
+  const int npair = (int)(end - beg);
+  const float4* __restrict__ w4 = reinterpret_cast<const float4*>(S.w) + beg;
+  const float4* __restrict__ V4 = reinterpret_cast<const float4*>(S.V) + beg;
+  const long long ld4 = S.ldv / 2;
+#pragma unroll
+  for (int q = 0; q < kPairs; ++q) {
+    const int p = threadIdx.x + q * kRT;
+    wsm[p] = p < npair ? w4[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+  int k = 0;
+  // two columns per iteration: 2 * kPairs independent 16-byte loads in flight per thread
+  for (; k + 1 < nv; k += 2) {
+    const float4* __restrict__ c0 = V4 + (long long)k * ld4;
+    const float4* __restrict__ c1 = c0 + ld4;
+    float4 a[kPairs], b[kPairs];
+#pragma unroll
+    for (int q = 0; q < kPairs; ++q) {
+      const int p = threadIdx.x + q * kRT;
+      a[q] = p < npair ? c0[p] : zero;
+      b[q] = p < npair ? c1[p] : zero;
+    }
+    DF r0{0.f, 0.f}, i0{0.f, 0.f}, r1{0.f, 0.f}, i1{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < kPairs; ++q) {
+      const float4 wv = wsm[threadIdx.x + q * kRT];
+      pair_terms(a[q], wv, r0, i0);
+      pair_terms(b[q], wv, r1, i1);
+    }
+    r0 = warp_df_sum(r0);
+    i0 = warp_df_sum(i0);
+    r1 = warp_df_sum(r1);
+    i1 = warp_df_sum(i1);
+    if (lane == 0) {
+      red[k][warp] = make_float4(r0.hi, r0.lo, i0.hi, i0.lo);
+      red[k + 1][warp] = make_float4(r1.hi, r1.lo, i1.hi, i1.lo);
+    }
+  }
+  if (k < nv) {
+    const float4* __restrict__ c0 = V4 + (long long)k * ld4;
+    DF r0{0.f, 0.f}, i0{0.f, 0.f};
+#pragma unroll
+    for (int q = 0; q < kPairs; ++q) {
+      const int p = threadIdx.x + q * kRT;
+      pair_terms(p < npair ? c0[p] : zero, wsm[p], r0, i0);
+    }
+    r0 = warp_df_sum(r0);
+    i0 = warp_df_sum(i0);
+    if (lane == 0) red[k][warp] = make_float4(r0.hi, r0.lo, i0.hi, i0.lo);
+  }
+  __syncthreads();
+  for (int kk = threadIdx.x; kk < nv; kk += blockDim.x) {
+    DF sr{0.f, 0.f}, si{0.f, 0.f};
+#pragma unroll
+    for (int wdx = 0; wdx < kRT / 32; ++wdx) {
+      const float4 r = red[kk][wdx];
+      sr = df_sum(sr, DF{r.x, r.y});
+      si = df_sum(si, DF{r.z, r.w});
+    }
+    partv[(long long)blockIdx.x * kMaxDots + kk] =
+        make_double2((double)sr.hi + (double)sr.lo, (double)si.hi + (double)si.lo);
+  }
+}
+
+// cout (+)= sum_k ccoef[k] V_k for an FP32 basis in double-float arithmetic: each FP64
+// coefficient is split into hi + lo floats, hi * v is formed exactly (FMA residual), lo * v
+// in FP32, and the sum is carried as a double-float per component, so the FP64 output
+// matches an FP64 accumulation to ~1e-14 while the FP64 pipe stays idle.
+__device__ __forceinline__ void df_axpy(DF& acc, float ch, float cl, float v) {
+  const float p = ch * v;
+  const float e = fmaf(ch, v, -p);
+  const float s = acc.hi + p;
+  const float bb = s - acc.hi;
+  const float err = (acc.hi - (s - bb)) + (p - bb);
+  acc.hi = s;
+  acc.lo += err + fmaf(cl, v, e);
+}
+
+__global__ void __launch_bounds__(kRT)
+    k_s1_combine_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst) {
+  __shared__ float4 cs[kBatchMaxKrylov + 2];  // (re.hi, re.lo, im.hi, im.lo)
+  const DevInst& S = st[chunk_inst[blockIdx.x]];
+  double2* out = S.cout;
+  if (!out) return;
+  const int nc = S.ccount;
+  for (int i = threadIdx.x; i < nc; i += blockDim.x) {
+    const double2 c = S.ccoef[i];
+    const float rh = (float)c.x, ih = (float)c.y;
+    cs[i] = make_float4(rh, (float)(c.x - (double)rh), ih, (float)(c.y - (double)ih));
+  }
+  __syncthreads();
+  long long beg, end;
+  chunk_range(S, blockIdx.x, beg, end);
+  const float2* __restrict__ V = reinterpret_cast<const float2*>(S.V);
+  const long long ld = S.ldv;
+  const int acc = S.cacc;
+  for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+    DF yr{0.f, 0.f}, yi{0.f, 0.f};
+#pragma unroll 4
+    for (int k = 0; k < nc; ++k) {
+      const float2 v = V[(long long)k * ld + e];
+      const float4 c = cs[k];
+      df_axpy(yr, c.x, c.y, v.x);
+      df_axpy(yr, -c.z, -c.w, v.y);
+      df_axpy(yi, c.x, c.y, v.y);
+      df_axpy(yi, c.z, c.w, v.x);
+    }
+    double ox = (double)yr.hi + (double)yr.lo, oy = (double)yi.hi + (double)yi.lo;
+    if (acc) {
+      const double2 o = out[e];
+      ox += o.x;
+      oy += o.y;
+    }
+    out[e] = make_double2(ox, oy);
+  }
+}
+
+// w -= sum_i V_i h_i for an FP32 basis (which 0: hA, 1: hB), FP32 update; with part also
+// the double-float |w|^2 partial of the result.
+__global__ void __launch_bounds__(kRT)
+    k_step_maxpy_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, int which,
+                     double* __restrict__ part) {
+  __shared__ float2 hs[kMaxDots];
+  __shared__ float2 smem[32];
+  const DevInst& S = st[chunk_inst[blockIdx.x]];
+  if (S.done) return;
+  const int nv = S.j + 1;
+  const double2* h = which == 0 ? S.hA : S.hB;
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) hs[i] = make_float2((float)h[i].x, (float)h[i].y);
+  __syncthreads();
+  long long beg, end;
+  pair_range(S, blockIdx.x, beg, end);
+  float4* __restrict__ w4 = reinterpret_cast<float4*>(S.w);
+  const float4* __restrict__ V4 = reinterpret_cast<const float4*>(S.V);
+  const long long ld4 = S.ldv / 2;
+  DF nrm{0.f, 0.f};
+  for (long long p = beg + threadIdx.x; p < end; p += blockDim.x) {
+    float4 wv = w4[p];
+#pragma unroll 4
+    for (int i = 0; i < nv; ++i) {
+      const float4 v = V4[(long long)i * ld4 + p];
+      const float2 c = hs[i];
+      wv.x = fmaf(-v.x, c.x, wv.x);
+      wv.x = fmaf(v.y, c.y, wv.x);
+      wv.y = fmaf(-v.x, c.y, wv.y);
+      wv.y = fmaf(-v.y, c.x, wv.y);
+      wv.z = fmaf(-v.z, c.x, wv.z);
+      wv.z = fmaf(v.w, c.y, wv.z);
+      wv.w = fmaf(-v.z, c.y, wv.w);
+      wv.w = fmaf(-v.w, c.x, wv.w);
+    }
+    w4[p] = wv;
+    df_add(nrm, fmaf(wv.x, wv.x, fmaf(wv.y, wv.y, fmaf(wv.z, wv.z, wv.w * wv.w))));
+  }
+  if (part) {
+    const double r = block_df_sum(nrm, smem);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+  }
+}
+
+// |w|^2 partial of the image (expv cycles), FP32 basis.
+__global__ void __launch_bounds__(kRT)
+    k_step_image_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double* __restrict__ part) {
+  __shared__ float2 smem[32];
+  const DevInst& S = st[chunk_inst[blockIdx.x]];
+  if (S.done || S.givens) return;
+  long long beg, end;
+  pair_range(S, blockIdx.x, beg, end);
+  const float4* __restrict__ w4 = reinterpret_cast<const float4*>(S.w);
+  DF nrm{0.f, 0.f};
+  for (long long p = beg + threadIdx.x; p < end; p += blockDim.x) {
+    const float4 wv = w4[p];
+    df_add(nrm, fmaf(wv.x, wv.x, fmaf(wv.y, wv.y, fmaf(wv.z, wv.z, wv.w * wv.w))));
+  }
+  const double r = block_df_sum(nrm, smem);
+  if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+// V_{j+1} = w / |w| (zero on an exact breakdown), FP32 basis.
+__global__ void __launch_bounds__(kRT)
+    k_step_normalize_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst) {
+  const DevInst& S = st[chunk_inst[blockIdx.x]];
+  if (S.done) return;
+  const double r = sqrt(S.rem2);
+  const float f = r > 0 ? (float)(1.0 / r) : 0.f;
+  long long beg, end;
+  pair_range(S, blockIdx.x, beg, end);
+  const float4* __restrict__ w4 = reinterpret_cast<const float4*>(S.w);
+  float4* __restrict__ out = reinterpret_cast<float4*>(S.V) + (long long)(S.j + 1) * (S.ldv / 2);
+  for (long long p = beg + threadIdx.x; p < end; p += blockDim.x) {
+    const float4 v = w4[p];
+    out[p] = make_float4(f * v.x, f * v.y, f * v.z, f * v.w);
   }
 }
 
@@ -669,8 +939,11 @@ bool DynamicsJob::setup(cudaStream_t s, int m, bool f32) {
   mixed_ = f32;
   cudaError_t e = cudaSuccess;
   const size_t es = f32 ? sizeof(float2) : sizeof(double2);
-  V = alloc(es * (size_t)dim * (m + 2), &e);
-  w = alloc(es * (size_t)dim, &e);
+  ldv = basis_stride(dim);
+  V = alloc(es * (size_t)ldv * (m + 2), &e);
+  w = alloc(es * (size_t)ldv, &e);
+  if (e == cudaSuccess) e = cudaMemsetAsync(V, 0, es * (size_t)ldv * (m + 2), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w, 0, es * (size_t)ldv, s);
   cur_ = (double2*)alloc(sizeof(double2) * dim, &e);
   trial_ = (double2*)alloc(sizeof(double2) * dim, &e);
   if (nobs_ > 0 && mixed_) obsz_ = (double2*)alloc(sizeof(double2) * dim * nobs_, &e);
@@ -1000,8 +1273,11 @@ bool SteadyJob::setup(cudaStream_t s, int m, bool f32) {
   m_ = (int)std::min<long long>(std::min(o_.krylovdim, m), dim);
   cudaError_t e = cudaSuccess;
   const size_t es = f32 ? sizeof(float2) : sizeof(double2);
-  V = alloc(es * (size_t)dim * (m + 2), &e);
-  w = alloc(es * (size_t)dim, &e);
+  ldv = basis_stride(dim);
+  V = alloc(es * (size_t)ldv * (m + 2), &e);
+  w = alloc(es * (size_t)ldv, &e);
+  if (e == cudaSuccess) e = cudaMemsetAsync(V, 0, es * (size_t)ldv * (m + 2), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(w, 0, es * (size_t)ldv, s);
   b_ = (double2*)alloc(sizeof(double2) * dim, &e);
   r_ = (double2*)alloc(sizeof(double2) * dim, &e);
   ay_ = (double2*)alloc(sizeof(double2) * dim, &e);
@@ -1277,6 +1553,7 @@ void Engine::rebuild() {
     d.diag_sector = dp.diag_sector;
     d.diag_index = dp.diag_index;
     d.dim = J->dim;
+    d.ldv = J->ldv;
     d.ndiag = dp.ndiag;
     d.chunk_begin = (int)ci.size();
     for (int c = 0; c < nc[i]; ++c) ci.push_back(i);
@@ -1361,16 +1638,16 @@ void Engine::arnoldi_step() {
   if (f32_) {
     launch(k_step_trace<float2>, n, kRT, 0, st);
     launch(k_bapply<float, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(float2), (const DevInst*)st, ti, tl);
-    launch(k_step_image_partial<float2>, C, kRT, 0, (const DevInst*)st, ci, part);
+    launch(k_step_image_f32, C, kRT, 0, (const DevInst*)st, ci, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);
-    launch(k_step_mdot_partial<float2, true>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
+    launch(k_step_mdot_f32, C, kRT, 0, (const DevInst*)st, ci, partv);
     launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
-    launch(k_step_maxpy<float2>, C, kRT, 0, (const DevInst*)st, ci, 0, none);
-    launch(k_step_mdot_partial<float2, true>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
+    launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 0, none);
+    launch(k_step_mdot_f32, C, kRT, 0, (const DevInst*)st, ci, partv);
     launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
-    launch(k_step_maxpy<float2>, C, kRT, 0, (const DevInst*)st, ci, 1, part);
+    launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 1, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
-    launch(k_step_normalize<float2>, C, kRT, 0, (const DevInst*)st, ci);
+    launch(k_step_normalize_f32, C, kRT, 0, (const DevInst*)st, ci);
   } else {
     launch(k_step_trace<double2>, n, kRT, 0, st);
     launch(k_bapply<double, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(double2), (const DevInst*)st, ti, tl);
@@ -1435,7 +1712,7 @@ bool Engine::tick() {
     if (flags & S1_COMBINE) {
       chk(cudaMemcpyAsync(coefs_, coefs_h_, sizeof(double2) * (m_ + 2) * n, cudaMemcpyHostToDevice, s_));
       if (f32_)
-        k_s1_combine<float2><<<C, kRT, 0, s_>>>(st, ci);
+        k_s1_combine_f32<<<C, kRT, 0, s_>>>(st, ci);
       else
         k_s1_combine<double2><<<C, kRT, 0, s_>>>(st, ci);
     }

@@ -34,6 +34,10 @@ constexpr int kBatchMaxObs = 16;   // observables per dynamics job
 constexpr int kOutSlots = 4 + 2 * kBatchMaxObs;  // per-job stage-1 outputs (doubles)
 constexpr int kBatchMaxKrylov = 120;
 
+// Column stride of a Krylov basis: dim rounded up to 64 elements (aligned 16-byte loads of
+// element pairs; the padding is zero).
+inline long long basis_stride(long long dim) { return (dim + 63) / 64 * 64; }
+
 // Stage-1 operation flags.
 enum : unsigned {
   S1_COMBINE = 1u,
@@ -56,6 +60,7 @@ struct DevInst {
   const int* diag_sector;
   const long long* diag_index;
   long long dim;
+  long long ldv;    // basis column stride: dim rounded up to a multiple of 64, zero padded
   int ndiag;
   int chunk_begin;  // first chunk of this job in the engine's chunk list
   // Krylov cycle
@@ -117,6 +122,7 @@ class Job {
   size_t bytes = 0;  // device bytes held by the job
   void* V = nullptr;
   void* w = nullptr;
+  long long ldv = 0;
   // Allocates the basis and the job's vectors; false on allocation failure.
   virtual bool setup(cudaStream_t s, int m, bool f32) = 0;
   // Stage 1: sets operands in d and coefficients in coef (when combining); returns flags.
