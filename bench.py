@@ -94,6 +94,229 @@ def solve_rates(picuda, torch):
     return out
 
 
+def scan_model(picuda, N, omega, gdown, gphi):
+    """Parameter-scan family: H = Omega Jx, local decay gdown, local dephasing gphi,
+    collective decay 1/N on J-."""
+    s = picuda.spin_matrices(2)
+    return picuda.qubit_ensemble_model(N, hamiltonian=omega * s["jx"], emission=gdown, dephasing=gphi,
+                                       collective_emission=1.0 / N)
+
+
+def scan_draws(count, seed=0, nmin=20, nmax=160):
+    """Seeded scan points: N ~ U{nmin..nmax}, Omega ~ U[0.2, 2], gdown ~ U[0.05, 0.5],
+    gphi ~ U[0, 0.2]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        N = int(rng.integers(nmin, nmax + 1))
+        out.append((N, float(rng.uniform(0.2, 2.0)), float(rng.uniform(0.05, 0.5)), float(rng.uniform(0.0, 0.2))))
+    return out
+
+
+def compile_all(picuda, models, threads=16):
+    """Plans built in parallel host threads (the C call releases the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(picuda.compile, models))
+
+
+def scan_rates(picuda, torch, count=256, intervals=2, seed=0):
+    """Batched parameter scan: `count` instances (N ~ U{20..160}, uneven PI dimensions) each
+    advance `intervals` saved intervals of dt = 0.05 from the all-excited state (expv m = 30,
+    tol 1e-10/1e-8) in one batched engine run, observables Jz and J+J- at every saved time.
+    Timed end to end: initial states uploaded from host, final states and observables read
+    back.  Reported per precision, with the mixed run's deviation from the FP64 run."""
+    sm = picuda.spin_matrices(2)
+    draws = scan_draws(count, seed)
+    models = [scan_model(picuda, *d) for d in draws]
+    t0 = time.perf_counter()
+    comp = compile_all(picuda, models)
+    compile_s = time.perf_counter() - t0
+    rho0 = [picuda.computational_product_state(m.basis, 2) for m in models]
+    obs = {"Jz": sm["jz"], "JpJm": sm["jp"] @ sm["jm"]}
+    dims = [len(m.basis) for m in models]
+    out = {"instances": count, "intervals": intervals, "dt": 0.05, "sum_dim": int(sum(dims)),
+           "min_dim": int(min(dims)), "max_dim": int(max(dims)), "plan_build_s": compile_s}
+    vals = {}
+    for prec in ("fp64", "mixed"):
+        alg = picuda.ExpvAlgorithm(krylovdim=30, precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res, fin, infos = picuda.solve_dynamics_batch(comp, rho0, (0.0, 0.05 * intervals), algorithm=alg, saveat=0.05,
+                                                      observables=obs, return_info=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        vals[prec] = res
+        out[prec] = {"seconds": dt, "instance_intervals_per_s": count * intervals / dt,
+                     "converged": int(sum(1 for i in infos if i["converged"])),
+                     "accepted_steps": int(sum(i["accepted_steps"] for i in infos)),
+                     "operator_applications": int(sum(i["operator_applications"] for i in infos))}
+        out[prec]["applies_per_s"] = out[prec]["operator_applications"] / dt
+    dev = 0.0
+    for a, b in zip(vals["mixed"], vals["fp64"]):
+        for k in obs:
+            ref = np.abs(b.values[k]).max()
+            dev = max(dev, float(np.abs(a.values[k] - b.values[k]).max() / max(ref, 1e-300)))
+    out["mixed_max_observable_rel_dev_vs_fp64"] = dev
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds"] / out["mixed"]["seconds"]
+    return out
+
+
+def request_stream(count, seed=0, nmin=10, nmax=300, steady_fraction=0.3):
+    """Served request mix: N = floor(exp(U[ln nmin, ln nmax])); 70% time evolution with
+    t_final ~ U[1, 10], dt = 0.05; 30% steady state; parameters drawn as in the scan."""
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        N = int(np.floor(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+        p = (N, float(rng.uniform(0.2, 2.0)), float(rng.uniform(0.05, 0.5)), float(rng.uniform(0.0, 0.2)))
+        kind = "steady" if rng.uniform() < steady_fraction else "dynamics"
+        reqs.append({"params": p, "kind": kind, "t_final": float(rng.uniform(1.0, 10.0)), "dt": 0.05})
+    return reqs
+
+
+def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9):
+    """Continuous-batching server on a Poisson request stream at `rate` req/s (the lowest
+    rate of the served configuration; the stream saturates the GPU): p50/p99 latency
+    (finish - submit) and completed solves/s, FP64 vs mixed, same requests and arrival
+    times.  Plans are built before the clock starts."""
+    reqs = request_stream(count, seed)
+    sm = picuda.spin_matrices(2)
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=count))
+    models = [scan_model(picuda, *r["params"]) for r in reqs]
+    comp = compile_all(picuda, models)
+    rho0 = [picuda.computational_product_state(m.basis, 2) for m in models]
+    out = {"requests": count, "rate_per_s": rate, "memory_budget_bytes": budget,
+           "dynamics": sum(1 for r in reqs if r["kind"] == "dynamics"),
+           "steady": sum(1 for r in reqs if r["kind"] == "steady"),
+           "max_dim": int(max(len(m.basis) for m in models))}
+    states, finals = {}, {}
+    for prec in ("fp64", "mixed"):
+        with picuda.Server(precision=prec, memory_budget=budget) as srv:
+            t0 = time.perf_counter()
+            done = []
+            for i, r in enumerate(reqs):
+                while time.perf_counter() - t0 < arrivals[i]:
+                    done.extend(srv.poll(timeout_ms=1))
+                if r["kind"] == "dynamics":
+                    srv.submit_dynamics(comp[i], rho0[i], r["t_final"], r["dt"], tag=i + 1,
+                                        observables={"tr": np.eye(2) / models[i].basis.N, "Jz": sm["jz"]})
+                else:
+                    srv.submit_steady(comp[i], tag=i + 1)
+            done.extend(srv.drain())
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        lat = np.array([c.latency for c in done])
+        ok = [c for c in done if c.ok]
+        span = max(c.finish_time for c in done) - min(c.submit_time for c in done)
+        res = {"wall_s": wall, "completed": len(done), "ok": len(ok), "solves_per_s": len(ok) / span,
+               "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+               "ticks": st["ticks"], "cycles": st["cycles"]}
+        for kind in ("dynamics", "steady"):
+            kl = np.array([c.latency for c in done if c.kind == kind])
+            if len(kl):
+                res[f"{kind}_p50_ms"] = float(np.percentile(kl, 50) * 1e3)
+                res[f"{kind}_p99_ms"] = float(np.percentile(kl, 99) * 1e3)
+        res["failed"] = [f"{c.tag}:{c.message[:80]}" for c in done if not c.ok][:5]
+        dyn = [c for c in done if c.ok and c.kind == "dynamics"]
+        res["max_final_trace_error_dynamics"] = max((abs(c.values["tr"][-1] - 1) for c in dyn), default=None)
+        out[prec] = res
+        states[prec] = {c.tag: c.state for c in done if c.ok}
+        finals[prec] = {c.tag: (c.values["tr"][-1], c.values["Jz"][-1]) for c in dyn}
+    # observable deviation on requests whose FP64 trace stayed within 1e-6 (the reference's
+    # reference-coordinate error control loses trace at large N; see the FP64 trace errors)
+    jdev, kept = 0.0, 0
+    for tag, (tr64, jz64) in finals["fp64"].items():
+        if tag in finals["mixed"] and abs(tr64 - 1) < 1e-6:
+            kept += 1
+            jdev = max(jdev, abs(finals["mixed"][tag][1] - jz64) / reqs[tag - 1]["params"][0])
+    out["mixed_max_Jz_per_N_dev_vs_fp64"] = jdev
+    out["requests_compared"] = kept
+    for kind in ("steady",):
+        dev, worst = 0.0, None
+        for tag, ref in states["fp64"].items():
+            got = states["mixed"].get(tag)
+            if got is None or reqs[tag - 1]["kind"] != kind:
+                continue
+            d = float(np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300))
+            if d >= dev:
+                dev, worst = d, tag
+        out[f"mixed_max_state_rel_dev_vs_fp64_{kind}"] = dev
+        if worst is not None:
+            out[f"worst_{kind}_request"] = {"N": reqs[worst - 1]["params"][0], "params": reqs[worst - 1]["params"],
+                                            "t_final": reqs[worst - 1]["t_final"]}
+    out["solves_per_s_ratio_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    return out
+
+
+def steady_family(picuda, family, count, seed):
+    """Steady-state request sets.  'driven': driven qubits (H = Omega Jx, local decay gamma),
+    N ~ U{8..20}, Omega ~ U[0.5, 1.5], gamma ~ U[0.3, 0.7] -- a family the reference's
+    unpreconditioned restarted GMRES brings to tolerance (GMRES(50), maxiter 5000).
+    'served': the served configuration's steady requests (N log-uniform in 10..300,
+    parameters as in the scan; GMRES(30), maxiter 500)."""
+    rng = np.random.default_rng(seed)
+    if family == "driven":
+        models = []
+        for _ in range(count):
+            N = int(rng.integers(8, 21))
+            models.append(picuda.Models.driven_qubits(N, drive=float(rng.uniform(0.5, 1.5)),
+                                                      emission=float(rng.uniform(0.3, 0.7)), pumping=0.0))
+        return models, 50, 5000
+    reqs = request_stream(count, seed, steady_fraction=1.0)
+    return [scan_model(picuda, *r["params"]) for r in reqs], 30, 500
+
+
+def steady_rates(picuda, torch, count=16, seed=7, family="driven"):
+    """Steady-state solves/s at the reference's tolerance (atol 1e-10, rtol 1e-8 on the
+    trace-bordered system): the plain FP64 GPU path (one pi_steady_state call per request,
+    in turn) against the served engine in FP64 and in mixed precision (all requests
+    submitted at once).  Solves/s counts converged solves only."""
+    models, m, maxiter = steady_family(picuda, family, count, seed)
+    comp = compile_all(picuda, models)
+    out = {"family": family, "requests": count, "krylovdim": m, "maxiter": maxiter,
+           "max_dim": int(max(len(x.basis) for x in models)), "n_values": [x.basis.N for x in models]}
+    t0 = time.perf_counter()
+    plain, its = {}, []
+    for i, c in enumerate(comp):
+        try:
+            r = picuda.stationary_state(c, algorithm=picuda.GMRESAlgorithm(krylovdim=m, maxiter=maxiter),
+                                        return_info=True)
+            plain[i] = r.state.data
+            its.append(r.info["iterations"])
+        except picuda.PiNotConverged:
+            plain[i] = None
+            its.append(-1)
+    dt = time.perf_counter() - t0
+    okc = sum(1 for v in its if v >= 0)
+    out["plain_fp64"] = {"seconds": dt, "converged": okc, "solves_per_s": okc / dt, "iterations": its,
+                         "converged_without_iterations": sum(1 for v in its if v == 0)}
+    for prec in ("fp64", "mixed"):
+        with picuda.Server(krylovdim=m, precision=prec) as srv:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for i, c in enumerate(comp):
+                srv.submit_steady(c, maxiter=maxiter, tag=i + 1)
+            done = srv.drain()
+            dt = time.perf_counter() - t0
+        ok = [c for c in done if c.ok]
+        lat = np.array([c.latency for c in done])
+        dev = 0.0
+        for c in ok:
+            ref = plain.get(c.tag - 1)
+            if ref is not None:
+                dev = max(dev, float(np.abs(c.state - ref).max() / max(np.abs(ref).max(), 1e-300)))
+        out[f"served_{prec}"] = {"seconds": dt, "converged": len(ok), "solves_per_s": len(ok) / dt,
+                                 "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                                 "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                                 "max_normalized_residual": max((c.residual for c in ok), default=None),
+                                 "max_state_rel_dev_vs_plain_fp64": dev}
+    out["ratio_served_mixed_vs_plain_fp64"] = (out["served_mixed"]["solves_per_s"] /
+                                               max(out["plain_fp64"]["solves_per_s"], 1e-300))
+    return out
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -287,6 +510,13 @@ def main():
                     help="time only the device applies (used for ncu captures)")
     ap.add_argument("--only-solves", action="store_true",
                     help="run only the solve-rate section (used for ncu launch lists)")
+    ap.add_argument("--only-scan", action="store_true", help="run only the batched-scan section")
+    ap.add_argument("--only-serve", action="store_true", help="run only the serving section")
+    ap.add_argument("--scan-instances", type=int, default=256)
+    ap.add_argument("--scan-intervals", type=int, default=2)
+    ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--only-steady", action="store_true", help="run only the steady-state rate section")
+    ap.add_argument("--steady-requests", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -302,6 +532,18 @@ def main():
     torch.cuda.set_device(local)
     if args.only_solves:
         print(json.dumps({"only_solves": True, "solves": solve_rates(picuda, torch)}))
+        return 0
+    if args.only_scan:
+        print(json.dumps({"only_scan": True, "scan": scan_rates(picuda, torch, args.scan_instances,
+                                                                  args.scan_intervals)}))
+        return 0
+    if args.only_steady:
+        print(json.dumps({"only_steady": True, "steady": steady_rates(picuda, torch, args.steady_requests),
+                          "steady_served_family": steady_rates(picuda, torch, args.steady_requests,
+                                                               family="served")}))
+        return 0
+    if args.only_serve:
+        print(json.dumps({"only_serve": True, "serve": serve_rates(picuda, torch, args.serve_requests)}))
         return 0
     model = model_c2(picuda)
     compiled = picuda.compile(model)
@@ -374,6 +616,11 @@ def main():
     e2e_value = world * bytes32 / e2e_s / 1e9
 
     solves = solve_rates(picuda, torch) if rank == 0 else None
+    scan = scan_rates(picuda, torch, args.scan_instances, args.scan_intervals) if rank == 0 else None
+    serve = serve_rates(picuda, torch, args.serve_requests) if rank == 0 else None
+    steady = steady_rates(picuda, torch, args.steady_requests) if rank == 0 else None
+    steady_served = (steady_rates(picuda, torch, args.steady_requests, family="served")
+                     if rank == 0 else None)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -406,6 +653,10 @@ def main():
                     "d2h_bytes_per_step": 8 * n * BATCH, "ms_per_step": e2e_s * 1e3,
                     "call": "pi_apply_host_f32 (pinned host buffers)"},
             "solves": solves,
+            "scan": scan,
+            "serve": serve,
+            "steady": steady,
+            "steady_served_family": steady_served,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": cl,
