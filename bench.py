@@ -120,7 +120,7 @@ def compile_all(picuda, models, threads=16):
         return list(ex.map(picuda.compile, models))
 
 
-def scan_rates(picuda, torch, count=256, intervals=2, seed=0):
+def scan_rates(picuda, torch, count=256, intervals=2, seed=0, precisions=("fp64", "mixed")):
     """Batched parameter scan: `count` instances (N ~ U{20..160}, uneven PI dimensions) each
     advance `intervals` saved intervals of dt = 0.05 from the all-excited state (expv m = 30,
     tol 1e-10/1e-8) in one batched engine run, observables Jz and J+J- at every saved time.
@@ -133,14 +133,21 @@ def scan_rates(picuda, torch, count=256, intervals=2, seed=0):
     comp = compile_all(picuda, models)
     compile_s = time.perf_counter() - t0
     rho0 = [picuda.computational_product_state(m.basis, 2) for m in models]
-    obs = {"Jz": sm["jz"], "JpJm": sm["jp"] @ sm["jm"]}
+    obs_ops = {"Jz": sm["jz"], "JpJm": sm["jp"] @ sm["jm"]}
+    # per-instance PI vectors of the observables, built before the clock starts
+    obs = [{k: picuda.collective_operator(m.basis, v) for k, v in obs_ops.items()} for m in models]
     dims = [len(m.basis) for m in models]
     out = {"instances": count, "intervals": intervals, "dt": 0.05, "sum_dim": int(sum(dims)),
            "min_dim": int(min(dims)), "max_dim": int(max(dims)), "plan_build_s": compile_s}
     vals = {}
-    for prec in ("fp64", "mixed"):
+    for prec in precisions:
         alg = picuda.ExpvAlgorithm(krylovdim=30, precision=prec)
+        # untimed first call: memory-pool growth, graph instantiation
         torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        picuda.solve_dynamics_batch(comp, rho0, (0.0, 0.05), algorithm=alg, saveat=0.05)
+        torch.cuda.synchronize()
+        first_s = time.perf_counter() - t0
         t0 = time.perf_counter()
         res, fin, infos = picuda.solve_dynamics_batch(comp, rho0, (0.0, 0.05 * intervals), algorithm=alg, saveat=0.05,
                                                       observables=obs, return_info=True)
@@ -148,13 +155,16 @@ def scan_rates(picuda, torch, count=256, intervals=2, seed=0):
         dt = time.perf_counter() - t0
         vals[prec] = res
         out[prec] = {"seconds": dt, "instance_intervals_per_s": count * intervals / dt,
+                     "first_call_1_interval_s": first_s,
                      "converged": int(sum(1 for i in infos if i["converged"])),
                      "accepted_steps": int(sum(i["accepted_steps"] for i in infos)),
                      "operator_applications": int(sum(i["operator_applications"] for i in infos))}
         out[prec]["applies_per_s"] = out[prec]["operator_applications"] / dt
+    if len(vals) < 2:
+        return out
     dev = 0.0
     for a, b in zip(vals["mixed"], vals["fp64"]):
-        for k in obs:
+        for k in obs_ops:
             ref = np.abs(b.values[k]).max()
             dev = max(dev, float(np.abs(a.values[k] - b.values[k]).max() / max(ref, 1e-300)))
     out["mixed_max_observable_rel_dev_vs_fp64"] = dev
@@ -514,6 +524,7 @@ def main():
     ap.add_argument("--only-serve", action="store_true", help="run only the serving section")
     ap.add_argument("--scan-instances", type=int, default=256)
     ap.add_argument("--scan-intervals", type=int, default=2)
+    ap.add_argument("--scan-precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--only-steady", action="store_true", help="run only the steady-state rate section")
     ap.add_argument("--steady-requests", type=int, default=16)
@@ -534,8 +545,9 @@ def main():
         print(json.dumps({"only_solves": True, "solves": solve_rates(picuda, torch)}))
         return 0
     if args.only_scan:
+        precs = ("fp64", "mixed") if args.scan_precision == "both" else (args.scan_precision,)
         print(json.dumps({"only_scan": True, "scan": scan_rates(picuda, torch, args.scan_instances,
-                                                                  args.scan_intervals)}))
+                                                                  args.scan_intervals, precisions=precs)}))
         return 0
     if args.only_steady:
         print(json.dumps({"only_steady": True, "steady": steady_rates(picuda, torch, args.steady_requests),

@@ -253,34 +253,56 @@ __global__ void __launch_bounds__(kRT)
   }
 }
 
-// Observable dots conj(ob_o) . obx over one chunk.
+// Observable dots conj(ob_o) . obx over one chunk (FP64 data).  Only the live observables
+// are reduced: warp shuffles per observable, then one shared-memory pass.
 __global__ void __launch_bounds__(kRT)
     k_s1_obs_partial(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv) {
-  __shared__ double smem[32 * 2 * kBatchMaxObs];
+  __shared__ double2 red[kBatchMaxObs][kRT / 32];
   const DevInst& S = st[chunk_inst[blockIdx.x]];
   const int nob = S.nob;
   if (nob == 0) return;
   long long beg, end;
   chunk_range(S, blockIdx.x, beg, end);
-  double acc[2 * kBatchMaxObs];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o0 = 0; o0 < nob; o0 += 4) {
+    double acc[8];
 #pragma unroll
-  for (int k = 0; k < 2 * kBatchMaxObs; ++k) acc[k] = 0;
-  for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
-    const double2 x = S.obx[e];
+    for (int k = 0; k < 8; ++k) acc[k] = 0;
+    for (long long e = beg + threadIdx.x; e < end; e += blockDim.x) {
+      const double2 x = S.obx[e];
 #pragma unroll
-    for (int o = 0; o < kBatchMaxObs; ++o) {
-      if (o < nob) {
-        const double2 v = S.ob[(long long)o * S.dim + e];
-        acc[2 * o] = fma(v.x, x.x, acc[2 * o]);
-        acc[2 * o] = fma(v.y, x.y, acc[2 * o]);
-        acc[2 * o + 1] = fma(v.x, x.y, acc[2 * o + 1]);
-        acc[2 * o + 1] = fma(-v.y, x.x, acc[2 * o + 1]);
+      for (int k = 0; k < 4; ++k) {
+        if (o0 + k < nob) {
+          const double2 v = S.ob[(long long)(o0 + k) * S.dim + e];
+          acc[2 * k] = fma(v.x, x.x, acc[2 * k]);
+          acc[2 * k] = fma(v.y, x.y, acc[2 * k]);
+          acc[2 * k + 1] = fma(v.x, x.y, acc[2 * k + 1]);
+          acc[2 * k + 1] = fma(-v.y, x.x, acc[2 * k + 1]);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (o0 + k < nob) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          acc[2 * k] += __shfl_down_sync(0xffffffffu, acc[2 * k], off);
+          acc[2 * k + 1] += __shfl_down_sync(0xffffffffu, acc[2 * k + 1], off);
+        }
+        if (lane == 0) red[o0 + k][warp] = make_double2(acc[2 * k], acc[2 * k + 1]);
       }
     }
   }
-  block_sum<2 * kBatchMaxObs>(acc, smem);
-  if (threadIdx.x == 0)
-    for (int o = 0; o < nob; ++o) partv[(long long)blockIdx.x * kMaxDots + o] = make_double2(acc[2 * o], acc[2 * o + 1]);
+  __syncthreads();
+  for (int o = threadIdx.x; o < nob; o += blockDim.x) {
+    double sx = 0, sy = 0;
+#pragma unroll
+    for (int wdx = 0; wdx < kRT / 32; ++wdx) {
+      sx += red[o][wdx].x;
+      sy += red[o][wdx].y;
+    }
+    partv[(long long)blockIdx.x * kMaxDots + o] = make_double2(sx, sy);
+  }
 }
 
 // Per-instance sums of chunk partials: one warp per value, fixed order.
@@ -1475,6 +1497,13 @@ Engine::Engine(int device, int krylovdim, bool f32, bool use_graphs)
     : device_(device), m_(krylovdim), f32_(f32), graphs_(use_graphs) {
   chk(cudaSetDevice(device));
   chk(cudaStreamCreateWithFlags(&s_, cudaStreamNonBlocking));
+  // Job workspaces come from the device's default memory pool; keep freed memory in the
+  // pool so that admitting the next requests does not go back to the driver.
+  cudaMemPool_t pool = nullptr;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess && pool) {
+    unsigned long long keep = ~0ULL;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
   const size_t smem64 = 3 * kWinElems * sizeof(double2);
   const size_t smem32 = 3 * kWinElems * sizeof(float2);
   set_smem(k_bapply<double, true>, smem64, err);

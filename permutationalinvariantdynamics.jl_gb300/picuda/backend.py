@@ -575,7 +575,9 @@ def solve_dynamics_batch(models, rho0s, tspans, algorithm: ExpvAlgorithm | None 
     """solve_dynamics(...; save_states=false) for many models in one batched engine run.
 
     tspans and saveat may be one value for all instances or one per instance (a list of n
-    tspans; a list of n saveat grids, each None or a sequence).  Returns one
+    tspans; a list of n saveat grids, each None or a sequence).  observables is one dict
+    name -> operator for all instances, or a list of n such dicts (e.g. prebuilt PI
+    vectors per instance).  Returns one
     DynamicsStreamResult per instance (values per observable name) plus the final states.
     """
     torch = _torch()
@@ -593,10 +595,13 @@ def solve_dynamics_batch(models, rho0s, tspans, algorithm: ExpvAlgorithm | None 
     xs = _device_states(compiled, rho0s)
     names, obs_dev = [], []
     if observables:
-        items = list(observables.items()) if isinstance(observables, dict) else list(observables)
-        names = [k for k, _ in items]
-        for c in compiled:
-            datas = [_observable_data(c.basis, v) for _, v in items]
+        per_instance = isinstance(observables, (list, tuple)) and len(observables) == n and all(
+            isinstance(o, dict) for o in observables)
+        first = observables[0] if per_instance else observables
+        names = list(first.keys()) if isinstance(first, dict) else [k for k, _ in first]
+        for i, c in enumerate(compiled):
+            src = observables[i] if per_instance else dict(first) if not isinstance(first, dict) else first
+            datas = [_observable_data(c.basis, src[k]) for k in names]
             obs_dev.append(torch.from_numpy(np.ascontiguousarray(np.stack(datas))).cuda())
     nobs = len(names)
     vals = [np.zeros((len(g), max(nobs, 1), 2), dtype=np.float64) for g in grids]
