@@ -2,7 +2,8 @@
 
 Workload (one step): the fused L x of the N=120 qubit-ensemble model (H = 0.3 Jz + 1.2 Jx,
 local decay 0.2, local dephasing 0.1, collective decay 0.05/N; PI dimension 302,621) applied
-to a batch of 128 resident state vectors (inputs larger than L2, no flush needed).  The
+to a batch of 128 resident state vectors (inputs larger than L2, no flush needed), stored
+element-major by default (a (dim, 128) array; --layout columns for (128, dim)).  The
 headline is the FP32 apply (the mixed-precision path's inner operator) in population
 coordinates: value = algorithmic bytes (read x once, write y once) / device time.
 The FP64 apply, the end-to-end host-buffer call, the steady-state solve rate and the CPU
@@ -518,6 +519,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-apply", action="store_true",
                     help="time only the device applies (used for ncu captures)")
+    ap.add_argument("--layout", default="element-major", choices=["columns", "element-major"],
+                    help="batch layout of the headline apply: (batch, dim) columns or (dim, batch)")
     ap.add_argument("--only-solves", action="store_true",
                     help="run only the solve-rate section (used for ncu launch lists)")
     ap.add_argument("--only-scan", action="store_true", help="run only the batched-scan section")
@@ -561,12 +564,17 @@ def main():
     compiled = picuda.compile(model)
     n = len(model.basis)
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
-    X32 = torch.randn((BATCH, n), dtype=torch.complex64, device="cuda", generator=g)
+    em = args.layout == "element-major"
+    shape = (n, BATCH) if em else (BATCH, n)
+    X32 = torch.randn(shape, dtype=torch.complex64, device="cuda", generator=g)
     Y32 = torch.empty_like(X32)
     stream = torch.cuda.current_stream()
 
     def step32():
-        picuda.apply_(Y32, compiled, X32, precision="fp32", coords="population")
+        if em:
+            picuda.apply_element_major_(Y32, compiled, X32, coords="population")
+        else:
+            picuda.apply_(Y32, compiled, X32, precision="fp32", coords="population")
 
     for _ in range(args.warmup):
         step32()
@@ -589,7 +597,7 @@ def main():
     achieved = bytes32 / (ms * 1e-3) / 1e9
 
     # FP64 apply on the same batch (plain path), timed the same way
-    X64 = X32.to(torch.complex128)
+    X64 = (X32.t().contiguous() if em else X32).to(torch.complex128)
     Y64 = torch.empty_like(X64)
     for _ in range(3):
         picuda.apply_(Y64, compiled, X64)
@@ -611,7 +619,7 @@ def main():
         return 0
 
     # End to end through the host-buffer C-ABI call (pinned host memory, H2D + apply + D2H)
-    xh = X32.cpu().pin_memory()
+    xh = (X32.t().contiguous() if em else X32).cpu().pin_memory()
     yh = torch.empty_like(xh).pin_memory()
     lib = picuda.load_library()
     import ctypes as C
@@ -650,12 +658,15 @@ def main():
             "vs_baseline": None, "dtype": "c64", "data": "synthetic",
             "config": {"workload": "fused L x, N=120 qubit ensemble (dim 302,621), batch of 128 resident "
                                    "state vectors, FP32 population coordinates",
+                       "layout": ("element-major (dim, 128): pi_apply_f32_em" if em else
+                                  "columns (128, dim): pi_apply_f32"),
                        "model": "H=0.3Jz+1.2Jx, local decay 0.2, local dephasing 0.1, collective decay 0.05/N",
                        "batch": BATCH, "pi_dim": n, "l2": "inputs larger than L2 (310 MB per step read)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": profile_traffic("apply_f32_batch128_N120"),
+                         "traffic": profile_traffic("apply_em_f32_batch128_N120" if em else
+                                                    "apply_f32_batch128_N120"),
                          "algorithmic_bytes_per_launch": bytes32},
             "fp64": {"value": bytes64 / (ms64 * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": ms64,
                      "frac_hbm": bytes64 / (ms64 * 1e-3) / 1e9 / peak,

@@ -91,6 +91,8 @@ typedef struct {
   int max_terms;     /* stencil terms of the busiest sector */
   long long stencil_terms; /* total stencil terms over all sectors */
   size_t device_bytes;     /* device memory owned by the plan tables */
+  int batched_kernel;      /* applies with >= 2 columns: 0 general tile kernel, 1 fixed-structure
+                              register kernel, 2 canonical-position register-reuse kernel */
 } pi_plan_info_t;
 int pi_plan_info(const pi_plan* plan, pi_plan_info_t* out);
 
@@ -139,6 +141,15 @@ int pi_apply_f64(pi_plan* plan, double* y_dev, const double* x_dev, int ncols, l
  * exponent range (stored PI coefficients of large-f sectors fall below 1e-38 near N=300). */
 int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld,
                  int coords, void* stream);
+/* Batched FP32 action on an element-major batch: y[e*ld + c] = (L x_c)[e] for the ncols
+ * right-hand sides c (a (dim, ncols) row-major array of complex values, e.g. a batch of
+ * Krylov vectors or initial states kept side by side).  Replaces the matrix form of
+ * apply! (liouvillian.jl:3232-3251) for a batch held in this layout.  ncols and ld even,
+ * both buffers 16-byte aligned.  Needs a plan whose stencil sits at the canonical
+ * positions (pi_plan_info_t.batched_kernel == 2); builds and caches the merged coefficient
+ * planes (about 80 bytes per PI coordinate) on first use. */
+int pi_apply_f32_em(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld,
+                    int coords, void* stream);
 /* Convenience with host buffers: copies x in, applies, copies y out (pinned host memory
  * gives full link bandwidth).  The FP32 variant takes PI_COORDS_* like pi_apply_f32. */
 int pi_apply_host_f64(pi_plan* plan, double* y_host, const double* x_host, int ncols);

@@ -176,6 +176,7 @@ int upload_plan(pi_plan* plan) {
   // imaginary RIGHT and fast_sr real sandwich terms per sector, padded with zero terms.
   std::vector<DevTerm> fterms;
   int fast_sr = 0;
+  int fast_zero_off = -1;  // zero coefficient pool of the fixed-structure tables
   {
     bool ok = true;
     int max_sr = 0;
@@ -193,6 +194,7 @@ int upload_plan(pi_plan* plan) {
         coef32z.push_back(make_float2(0, 0));
       }
       const int zero_off = (int)coef64.size();
+      fast_zero_off = zero_off;
       const int zlen = ((hp.max_n + 3) / 4) * 4 + 4;
       for (int i = 0; i < zlen; ++i) {
         coef64.push_back(make_double2(0, 0));
@@ -212,6 +214,66 @@ int upload_plan(pi_plan* plan) {
       }
     }
   }
+  // Canonical-position table for the register-reuse batched kernel (pi_apply.cu,
+  // k_apply_canon): per sector kCanonEntries int4 (alpha_off, beta_off, 0, 0):
+  //   [0] ADD; [1], [2] imaginary LEFT at row shift p = -1, +1; [3], [4] imaginary RIGHT at
+  //   column shift q = -1, +1; then, for each source slot (0..2) and diagonal shift
+  //   p = q = -1, 0, +1, kCanonPerPos real sandwich terms (zero-padded).
+  // Built only when every term of every sector sits at one of these positions.
+  std::vector<int4> canon;
+  int canon_plus = 0;
+  if (fast_sr > 0) {
+    bool ok = true;
+    std::vector<int4> table;
+    const int zoff = fast_zero_off;
+    for (int s = 0; s < S && ok; ++s) {
+      std::vector<int4> e(kCanonEntries, make_int4(zoff, zoff, 0, 0));
+      int nsand[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      bool have_add = false, have_l[2] = {false, false}, have_r[2] = {false, false};
+      for (int g = 0; g < G_COUNT && ok; ++g) {
+        for (const DevTerm& dt : by_group[s][g]) {
+          // woff = slot * kWinElems + p + q * kWinRows, |p|, |q| <= kHalo
+          const int span = kHalo + kHalo * kWinRows;
+          const int slot = (dt.woff + span) / kWinElems;
+          const int rem = dt.woff - slot * kWinElems;
+          // rem = p + q * kWinRows with p, q in [-2, 2]
+          int q = (rem + 2 + 2 * kWinRows) / kWinRows - 2;
+          int p = rem - q * kWinRows;
+          if (g == G_ADD) {
+            ok = slot == 1 && p == 0 && q == 0 && !have_add;
+            e[0] = make_int4(dt.alpha_off, dt.beta_off, 0, 0);
+            have_add = true;
+          } else if (g == G_LEFT_IM) {
+            const int i = p < 0 ? 0 : 1;
+            ok = slot == 1 && q == 0 && (p == -1 || p == 1) && !have_l[i];
+            e[1 + i] = make_int4(dt.alpha_off, dt.beta_off, 0, 0);
+            have_l[i] = true;
+          } else if (g == G_RIGHT_IM) {
+            const int i = q < 0 ? 0 : 1;
+            ok = slot == 1 && p == 0 && (q == -1 || q == 1) && !have_r[i];
+            e[3 + i] = make_int4(dt.alpha_off, dt.beta_off, 0, 0);
+            have_r[i] = true;
+          } else if (g == G_SAND_RE) {
+            ok = p == q && p >= -1 && p <= 1;
+            if (!ok) break;
+            const int pos = slot * 3 + (p + 1);
+            if (nsand[pos] >= kCanonPerPos) {
+              ok = false;
+              break;
+            }
+            e[5 + pos * kCanonPerPos + nsand[pos]] = make_int4(dt.alpha_off, dt.beta_off, 0, 0);
+            ++nsand[pos];
+            if (p == 1) canon_plus = 1;
+          } else {
+            ok = false;
+          }
+          if (!ok) break;
+        }
+      }
+      table.insert(table.end(), e.begin(), e.end());
+    }
+    if (ok && zoff >= 0) canon.swap(table);
+  }
   // Largest sectors first: their tiles are the longest-running.
   std::stable_sort(tiles.begin(), tiles.end(), [&](const DevTile& x, const DevTile& y) {
     return hp.sectors[x.sector].n > hp.sectors[y.sector].n;
@@ -230,6 +292,10 @@ int upload_plan(pi_plan* plan) {
     if ((rc = upload(plan, fterms, &ft))) return rc;
     plan->dev.fterms = reinterpret_cast<const int4*>(ft);
     plan->dev.fast_sr = fast_sr;
+  }
+  if (!canon.empty()) {
+    if ((rc = upload(plan, canon, &plan->dev.canon))) return rc;
+    plan->dev.canon_plus = canon_plus;
   }
   if ((rc = upload(plan, diag_index, &plan->dev.diag_index))) return rc;
   plan->dev.nsectors = S;
@@ -446,6 +512,7 @@ int pi_plan_info(const pi_plan* plan, pi_plan_info_t* out) {
   out->max_terms = plan->host.max_terms;
   out->stencil_terms = plan->stencil_terms;
   out->device_bytes = plan->device_bytes;
+  out->batched_kernel = plan->dev.canon ? 2 : (plan->dev.fast_sr > 0 ? 1 : 0);
   return PI_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <atomic>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -24,6 +25,12 @@ struct pi_plan {
   size_t stage_bytes = 0;
   cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
   std::atomic<int> busy{0};
+  // Element-major batched apply (pi_apply_em.cu): tile list and merged coefficient planes,
+  // built on first use (FP32 reference / population coordinates).
+  std::mutex em_mu;
+  const picuda::DevTile* em_tiles = nullptr;
+  int em_ntiles = 0;
+  const float2* em_planes32[2] = {nullptr, nullptr};
 };
 
 namespace picuda {

@@ -22,6 +22,8 @@ struct DevicePlan {
   const long long* diag_index = nullptr;  // per diagonal entry: its element index
   const int4* fterms = nullptr;     // padded fixed-structure term table (batched apply)
   int fast_sr = 0;                   // real sandwich terms per sector of the fixed structure (0: none)
+  const int4* canon = nullptr;      // canonical-position table (kCanonEntries per sector) or null
+  int canon_plus = 0;                // some sandwich term sits at the +1 diagonal shift
   int nsectors = 0;
   int ntiles = 0;
   int ndiag = 0;
@@ -31,6 +33,11 @@ struct DevicePlan {
 // Applies with at least this many right-hand sides use the fixed-structure batched kernel
 // when the plan has one.
 constexpr int kFastMinCols = 2;
+
+// Canonical-position table: ADD, LEFT(p = -1, +1), RIGHT(q = -1, +1), then per source slot
+// and diagonal shift p = q = -1, 0, +1 up to kCanonPerPos real sandwich terms.
+constexpr int kCanonPerPos = 3;
+constexpr int kCanonEntries = 5 + 9 * kCanonPerPos;  // 32
 
 // Apply kernels (pi_apply.cu).
 cudaError_t launch_apply_f64(const DevicePlan& dp, const double* x, double* y, int ncols, long long ld,

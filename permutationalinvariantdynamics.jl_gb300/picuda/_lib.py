@@ -58,7 +58,8 @@ class pi_capability_t(C.Structure):
 class pi_plan_info_t(C.Structure):
     _fields_ = [("N", C.c_int), ("nsectors", C.c_int), ("dim", C.c_longlong),
                 ("max_block", C.c_int), ("max_terms", C.c_int),
-                ("stencil_terms", C.c_longlong), ("device_bytes", C.c_size_t)]
+                ("stencil_terms", C.c_longlong), ("device_bytes", C.c_size_t),
+                ("batched_kernel", C.c_int)]
 
 
 class pi_gmres_opts_t(C.Structure):
@@ -150,6 +151,7 @@ PROTOTYPES = {
     "pi_sector_multiplicity": (C.c_int, [C.c_int, C.c_int, _D, _D]),
     "pi_apply_f64": (C.c_int, [_P, _P, _P, C.c_int, C.c_longlong, _P]),
     "pi_apply_f32": (C.c_int, [_P, _P, _P, C.c_int, C.c_longlong, C.c_int, _P]),
+    "pi_apply_f32_em": (C.c_int, [_P, _P, _P, C.c_int, C.c_longlong, C.c_int, _P]),
     "pi_apply_host_f64": (C.c_int, [_P, _P, _P, C.c_int]),
     "pi_apply_host_f32": (C.c_int, [_P, _P, _P, C.c_int, C.c_int]),
     "pi_dot_f64": (C.c_int, [_P, _P, _P, _D]),

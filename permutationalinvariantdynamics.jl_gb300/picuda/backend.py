@@ -241,6 +241,28 @@ def apply_(y, compiled: CompiledPIModel, x, t=0.0, p=None, precision="fp64", coo
     return y
 
 
+def apply_element_major_(y, compiled: CompiledPIModel, x, coords="population"):
+    """Batched FP32 apply on an element-major batch: y[e, c] = (L x[:, c])[e].
+
+    x, y: complex64 CUDA tensors of shape (dim, ncols) with unit column stride and an even
+    row stride (ncols even) -- the batch kept side by side per PI coordinate.  Needs a plan
+    with compiled.info["batched_kernel"] == 2 (real one-body qubit operators)."""
+    torch = _torch()
+    lib = _lib.load()
+    n = len(compiled.basis)
+    if x.shape != y.shape or x.dim() != 2 or x.shape[0] != n or not x.is_cuda or not y.is_cuda:
+        raise PiDimensionMismatch("element-major batches have shape (dim, ncols) on the GPU")
+    if x.dtype != torch.complex64 or y.dtype != torch.complex64:
+        raise PiArgumentError("element-major apply needs complex64 tensors")
+    if x.stride(1) != 1 or y.stride(1) != 1 or x.stride(0) != y.stride(0):
+        raise PiArgumentError("element-major batches need unit column stride and equal row strides")
+    cc = _lib.PI_COORDS_POPULATION if coords == "population" else _lib.PI_COORDS_REFERENCE
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(lib.pi_apply_f32_em(compiled.handle, _ptr(y), _ptr(x), x.shape[1], x.stride(0), cc, stream),
+               "apply! (element-major batch)")
+    return y
+
+
 def mul(compiled: CompiledPIModel, x):
     """L * x for a host vector (allocating wrapper of apply!)."""
     y = np.empty_like(np.asarray(x, dtype=np.complex128))

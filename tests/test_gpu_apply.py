@@ -178,3 +178,89 @@ def test_library_basis_maps_bit_exact(torch_cuda):
         idx, val = compiled.library_trace_functional()
         oidx, oval = O.trace_functional(ob)
         assert np.array_equal(idx, oidx) and np.array_equal(val, oval.real)
+
+
+@pytest.mark.parametrize("name,make,kernel", [
+    ("c2_N40", lambda: M.ensemble_c2(40), 2),
+    ("pump_decay_N12", lambda: picuda.Models.local_pump_decay(12, down=1.0, up=0.3), 2),
+    ("driven_N9", lambda: M.driven_c1(9), 2),
+    ("general_N7", lambda: M.general(7, 2), 0),
+])
+def test_batched_kernel_paths_match_oracle(torch_cuda, name, make, kernel):
+    """The plan picks the canonical-position kernel for real-operator qubit models (with and
+    without +1 diagonal shifts, i.e. pumping) and the general tile kernel otherwise; every
+    path matches the oracle."""
+    torch = torch_cuda
+    model = make()
+    compiled = picuda.compile(model)
+    assert compiled.info["batched_kernel"] == kernel, name
+    oplan = O.Plan(M.to_oracle(model))
+    n = len(model.basis)
+    X = np.stack([M.random_state_vector(n, 40 + s) for s in range(5)])
+    Yd = torch.empty((5, n), dtype=torch.complex128, device="cuda")
+    picuda.apply_(Yd, compiled, _dev(torch, X))
+    Y32 = torch.empty((5, n), dtype=torch.complex64, device="cuda")
+    picuda.apply_(Y32, compiled, _dev(torch, X, torch.complex64), precision="fp32", coords="reference")
+    torch.cuda.synchronize()
+    for c in range(5):
+        ref = O.apply(oplan, X[c])
+        assert np.abs(Yd[c].cpu().numpy() - ref).max() <= TOL_F64 * np.abs(ref).max(), name
+        assert np.abs(Y32[c].cpu().numpy() - ref).max() <= TOL_F32 * np.abs(ref).max(), name
+
+
+@pytest.mark.parametrize("name,make", [
+    ("c2_N40", lambda: M.ensemble_c2(40)),
+    ("c2_N121", lambda: M.ensemble_c2(121)),
+    ("pump_decay_N12", lambda: picuda.Models.local_pump_decay(12, down=1.0, up=0.3)),
+    ("scan_N33", lambda: M.scan_model(33, 1.3, 0.2, 0.05)),
+])
+@pytest.mark.parametrize("coords", ["reference", "population"])
+def test_element_major_apply_matches_column_apply(torch_cuda, name, make, coords):
+    """Element-major batch (dim, ncols) against the column-batch FP32 apply and the oracle."""
+    torch = torch_cuda
+    model = make()
+    compiled = picuda.compile(model)
+    n = len(model.basis)
+    ncols = 6
+    X = np.stack([M.random_state_vector(n, 60 + s) for s in range(ncols)])  # (ncols, n)
+    Xc = _dev(torch, X, torch.complex64)
+    Yc = torch.empty_like(Xc)
+    picuda.apply_(Yc, compiled, Xc, precision="fp32", coords=coords)
+    Xe = Xc.t().contiguous()  # (n, ncols)
+    Ye = torch.empty_like(Xe)
+    picuda.apply_element_major_(Ye, compiled, Xe, coords=coords)
+    torch.cuda.synchronize()
+    got = Ye.t().cpu().numpy()
+    ref = Yc.cpu().numpy()
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() <= 2e-6 * scale, name
+    if coords == "reference":
+        oplan = O.Plan(M.to_oracle(model))
+        for c in range(ncols):
+            r = O.apply(oplan, X[c])
+            assert np.abs(got[c] - r).max() <= TOL_F32 * np.abs(r).max(), name
+
+
+def test_element_major_apply_padded_stride_and_errors(torch_cuda):
+    torch = torch_cuda
+    model = M.ensemble_c2(20)
+    compiled = picuda.compile(model)
+    n = len(model.basis)
+    base = torch.randn((n, 10), dtype=torch.complex64, device="cuda")
+    X = base[:, :8]  # row stride 10, 8 columns
+    Yb = torch.zeros((n, 10), dtype=torch.complex64, device="cuda")
+    Y = Yb[:, :8]
+    picuda.apply_element_major_(Y, compiled, X)
+    ref = torch.empty_like(X.t().contiguous())
+    picuda.apply_(ref, compiled, X.t().contiguous(), precision="fp32", coords="population")
+    torch.cuda.synchronize()
+    assert (Y.t() - ref).abs().max().item() <= 2e-6 * ref.abs().max().item()
+    assert torch.count_nonzero(Yb[:, 8:]).item() == 0  # padding columns untouched
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.apply_element_major_(torch.empty((n, 7), dtype=torch.complex64, device="cuda")[:, :7], compiled,
+                                    torch.empty((n, 7), dtype=torch.complex64, device="cuda"))
+    general = picuda.compile(M.general(6, 2))
+    ng = len(general.basis)
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.apply_element_major_(torch.empty((ng, 2), dtype=torch.complex64, device="cuda"), general,
+                                    torch.empty((ng, 2), dtype=torch.complex64, device="cuda"))
