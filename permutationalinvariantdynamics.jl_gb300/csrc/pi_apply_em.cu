@@ -99,38 +99,27 @@ __global__ void k_em_planes(const DevSector* __restrict__ sectors, const int4* _
   }
 }
 
-// Scalar FP32 FMA kept scalar: left to itself the compiler pairs independent FMAs that
-// share an operand into packed two-wide FP32 instructions, which GB300 issues to its narrow
-// FP64 pipe (measured: one such instruction per multiply-accumulate group, the pipe 85%
-// busy and the kernel bound by it).
-__device__ __forceinline__ float sfma(float a, float b, float c) {
-  float d;
-  asm("fma.rn.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-  return d;
-}
-
 __device__ __forceinline__ void cmac2(float4& acc, const float cr, const float ci, const float4 v) {
   // acc.(xy) += c * v.(xy), acc.(zw) += c * v.(zw) (complex c = cr + i ci)
-  acc.x = sfma(cr, v.x, acc.x);
-  acc.x = sfma(-ci, v.y, acc.x);
-  acc.y = sfma(cr, v.y, acc.y);
-  acc.y = sfma(ci, v.x, acc.y);
-  acc.z = sfma(cr, v.z, acc.z);
-  acc.z = sfma(-ci, v.w, acc.z);
-  acc.w = sfma(cr, v.w, acc.w);
-  acc.w = sfma(ci, v.z, acc.w);
+  acc.x = fmaf(cr, v.x, acc.x);
+  acc.x = fmaf(-ci, v.y, acc.x);
+  acc.y = fmaf(cr, v.y, acc.y);
+  acc.y = fmaf(ci, v.x, acc.y);
+  acc.z = fmaf(cr, v.z, acc.z);
+  acc.z = fmaf(-ci, v.w, acc.z);
+  acc.w = fmaf(cr, v.w, acc.w);
+  acc.w = fmaf(ci, v.z, acc.w);
 }
 __device__ __forceinline__ void rmac2(float4& acc, const float c, const float4 v) {
-  acc.x = sfma(c, v.x, acc.x);
-  acc.y = sfma(c, v.y, acc.y);
-  acc.z = sfma(c, v.z, acc.z);
-  acc.w = sfma(c, v.w, acc.w);
+  acc.x = fmaf(c, v.x, acc.x);
+  acc.y = fmaf(c, v.y, acc.y);
+  acc.z = fmaf(c, v.z, acc.z);
+  acc.w = fmaf(c, v.w, acc.w);
 }
 
 // A source stream: one column of one source block, walked row by row as the warp walks its
 // output rows.  Positions are 32-bit indices in float4 units (dim * ld/2 < 2^32, checked on
-// the host) advanced with 32-bit adds: on GB300 64-bit integer adds and wide multiplies
-// issue to the narrow FP64 pipe, so none is left in the row loop.
+// the host), advanced by the row stride with one 32-bit add per row.
 struct Stream {
   unsigned idx;  // float4 index of row `row` (meaningful when the row and column are valid)
   int row;
