@@ -53,14 +53,16 @@ def to_oracle(model):
 def solve_rates(picuda, torch):
     """Solves/s of the reference's Krylov methods, plain FP64 vs mixed precision.
 
-    steady state: driven qubits N=20 (H = Jx, local decay 0.5; dim 1771), GMRES(50) to
-    atol 1e-10 / rtol 1e-8 -- the largest size of this family that the reference's
-    unpreconditioned restarted GMRES brings to tolerance;
-    dynamics: the N=120 ensemble, expv m=30 over one dt = 0.05 interval from the
-    all-excited state."""
+    steady state: driven qubits N=16 (H = Jx, local decay 0.5; dim 969), GMRES(50) to
+    atol 1e-10 / rtol 1e-8 -- a size of this family that the reference's unpreconditioned
+    restarted GMRES brings to tolerance with margin (N=20 sits on the edge of its final
+    trace test);
+    dynamics: the N=120 ensemble, expv m=30 over 20 saved intervals of dt = 0.05 from the
+    all-excited state with observables Jz and J+J- streamed at every saved time (the large
+    time-evolution configuration runs 200 such intervals); observables built once."""
     out = {}
     sm = picuda.spin_matrices(2)
-    ss_model = picuda.Models.driven_qubits(20, drive=1.0, emission=0.5, pumping=0.0)
+    ss_model = picuda.Models.driven_qubits(16, drive=1.0, emission=0.5, pumping=0.0)
     cm = picuda.compile(ss_model)
     for prec in ("fp64", "mixed"):
         alg = picuda.GMRESAlgorithm(krylovdim=50, maxiter=5000, precision=prec)
@@ -78,20 +80,26 @@ def solve_rates(picuda, torch):
     ref = None
     c2 = picuda.compile(model_c2(picuda))
     rho0 = picuda.computational_product_state(c2.basis, 2)
-    obs = {"Jz": sm["jz"], "JpJm": sm["jp"] @ sm["jm"]}
+    obs = {"Jz": picuda.collective_operator(c2.basis, sm["jz"]),
+           "JpJm": picuda.collective_operator(c2.basis, sm["jp"] @ sm["jm"])}
+    nint = 20
     for prec in ("fp64", "mixed"):
         alg = picuda.ExpvAlgorithm(krylovdim=30, precision=prec)
+        picuda.solve_dynamics(c2, rho0, (0.0, 0.05), algorithm=alg, observables=obs, save_states=False)  # warm
         times = []
         for _ in range(3):
             t0 = time.perf_counter()
-            res = picuda.solve_dynamics(c2, rho0, (0.0, 0.05), algorithm=alg, observables=obs, save_states=False)
+            res = picuda.solve_dynamics(c2, rho0, (0.0, 0.05 * nint), saveat=0.05, algorithm=alg, observables=obs,
+                                        save_states=False)
             times.append(time.perf_counter() - t0)
-        vals = np.array([res.values[k][-1] for k in obs])
+        vals = np.array([res.values[k] for k in obs])
         if prec == "fp64":
             ref = vals
-        out[f"expv_{prec}"] = {"intervals_per_s": 1.0 / statistics.median(times),
-                               "p50_ms": statistics.median(times) * 1e3, "p99_ms": max(times) * 1e3,
-                               "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref)))}
+        per = statistics.median(times) / nint
+        out[f"expv_{prec}"] = {"intervals_per_s": 1.0 / per, "ms_per_interval": per * 1e3,
+                               "p50_ms_per_call": statistics.median(times) * 1e3, "p99_ms_per_call": max(times) * 1e3,
+                               "intervals_per_call": nint,
+                               "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref).max()))}
     return out
 
 

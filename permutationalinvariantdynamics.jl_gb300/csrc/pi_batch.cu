@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <random>
 #include <tuple>
 #include <unordered_set>
 #include <utility>
@@ -69,8 +70,8 @@ __device__ __forceinline__ void df_add_prod(DF& acc, float a, float b) {
 }
 
 __device__ __forceinline__ void chunk_range(const DevInst& S, int c, long long& beg, long long& end) {
-  beg = (long long)(c - S.chunk_begin) * kBatchChunk;
-  end = min(beg + (long long)kBatchChunk, S.dim);
+  beg = (long long)(c - S.chunk_begin) * S.chunk;
+  end = min(beg + (long long)S.chunk, S.dim);
 }
 
 constexpr int kRT = kReduceThreads;  // threads of the chunk kernels
@@ -568,8 +569,8 @@ __global__ void __launch_bounds__(kRT) k_step_normalize(const DevInst* __restric
 // never straddle a column; padding entries stay zero through every update.
 
 __device__ __forceinline__ void pair_range(const DevInst& S, int c, long long& beg, long long& end) {
-  beg = (long long)(c - S.chunk_begin) * (kBatchChunk / 2);
-  end = min(beg + (long long)(kBatchChunk / 2), (S.dim + 1) / 2);
+  beg = (long long)(c - S.chunk_begin) * (S.chunk / 2);
+  end = min(beg + (long long)(S.chunk / 2), (S.dim + 1) / 2);
 }
 
 // a += t, the rounding error of the addition carried in a.lo (TwoSum).
@@ -616,20 +617,21 @@ __device__ __forceinline__ double block_df_sum(DF v, float2* smem) {
 }
 
 // CGS2 projections for an FP32 basis: partv[c][i] = conj(V_i) . w over chunk c for every
-// i <= j.  Each thread keeps its kPairs element pairs of w in registers and streams every
+// i <= j.  The block stages its chunk of w (CH elements) in shared memory and streams every
 // basis column once: per column it forms each pair term (two complex products) in FP32 and
 // accumulates the terms in double-float (no rounding error in the accumulation), then the
 // warp sums its lanes in FP64 into shared memory.
-constexpr int kPairs = kBatchChunk / 2 / kRT;  // element pairs per thread and chunk
 
 __device__ __forceinline__ void pair_terms(const float4 a, const float4 b, DF& re, DF& im) {
   df_add(re, fmaf(a.x, b.x, fmaf(a.y, b.y, fmaf(a.z, b.z, a.w * b.w))));
   df_add(im, fmaf(a.x, b.y, fmaf(-a.y, b.x, fmaf(a.z, b.w, -(a.w * b.z)))));
 }
 
+template <int CH>
 __global__ void __launch_bounds__(kRT, 3)
     k_step_mdot_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv) {
-  __shared__ float4 wsm[kBatchChunk / 2];
+  constexpr int kPairs = CH / 2 / kRT;  // element pairs per thread and chunk
+  __shared__ float4 wsm[CH / 2];
   __shared__ float4 red[kMaxDots][kRT / 32];  // per warp: (re.hi, re.lo, im.hi, im.lo)
   const DevInst& S = st[chunk_inst[blockIdx.x]];
   if (S.done) return;
@@ -1281,8 +1283,8 @@ pi_expv_info_t DynamicsJob::info() const {
 // Steady-state job
 // ---------------------------------------------------------------------------------------
 
-SteadyJob::SteadyJob(pi_plan* p, double* x, const pi_gmres_opts_t& o, unsigned long long seed)
-    : x_((double2*)x), o_(o), seed_(seed) {
+SteadyJob::SteadyJob(pi_plan* p, double* x, const pi_gmres_opts_t& o, unsigned long long seed, bool host_probes)
+    : x_((double2*)x), o_(o), seed_(seed), host_probes_(host_probes) {
   plan = p;
   dim = p->host.dim;
 }
@@ -1313,6 +1315,19 @@ bool SteadyJob::setup(cudaStream_t s, int m, bool f32) {
   }
   if (e == cudaSuccess && !o_.use_initial) e = cudaMemcpyAsync(x_, b_, sizeof(double2) * dim, cudaMemcpyDeviceToDevice, s);
   if (e != cudaSuccess) return false;
+  if (host_probes_ && o_.operator_scale <= 0) {
+    // krylov.jl:156-169 draws three complex normal probes from a seeded generator
+    probes_ = (double2*)alloc(sizeof(double2) * dim * 3, &e);
+    if (e != cudaSuccess) return false;
+    std::vector<double2> h((size_t)dim * 3);
+    std::mt19937_64 rng(seed_);
+    std::normal_distribution<double> nd(0.0, 1.0);
+    // same expression as the host-driven solver (argument evaluation order included)
+    for (size_t i = 0; i < h.size(); ++i) h[i] = make_double2(nd(rng) * M_SQRT1_2, nd(rng) * M_SQRT1_2);
+    e = cudaMemcpyAsync(probes_, h.data(), sizeof(double2) * h.size(), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // h is released on return
+    if (e != cudaSuccess) return false;
+  }
   state_ = INIT;
   return true;
 }
@@ -1323,15 +1338,21 @@ unsigned SteadyJob::stage1(DevInst& d, double2* coef) {
       d.nrm0 = b_;
       return S1_NORM;
     case SCALE:
-      d.probe = r_;
-      d.seed = seed_ * 4 + (unsigned long long)probe_;
-      d.ax = r_;
+      if (probes_) {
+        const double2* pr = probes_ + (size_t)probe_ * dim;
+        d.ax = pr;
+        d.nrm0 = pr;
+      } else {
+        d.probe = r_;
+        d.seed = seed_ * 4 + (unsigned long long)probe_;
+        d.ax = r_;
+        d.nrm0 = r_;
+      }
       d.ay = ay_;
       d.aux_scale = 1.0;
       d.aux_border = 0;
-      d.nrm0 = r_;
       d.nrm1 = ay_;
-      return S1_PROBE | S1_AUX | S1_NORM;
+      return (probes_ ? 0u : S1_PROBE) | S1_AUX | S1_NORM;
     case RESID: {
       unsigned f = 0;
       if (pending_update_) {
@@ -1555,6 +1576,11 @@ std::vector<Job*> Engine::retire() {
 void Engine::rebuild() {
   const int n = (int)jobs_.size();
   const size_t nn = std::max(n, 1);
+  // Chunk size: large chunks amortise the per-block reductions; when the active jobs hold
+  // fewer elements than about eight large chunks per SM, small chunks keep the GPU full.
+  long long total_elems = 0;
+  for (int i = 0; i < n; ++i) total_elems += jobs_[i]->dim;
+  chunk_ = total_elems >= 8LL * 152 * kBatchChunk ? kBatchChunk : kBatchChunkSmall;
   std::vector<int> ti, tl, ci, nc(n);
   for (int i = 0; i < n; ++i) {
     const int ntiles = jobs_[i]->plan->dev.ntiles;
@@ -1562,7 +1588,7 @@ void Engine::rebuild() {
       ti.push_back(i);
       tl.push_back(t);
     }
-    nc[i] = (int)((jobs_[i]->dim + kBatchChunk - 1) / kBatchChunk);
+    nc[i] = (int)((jobs_[i]->dim + chunk_ - 1) / chunk_);
   }
   reserve(&hab_, &hab_cap_, sizeof(double2) * 2 * kMaxDots * nn, false);
   reserve(&rec_, &rec_cap_, sizeof(double2) * rec_stride_ * nn, false);
@@ -1585,6 +1611,7 @@ void Engine::rebuild() {
     d.ldv = J->ldv;
     d.ndiag = dp.ndiag;
     d.chunk_begin = (int)ci.size();
+    d.chunk = chunk_;
     for (int c = 0; c < nc[i]; ++c) ci.push_back(i);
     d.V = J->V;
     d.w = J->w;
@@ -1669,10 +1696,16 @@ void Engine::arnoldi_step() {
     launch(k_bapply<float, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(float2), (const DevInst*)st, ti, tl);
     launch(k_step_image_f32, C, kRT, 0, (const DevInst*)st, ci, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);
-    launch(k_step_mdot_f32, C, kRT, 0, (const DevInst*)st, ci, partv);
+    if (chunk_ == kBatchChunk)
+      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv);
+    else
+      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv);
     launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 0, none);
-    launch(k_step_mdot_f32, C, kRT, 0, (const DevInst*)st, ci, partv);
+    if (chunk_ == kBatchChunk)
+      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv);
+    else
+      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv);
     launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 1, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
@@ -1812,6 +1845,45 @@ bool Engine::tick() {
   for (int i = 0; i < n; ++i)
     if (in_enl[i]) jobs_[i]->after_enlarge(dl[i], rech + (size_t)i * rec_stride_);
   return err == cudaSuccess;
+}
+
+int run_single_job(pi_plan* plan, Job* job, int m, bool f32, const char* what) {
+  if (plan->engine && (plan->engine_m != m || plan->engine_f32 != f32 || plan->engine->err != cudaSuccess)) {
+    delete plan->engine;
+    plan->engine = nullptr;
+  }
+  if (!plan->engine) {
+    plan->engine = new Engine(plan->device, m, f32, true);
+    plan->engine_m = m;
+    plan->engine_f32 = f32;
+    if (plan->engine->err != cudaSuccess) {
+      const cudaError_t e = plan->engine->err;
+      delete plan->engine;
+      plan->engine = nullptr;
+      return cuda_fail(e, what);
+    }
+  }
+  Engine& E = *plan->engine;
+  if (!job->setup(E.stream(), E.m(), E.f32())) return cuda_fail(cudaErrorMemoryAllocation, what);
+  E.add(job);
+  while (E.njobs() > 0) {
+    if (!E.tick()) {
+      const cudaError_t e = E.err;
+      E.retire();
+      delete plan->engine;
+      plan->engine = nullptr;
+      return cuda_fail(e, what);
+    }
+    for (Job* j : E.retire()) j->finish(E.stream());
+  }
+  const cudaError_t e = cudaStreamSynchronize(E.stream());
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return PI_OK;
+}
+
+void release_plan_engine(pi_plan* plan) {
+  delete plan->engine;
+  plan->engine = nullptr;
 }
 
 namespace {

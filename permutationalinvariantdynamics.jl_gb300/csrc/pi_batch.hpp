@@ -29,7 +29,8 @@
 
 namespace picuda {
 
-constexpr int kBatchChunk = 4096;  // elements per reduction chunk
+constexpr int kBatchChunk = 4096;       // elements per reduction chunk, large batches
+constexpr int kBatchChunkSmall = 1024;  // when the active jobs hold few elements in total
 constexpr int kBatchMaxObs = 16;   // observables per dynamics job
 constexpr int kOutSlots = 4 + 2 * kBatchMaxObs;  // per-job stage-1 outputs (doubles)
 constexpr int kBatchMaxKrylov = 120;
@@ -63,6 +64,7 @@ struct DevInst {
   long long ldv;    // basis column stride: dim rounded up to a multiple of 64, zero padded
   int ndiag;
   int chunk_begin;  // first chunk of this job in the engine's chunk list
+  int chunk;        // elements per chunk (the engine's choice, kBatchChunkSmall or kBatchChunk)
   // Krylov cycle
   void* V;  // m + 2 basis columns (FP64 or FP32)
   void* w;
@@ -205,7 +207,10 @@ class DynamicsJob : public Job {
 // (krylov.jl:732-891), FP64 or FP32 inner cycles with FP64 residual refinement.
 class SteadyJob : public Job {
  public:
-  SteadyJob(pi_plan* p, double* x, const pi_gmres_opts_t& o, unsigned long long seed);
+  // host_probes: draw the operator-scale probes on the host (std::mt19937_64 with the seed,
+  // complex normal entries in element order, as the single-instance solver always has);
+  // otherwise a counter-based generator on the device.
+  SteadyJob(pi_plan* p, double* x, const pi_gmres_opts_t& o, unsigned long long seed, bool host_probes = false);
   bool setup(cudaStream_t s, int m, bool f32) override;
   unsigned stage1(DevInst& d, double2* coef) override;
   void after_stage1(const double* out) override;
@@ -223,6 +228,8 @@ class SteadyJob : public Job {
   double2* b_ = nullptr;
   double2* r_ = nullptr;
   double2* ay_ = nullptr;
+  double2* probes_ = nullptr;  // host-drawn probes (3 x dim), when host_probes_
+  bool host_probes_ = false;
   State state_ = INIT;
   int probe_ = 0;
   double scale_ = 0, s_op_ = 0, tol_ = 0, beta_ = 0;
@@ -232,6 +239,12 @@ class SteadyJob : public Job {
   double linear_residual_ = 0;
   pi_gmres_info_t info_{};
 };
+
+// Runs one job to completion on the plan's cached engine (Krylov dimension m, FP32 basis
+// when f32); returns PI_OK or a CUDA failure status, the job's own status is job->rc.
+int run_single_job(pi_plan* plan, Job* job, int m, bool f32, const char* what);
+// Releases a plan's cached engine (plan teardown).
+void release_plan_engine(pi_plan* plan);
 
 // The engine: membership, work lists, stage execution.
 class Engine {
@@ -273,6 +286,7 @@ class Engine {
   std::vector<Job*> jobs_;
   bool dirty_ = true;
   int total_tiles_ = 0, total_chunks_ = 0;
+  int chunk_ = kBatchChunk;
   size_t rec_stride_ = 0;  // double2 per job record
   // device work lists and scratch (capacity-managed)
   void* st_ = nullptr; size_t st_cap_ = 0;

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/picuda.h"
+#include "pi_batch.hpp"
 #include "pi_handle.hpp"
 
 namespace picuda {
@@ -59,6 +60,7 @@ void free_plan(pi_plan* plan) {
   cudaGetDevice(&cur);
   cudaSetDevice(plan->device);
   if (plan->stream) cudaStreamSynchronize(plan->stream);
+  release_plan_engine(plan);
   for (void* p : plan->allocations) cudaFree(p);
   if (plan->stage_x) cudaFree(plan->stage_x);
   if (plan->stage_y) cudaFree(plan->stage_y);

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "../../include/picuda.h"
+#include "pi_batch.hpp"
 #include "pi_dense.hpp"
 #include "pi_handle.hpp"
 
@@ -393,6 +394,14 @@ int pi_expv(pi_plan* plan, double* x_dev, double t, const pi_expv_opts_t* opts, 
   if (!std::isfinite(t)) return fail(PI_ERR_INVALID_ARGUMENT, "time must be finite");
   BusyGuard guard(plan);
   if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
+  if (opts->krylovdim <= kBatchMaxKrylov) {
+    // one job of the plan's batched engine: the whole Arnoldi cycle on the device
+    DynamicsJob job(plan, x_dev, {0.0, t}, 0, nullptr, nullptr, *opts, true);
+    rc = run_single_job(plan, &job, opts->krylovdim, opts->precision == PI_FP32, "expv");
+    if (rc) return rc;
+    if (info) *info = job.info();
+    return job.rc == PI_OK ? PI_OK : fail(job.rc, job.msg);
+  }
   pi_expv_info_t loc;
   ExpvWork W{plan, plan->stream, plan->host.dim, (int)std::min<long long>(opts->krylovdim, plan->host.dim),
              opts->precision == PI_FP32};
@@ -431,6 +440,13 @@ int pi_solve_dynamics(pi_plan* plan, double* rho_dev, int nt, const double* time
       return fail(PI_ERR_INVALID_ARGUMENT, "Krylov exponential output times must be nondecreasing");
   BusyGuard guard(plan);
   if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
+  if (opts->krylovdim <= kBatchMaxKrylov && nobs <= kBatchMaxObs) {
+    DynamicsJob job(plan, rho_dev, std::vector<double>(times, times + nt), nobs, obs_dev, values_host, *opts, false);
+    rc = run_single_job(plan, &job, opts->krylovdim, opts->precision == PI_FP32, "dynamics");
+    if (rc) return rc;
+    if (info) *info = job.info();
+    return job.rc == PI_OK ? PI_OK : fail(job.rc, job.msg);
+  }
   ExpvWork W{plan, plan->stream, plan->host.dim, (int)std::min<long long>(opts->krylovdim, plan->host.dim),
              opts->precision == PI_FP32};
   pi_expv_info_t total;

@@ -9,6 +9,10 @@
 #include "pi_internal.hpp"
 #include "pi_plan.hpp"
 
+namespace picuda {
+class Engine;
+}
+
 struct pi_plan {
   picuda::QubitPlan host;
   picuda::DevicePlan dev;
@@ -31,6 +35,11 @@ struct pi_plan {
   const picuda::DevTile* em_tiles = nullptr;
   int em_ntiles = 0;
   const float2* em_planes32[2] = {nullptr, nullptr};
+  // Single-instance solves run as one job of a batched engine kept with the plan (created on
+  // first use for a Krylov dimension and basis precision, replaced when those change).
+  picuda::Engine* engine = nullptr;
+  int engine_m = 0;
+  bool engine_f32 = false;
 };
 
 namespace picuda {

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/picuda.h"
+#include "pi_batch.hpp"
 #include "pi_dense.hpp"
 #include "pi_handle.hpp"
 
@@ -388,6 +389,14 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
     return fail(PI_ERR_INVALID_ARGUMENT, "precision must be PI_FP64 or PI_FP32");
   BusyGuard guard(plan);
   if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
+  if (opts->krylovdim <= kBatchMaxKrylov) {
+    // one job of the plan's batched engine: each GMRES cycle on the device, Givens included
+    SteadyJob job(plan, x_dev, *opts, 0x51ca1eULL, true);
+    const int rc = run_single_job(plan, &job, opts->krylovdim, opts->precision == PI_FP32, "GMRES");
+    if (rc) return rc;
+    if (info) *info = job.info();
+    return job.rc == PI_OK ? PI_OK : fail(job.rc, job.msg);
+  }
   Run R(plan);
   const long long n = R.n;
   const int m = (int)std::min<long long>(opts->krylovdim, n);
