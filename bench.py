@@ -59,7 +59,9 @@ def solve_rates(picuda, torch):
     trace test);
     dynamics: the N=120 ensemble, expv m=30 over 20 saved intervals of dt = 0.05 from the
     all-excited state with observables Jz and J+J- streamed at every saved time (the large
-    time-evolution configuration runs 200 such intervals); observables built once."""
+    time-evolution configuration runs 200 such intervals); observables built once.  The same
+    dynamics with the reference's default algorithm, fixed-step RK4 with 64 steps per saved
+    interval, FP64 and mixed (FP32 applies, double-float state)."""
     out = {}
     sm = picuda.spin_matrices(2)
     ss_model = picuda.Models.driven_qubits(16, drive=1.0, emission=0.5, pumping=0.0)
@@ -100,6 +102,27 @@ def solve_rates(picuda, torch):
                                "p50_ms_per_call": statistics.median(times) * 1e3, "p99_ms_per_call": max(times) * 1e3,
                                "intervals_per_call": nint,
                                "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref).max()))}
+    # The reference's default dynamics algorithm: fixed-step RK4, 64 steps per saved interval.
+    ref_expv = ref
+    for prec in ("fp64", "mixed"):
+        kw = dict(observables=obs, save_states=False, steps_per_interval=64, precision=prec)
+        picuda.solve_dynamics(c2, rho0, (0.0, 0.05), **kw)  # warm
+        times = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            res = picuda.solve_dynamics(c2, rho0, (0.0, 0.05 * nint), saveat=0.05, **kw)
+            times.append(time.perf_counter() - t0)
+        vals = np.array([res.values[k] for k in obs])
+        if prec == "fp64":
+            ref = vals
+        per = statistics.median(times) / nint
+        out[f"rk4_{prec}"] = {"intervals_per_s": 1.0 / per, "ms_per_interval": per * 1e3,
+                              "us_per_stage": per / 256 * 1e6,
+                              "p50_ms_per_call": statistics.median(times) * 1e3, "p99_ms_per_call": max(times) * 1e3,
+                              "intervals_per_call": nint, "steps_per_interval": 64,
+                              "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref).max())),
+                              "max_obs_rel_dev_vs_expv_fp64": float(np.max(np.abs(vals - ref_expv)
+                                                                           / np.abs(ref_expv).max()))}
     return out
 
 

@@ -240,6 +240,40 @@ int pi_solve_dynamics(pi_plan* plan, double* rho_dev, int nt, const double* time
                       int nobs, const double* obs_dev, double* values_host,
                       const pi_expv_opts_t* opts, pi_expv_info_t* info);
 
+/* ---- fixed-step RK4 (the reference's default dynamics algorithm) ---------------------
+ * evolve! (evolution.jl:75-118): steps classical RK4 steps of h = (t1 - t0) / steps with
+ * the reference's stage sequence and three scratch vectors.  Each step is four fused
+ * launches: the stencil apply of one stage with that stage's vector updates as its
+ * epilogue; the steps of one saved interval run as one CUDA graph.  PI_FP32 applies the
+ * operator in FP32 population coordinates (z = sqrt(f) x) while the state and the stage
+ * sum stay FP64. */
+typedef struct {
+  int steps_per_interval;  /* > 0; solve_dynamics' default is 64, evolve!'s is 256 */
+  int precision;           /* PI_FP64 or PI_FP32 */
+} pi_rk4_opts_t;
+
+typedef struct {
+  long long steps;                  /* RK4 steps taken */
+  long long operator_applications;  /* 4 per step */
+  double reached_time;
+} pi_rk4_info_t;
+
+void pi_rk4_default_opts(pi_rk4_opts_t* opts);
+
+/* evolve!(dest, L, src, (t0, t1); steps): dest_dev <- RK4 propagation of src_dev (device,
+ * complex FP64).  dest may equal src; partially overlapping storage is rejected
+ * (evolution.jl:83-84); steps must be positive (:82). */
+int pi_evolve(pi_plan* plan, double* dest_dev, const double* src_dev, double t0, double t1,
+              const pi_rk4_opts_t* opts, pi_rk4_info_t* info);
+
+/* solve_dynamics(..., algorithm=:auto | :rk4, saveat=times, steps_per_interval,
+ * observables=obs, save_states=false) (highlevel.jl:559-566, 693-733): RK4 over every
+ * saved interval, zero-length intervals skipped; the layout of times, obs_dev and
+ * values_host is pi_solve_dynamics's. */
+int pi_solve_dynamics_rk4(pi_plan* plan, double* rho_dev, int nt, const double* times,
+                          int nobs, const double* obs_dev, double* values_host,
+                          const pi_rk4_opts_t* opts, pi_rk4_info_t* info);
+
 /* ---- batched solves over many plans (parameter scans, mixed particle numbers) --------
  * One engine advances every instance together: each Arnoldi step of all instances is one
  * launch per kernel over an (instance, sector-tile) or (instance, element-chunk) work list,

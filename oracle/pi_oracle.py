@@ -995,3 +995,60 @@ def solve_dynamics_expv(plan: Plan, rho0, tspan, saveat=None, observables=None,
             states.append(current.copy())
     return dict(t=ts, states=states, values={k: np.array(v) for k, v in values.items()},
                 infos=infos)
+
+
+# --------------------------------------------------------------------------------------
+# Fixed-step RK4: evolution.jl (evolve!) and the default solve_dynamics algorithm
+# --------------------------------------------------------------------------------------
+
+
+def evolve_rk4(A, src, tspan, steps=256):
+    """evolve!(dest, L, src, tspan; steps) (evolution.jl:75-118).
+
+    Three scratch vectors k1, k2 (the stage sum) and tmp; per step
+    k1 = L dest; k2 = k1; tmp = dest + (h/2) k1; k1 = L tmp; k2 += 2 k1;
+    tmp = dest + (h/2) k1; k1 = L tmp; k2 += 2 k1; tmp = dest + h k1; k1 = L tmp;
+    k2 += k1; dest += (h/6) k2, with h = (t1 - t0) / steps.
+    """
+    if steps <= 0:
+        raise ValueError("steps must be positive")
+    t0, t1 = float(tspan[0]), float(tspan[1])
+    h = (t1 - t0) / steps
+    dest = np.array(src, dtype=np.complex128)
+    for _ in range(steps):
+        k1 = A(dest)
+        k2 = k1.copy()
+        tmp = dest + (h / 2) * k1
+        k1 = A(tmp)
+        k2 = k2 + 2 * k1
+        tmp = dest + (h / 2) * k1
+        k1 = A(tmp)
+        k2 = k2 + 2 * k1
+        tmp = dest + h * k1
+        k1 = A(tmp)
+        k2 = k2 + k1
+        dest = dest + (h / 6) * k2
+    return dest
+
+
+def solve_dynamics_rk4(plan: Plan, rho0, tspan, saveat=None, observables=None,
+                       steps_per_interval=64, save_states=True):
+    """solve_dynamics(...; algorithm=:auto) on a matrix-free source: RK4 per saved interval
+    with `steps_per_interval` steps, skipping zero-length intervals (highlevel.jl:559-566,
+    623-631, 693-712; the :auto choice is highlevel.jl:1482-1523)."""
+    if steps_per_interval <= 0:
+        raise ValueError("steps_per_interval must be positive")
+    ts = saved_times(tspan, saveat)
+    current = np.array(rho0, dtype=np.complex128)
+    A = lambda z: apply(plan, z)
+    obs = observables or {}
+    values = {k: [expectation(o, current)] for k, o in obs.items()}
+    states = [current.copy()] if save_states else None
+    for i in range(1, len(ts)):
+        if ts[i] != ts[i - 1]:
+            current = evolve_rk4(A, current, (ts[i - 1], ts[i]), steps=steps_per_interval)
+        for k, o in obs.items():
+            values[k].append(expectation(o, current))
+        if save_states:
+            states.append(current.copy())
+    return dict(t=ts, states=states, values={k: np.array(v) for k, v in values.items()})

@@ -110,16 +110,25 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// One 32 x 32 output tile of y = scale * (L x) (+ alpha * v on the diagonal) for the sector
+// Output sink of the tile loop that stores (L x)[e] into y[e].
+template <typename T2>
+struct StoreSink {
+  T2* __restrict__ y;
+  __device__ __forceinline__ void operator()(long long e, T2 v) const { y[e] = v; }
+};
+
+// One 32 x 32 output tile of scale * (L x) (+ alpha * v on the diagonal) for the sector
 // block `tile`: stage the source windows and the sector's grouped terms in shared memory,
-// then evaluate every stencil term.  `alpha` is the device trace value of this column (or
-// nullptr).  Shared by the single-plan and the multi-instance kernels.
-template <typename T>
-__device__ __forceinline__ void apply_tile(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
-                                           const typename Vec2<T>::type* __restrict__ coef, const DevTile tile,
-                                           const typename Vec2<T>::type* __restrict__ x,
-                                           typename Vec2<T>::type* __restrict__ y, const BorderArgs& border,
-                                           const double2* alpha, typename Vec2<T>::type* win, int4* st, int* ge) {
+// then evaluate every stencil term and hand each output entry, with its element index, to
+// `sink` (a plain store, or a fused epilogue such as an RK4 stage update).  `alpha` is the
+// device trace value of this column (or nullptr).  Shared by the single-plan and the
+// multi-instance kernels.
+template <typename T, typename Sink>
+__device__ __forceinline__ void apply_tile_to(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
+                                              const typename Vec2<T>::type* __restrict__ coef, const DevTile tile,
+                                              const typename Vec2<T>::type* __restrict__ x, const Sink& sink,
+                                              const BorderArgs& border, const double2* alpha,
+                                              typename Vec2<T>::type* win, int4* st, int* ge) {
   using T2 = typename Vec2<T>::type;
   const DevSector& sec = sectors[tile.sector];
   const int tb = sec.term_begin;
@@ -130,7 +139,10 @@ __device__ __forceinline__ void apply_tile(const DevSector* __restrict__ sectors
   const int warp = threadIdx.x >> 5;
   // Stage the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every
   // source sector (e = -1, 0, +1): lane = window row (plus rows 32..35 on lanes 0..3),
-  // warps stride over the 36 window columns.
+  // warps stride over the 36 window columns.  Every element is one asynchronous copy with
+  // hardware zero fill (cp.async), so all of a thread's ~30 copies are in flight at once
+  // and the block waits for memory once, not once per window column.
+  const bool extra = la < kWinRows - 32;
 #pragma unroll 1
   for (int slot = 0; slot < 3; ++slot) {
     const int s2 = sec.src[slot];
@@ -140,18 +152,18 @@ __device__ __forceinline__ void apply_tile(const DevSector* __restrict__ sectors
     const int r0 = tile.a0 + slot - 1 - kHalo, c0 = tile.b0 + slot - 1 - kHalo;
     T2* w = win + slot * kWinElems;
     const int R = r0 + la, R2 = r0 + 32 + la;
-    const bool rv = (unsigned)R < (unsigned)m, rv2 = la < kWinRows - 32 && (unsigned)R2 < (unsigned)m;
+    const bool rv = (unsigned)R < (unsigned)m, rv2 = extra && (unsigned)R2 < (unsigned)m;
+#pragma unroll
     for (int j = warp; j < kWinCols; j += kApplyWarps) {
       const int C = c0 + j;
       const bool cv = (unsigned)C < (unsigned)m;
-      T2 v, v2;
-      v.x = v.y = v2.x = v2.y = 0;
-      if (rv && cv) v = __ldg(xs + R + C * m);
-      if (rv2 && cv) v2 = __ldg(xs + R2 + C * m);
-      w[la + j * kWinRows] = v;
-      if (la < kWinRows - 32) w[32 + la + j * kWinRows] = v2;
+      const bool v1 = rv && cv, v2 = rv2 && cv;
+      cp_async_zfill<sizeof(T2)>(w + la + j * kWinRows, v1 ? xs + R + (long long)C * m : x, v1);
+      if (extra) cp_async_zfill<sizeof(T2)>(w + 32 + la + j * kWinRows, v2 ? xs + R2 + (long long)C * m : x, v2);
     }
   }
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
   const int n = sec.n;
   const int lb = warp * kColsPerThread;
@@ -182,7 +194,7 @@ __device__ __forceinline__ void apply_tile(const DevSector* __restrict__ sectors
       acc.im[k] *= scale;
     }
   }
-  T2* yp = y + sec.offset + a + (long long)b0 * n;
+  const long long e0 = sec.offset + a + (long long)b0 * n;
 #pragma unroll
   for (int k = 0; k < kColsPerThread; ++k) {
     if (k >= ncol) break;
@@ -195,8 +207,17 @@ __device__ __forceinline__ void apply_tile(const DevSector* __restrict__ sectors
       out.x += (T)(al.x * v);
       out.y += (T)(al.y * v);
     }
-    yp[(long long)k * n] = out;
+    sink(e0 + (long long)k * n, out);
   }
+}
+
+template <typename T>
+__device__ __forceinline__ void apply_tile(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
+                                           const typename Vec2<T>::type* __restrict__ coef, const DevTile tile,
+                                           const typename Vec2<T>::type* __restrict__ x,
+                                           typename Vec2<T>::type* __restrict__ y, const BorderArgs& border,
+                                           const double2* alpha, typename Vec2<T>::type* win, int4* st, int* ge) {
+  apply_tile_to<T>(sectors, terms, coef, tile, x, StoreSink<typename Vec2<T>::type>{y}, border, alpha, win, st, ge);
 }
 
 }  // namespace picuda

@@ -8,9 +8,9 @@ from ._lib import (PI_FP32, PI_FP64, PiArgumentError, PiDimensionMismatch, PiErr
                    load as load_library)
 from .backend import (AcceleratorCapability, CompiledPIModel, DynamicsResult, DynamicsStreamResult,
                       ExpvAlgorithm, GMRESAlgorithm, SteadyStateResult, accelerator_capability, apply_, apply_element_major_,
-                      compile, krylov_expv, krylov_expv_batch, mul, saved_times, solve_dynamics,
+                      compile, evolve_, krylov_expv, krylov_expv_batch, mul, saved_times, solve_dynamics,
                       solve_dynamics_batch, stationary_state, stationary_state_batch, steady_state,
-                      stencil_tables)
+                      stencil_tables, time_evolve)
 from .serving import Completion, Server
 from .core import (CollectiveHamiltonian, CollectiveJump, LocalHamiltonian, LocalJump, Models, PIBasis,
                    PIModel, PIOperator, PIState, Term, collective_operator, collective_spin,

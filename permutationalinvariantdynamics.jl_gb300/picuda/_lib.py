@@ -90,6 +90,15 @@ class pi_expv_info_t(C.Structure):
                 ("trial_evaluations", C.c_int), ("estimated_error", C.c_double)]
 
 
+class pi_rk4_opts_t(C.Structure):
+    _fields_ = [("steps_per_interval", C.c_int), ("precision", C.c_int)]
+
+
+class pi_rk4_info_t(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("operator_applications", C.c_longlong),
+                ("reached_time", C.c_double)]
+
+
 class pi_dynamics_job_t(C.Structure):
     _fields_ = [("plan", C.c_void_p), ("state_dev", C.c_void_p), ("nt", C.c_int),
                 ("times", C.POINTER(C.c_double)), ("nobs", C.c_int), ("obs_dev", C.c_void_p),
@@ -163,6 +172,11 @@ PROTOTYPES = {
                           C.POINTER(pi_expv_info_t)]),
     "pi_solve_dynamics": (C.c_int, [_P, _P, C.c_int, _D, C.c_int, _P, _D,
                                     C.POINTER(pi_expv_opts_t), C.POINTER(pi_expv_info_t)]),
+    "pi_rk4_default_opts": (None, [C.POINTER(pi_rk4_opts_t)]),
+    "pi_evolve": (C.c_int, [_P, _P, _P, C.c_double, C.c_double, C.POINTER(pi_rk4_opts_t),
+                            C.POINTER(pi_rk4_info_t)]),
+    "pi_solve_dynamics_rk4": (C.c_int, [_P, _P, C.c_int, _D, C.c_int, _P, _D,
+                                        C.POINTER(pi_rk4_opts_t), C.POINTER(pi_rk4_info_t)]),
     "pi_expv_batch": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P), _D,
                                 C.POINTER(pi_expv_opts_t), C.POINTER(pi_expv_info_t)]),
     "pi_dynamics_batch": (C.c_int, [C.c_int, C.POINTER(pi_dynamics_job_t),

@@ -478,19 +478,93 @@ def _observable_data(basis, obs):
     raise PiDimensionMismatch("observable must be a PIOperator, a local d x d matrix or a PI vector")
 
 
-def solve_dynamics(x, rho0: PIState, tspan, algorithm="expv", saveat=None, observables=None,
-                   save_states=True, parameters=None):
-    """solve_dynamics(x, rho0, tspan; algorithm=:expv | ExpvAlgorithm(...)) (highlevel.jl:559-733)."""
-    torch = _torch()
-    if parameters is not None:
-        raise PiArgumentError("Krylov exponential dynamics requires parameters=nothing")
+_DYNAMICS_ALGORITHM_NAMES = ("auto", "rk4", "expv", "krylov_expv", "adaptive_or_rk4", "dynamics")
+
+
+def _dynamics_algorithm(algorithm):
+    """(name, ExpvAlgorithm or None) for a dynamics algorithm: symbols canonicalised as in
+    solver_algorithms.jl:38-44 and highlevel.jl:285-298; :auto selects RK4 for a matrix-free
+    source (highlevel.jl:1482-1523)."""
+    if isinstance(algorithm, ExpvAlgorithm):
+        return "expv", algorithm
     if isinstance(algorithm, str):
-        if algorithm in ("expv", "krylov_expv"):
-            algorithm = ExpvAlgorithm()
-        else:
-            raise PiArgumentError("the CUDA backend propagates with algorithm=:expv (ExpvAlgorithm)")
-    if not isinstance(algorithm, ExpvAlgorithm):
-        raise PiArgumentError("algorithm must be :expv or an ExpvAlgorithm")
+        name = {"adaptive_or_rk4": "rk4", "dynamics": "rk4", "krylov_expv": "expv"}.get(algorithm, algorithm)
+        if name not in ("auto", "rk4", "expv"):
+            raise PiArgumentError(f"unsupported dynamics algorithm {algorithm}; choose one of "
+                                  f"{_DYNAMICS_ALGORITHM_NAMES}")
+        if name == "auto":
+            name = "rk4"
+        return name, (ExpvAlgorithm() if name == "expv" else None)
+    raise PiArgumentError("unsupported dynamics algorithm; use a dynamics algorithm name or ExpvAlgorithm()")
+
+
+def _rk4_opts(steps, precision):
+    if int(steps) <= 0:
+        raise PiArgumentError("steps must be positive")
+    if precision not in ("fp64", "mixed"):
+        raise PiArgumentError("precision must be 'fp64' or 'mixed'")
+    return _lib.pi_rk4_opts_t(int(steps), _lib.PI_FP32 if precision == "mixed" else _lib.PI_FP64)
+
+
+def evolve_(dest, x, src, tspan, steps=256, precision="fp64"):
+    """evolve!(dest, L, src, tspan; steps=256) (evolution.jl:75-118): fixed-step RK4 of
+    h = (t1 - t0) / steps on the GPU.
+
+    dest, src: complex128 CUDA tensors of length dim (device-resident; dest may be src but
+    must not partially overlap it) or PIStates (host data, copied in and out).
+    precision="mixed" applies the operator in FP32 population coordinates with an FP64 state
+    and stage sum.  Returns dest.
+    """
+    torch = _torch()
+    compiled = _as_compiled(x)
+    n = len(compiled.basis)
+    t0, t1 = float(tspan[0]), float(tspan[1])
+    o = _rk4_opts(steps, precision)
+    info = _lib.pi_rk4_info_t()
+    lib = _lib.load()
+    if isinstance(dest, PIState) or isinstance(src, PIState):
+        if not (isinstance(dest, PIState) and isinstance(src, PIState)):
+            raise PiArgumentError("dest and src must both be PIStates or both device tensors")
+        if dest.basis.N != compiled.basis.N or src.basis.N != compiled.basis.N:
+            raise PiArgumentError("source and destination use incompatible PI bases")
+        xd = torch.from_numpy(np.ascontiguousarray(src.data, dtype=np.complex128)).cuda()
+        torch.cuda.synchronize()
+        _lib.check(lib.pi_evolve(compiled.handle, _ptr(xd), _ptr(xd), t0, t1, C.byref(o), C.byref(info)), "evolve!")
+        dest.data[...] = xd.cpu().numpy()
+        return dest
+    if dest.shape != (n,) or src.shape != (n,) or not dest.is_cuda or not src.is_cuda:
+        raise PiDimensionMismatch("source and destination dimensions differ from the Liouvillian's")
+    if dest.dtype != torch.complex128 or src.dtype != torch.complex128:
+        raise PiArgumentError("evolve! needs complex128 device vectors")
+    if not (dest.is_contiguous() and src.is_contiguous()):
+        raise PiArgumentError("device vectors must be contiguous")
+    torch.cuda.synchronize()
+    _lib.check(lib.pi_evolve(compiled.handle, _ptr(dest), _ptr(src), t0, t1, C.byref(o), C.byref(info)), "evolve!")
+    return dest
+
+
+def time_evolve(x, rho: PIState, tspan, steps=256, precision="fp64"):
+    """time_evolve(L, rho, tspan; steps) (evolution.jl:131-134): a new PIState, rho unchanged."""
+    out = PIState(rho.basis, np.array(rho.data, dtype=np.complex128))
+    return evolve_(out, x, PIState(rho.basis, rho.data), tspan, steps=steps, precision=precision)
+
+
+def solve_dynamics(x, rho0: PIState, tspan, algorithm="auto", saveat=None, observables=None,
+                   save_states=True, parameters=None, steps_per_interval=64, precision="fp64"):
+    """solve_dynamics(x, rho0, tspan; algorithm=:auto, saveat, steps_per_interval=64,
+    observables, save_states) (highlevel.jl:559-733).
+
+    algorithm :auto / :rk4 (the reference's default: fixed-step RK4 with steps_per_interval
+    steps per saved interval) or :expv / ExpvAlgorithm(...) (adaptive Krylov exponential).
+    precision="mixed" selects FP32 applies with an FP64 state for RK4 (ExpvAlgorithm carries
+    its own precision).
+    """
+    torch = _torch()
+    if int(steps_per_interval) <= 0:
+        raise PiArgumentError("steps_per_interval must be positive")
+    name, algorithm = _dynamics_algorithm(algorithm)
+    if parameters is not None:
+        raise PiArgumentError("the CUDA plan is one autonomous generator: parameters must be nothing")
     compiled = _as_compiled(x)
     if rho0.basis.N != compiled.basis.N or rho0.basis.sectors != compiled.basis.sectors:
         raise PiArgumentError("Liouvillian source and initial state use incompatible PI bases")
@@ -498,7 +572,6 @@ def solve_dynamics(x, rho0: PIState, tspan, algorithm="expv", saveat=None, obser
         raise PiArgumentError("save_states=false requires at least one observable")
     ts = saved_times(tspan, saveat)
     lib = _lib.load()
-    n = len(compiled.basis)
     xd = torch.from_numpy(np.ascontiguousarray(rho0.data)).cuda()
     names = []
     obs_dev = None
@@ -511,17 +584,22 @@ def solve_dynamics(x, rho0: PIState, tspan, algorithm="expv", saveat=None, obser
             datas.append(_observable_data(compiled.basis, v))
         obs_dev = torch.from_numpy(np.ascontiguousarray(np.stack(datas))).cuda()
     nobs = len(names)
-    o = algorithm.opts()
-    info = _lib.pi_expv_info_t()
+    if name == "rk4":
+        o = _rk4_opts(steps_per_interval, precision)
+        info = _lib.pi_rk4_info_t()
+    else:
+        o = algorithm.opts()
+        info = _lib.pi_expv_info_t()
     torch.cuda.synchronize()
     if not save_states:
         times = np.array(ts, dtype=np.float64)
         vals = np.zeros((len(ts), max(nobs, 1), 2), dtype=np.float64)
-        _lib.check(lib.pi_solve_dynamics(compiled.handle, _ptr(xd), len(ts), _lib.dptr(times), nobs,
-                                         _ptr(obs_dev) if obs_dev is not None else None, _lib.dptr(vals),
-                                         C.byref(o), C.byref(info)), "solve_dynamics")
+        fn = lib.pi_solve_dynamics_rk4 if name == "rk4" else lib.pi_solve_dynamics
+        _lib.check(fn(compiled.handle, _ptr(xd), len(ts), _lib.dptr(times), nobs,
+                      _ptr(obs_dev) if obs_dev is not None else None, _lib.dptr(vals), C.byref(o), C.byref(info)),
+                   "solve_dynamics")
         values = {k: vals[:, i, 0] + 1j * vals[:, i, 1] for i, k in enumerate(names)}
-        return DynamicsStreamResult(ts, None, values)
+        return DynamicsStreamResult(ts, None, values, algorithm=name)
     states = [rho0.copy()]
     series = {k: [] for k in names}
 
@@ -538,12 +616,16 @@ def solve_dynamics(x, rho0: PIState, tspan, algorithm="expv", saveat=None, obser
         dt = ts[i] - ts[i - 1]
         if dt != 0:
             torch.cuda.synchronize()
-            _lib.check(lib.pi_expv(compiled.handle, _ptr(xd), dt, C.byref(o), C.byref(info)), "solve_dynamics")
+            if name == "rk4":
+                _lib.check(lib.pi_evolve(compiled.handle, _ptr(xd), _ptr(xd), ts[i - 1], ts[i], C.byref(o),
+                                         C.byref(info)), "solve_dynamics")
+            else:
+                _lib.check(lib.pi_expv(compiled.handle, _ptr(xd), dt, C.byref(o), C.byref(info)), "solve_dynamics")
         states.append(PIState(compiled.basis, xd.cpu().numpy()))
         record(xd)
     if nobs:
-        return DynamicsStreamResult(ts, states, {k: np.array(v) for k, v in series.items()})
-    return DynamicsResult(ts, states)
+        return DynamicsStreamResult(ts, states, {k: np.array(v) for k, v in series.items()}, algorithm=name)
+    return DynamicsResult(ts, states, algorithm=name)
 
 
 # ---------------------------------------------------------------------------------------

@@ -87,7 +87,7 @@ def test_dynamics_batch_matches_single_solve_dynamics(torch_cuda):
     obs = {"exc": EXC, "jz": JZ}
     results, finals = picuda.solve_dynamics_batch(models, rho0s, (0.0, 1.0), saveat=0.1, observables=obs)
     for m, r0, res, fin in zip(models, rho0s, results, finals):
-        ref = picuda.solve_dynamics(m, r0, (0.0, 1.0), saveat=0.1, save_states=False, observables=obs)
+        ref = picuda.solve_dynamics(m, r0, (0.0, 1.0), algorithm="expv", saveat=0.1, save_states=False, observables=obs)
         assert res.t == ref.t
         for k in obs:
             assert np.abs(res.values[k] - ref.values[k]).max() <= 1e-10 * max(np.abs(ref.values[k]).max(), 1.0)
@@ -102,7 +102,7 @@ def test_dynamics_batch_zero_length_intervals(torch_cuda):
                                            observables={"exc": np.array([[0, 0], [0, 1]])})
     v = res[0].values["exc"]
     assert v[0] == v[1] and v[2] == v[3]
-    ref = picuda.solve_dynamics(m, rho0, (0.0, 0.4), saveat=[0.0, 0.0, 0.2, 0.2, 0.4], save_states=False,
+    ref = picuda.solve_dynamics(m, rho0, (0.0, 0.4), algorithm="expv", saveat=[0.0, 0.0, 0.2, 0.2, 0.4], save_states=False,
                                 observables={"exc": np.array([[0, 0], [0, 1]])})
     assert np.abs(v - ref.values["exc"]).max() <= 1e-10 * np.abs(ref.values["exc"]).max()
 

@@ -44,7 +44,7 @@ def test_server_dynamics_and_steady_match_direct_calls(torch_cuda):
         assert c.finish_time >= c.start_time >= c.submit_time
         if kind == "d":
             m = dyn[i]
-            ref = picuda.solve_dynamics(m, _excited(m), (0.0, 0.4 + 0.1 * i), saveat=0.05, save_states=False,
+            ref = picuda.solve_dynamics(m, _excited(m), (0.0, 0.4 + 0.1 * i), algorithm="expv", saveat=0.05, save_states=False,
                                         observables={"exc": EXC})
             assert c.times == ref.t
             assert np.abs(c.values["exc"] - ref.values["exc"]).max() <= 1e-10 * np.abs(ref.values["exc"]).max()

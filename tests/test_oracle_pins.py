@@ -270,3 +270,40 @@ def test_threaded_c_baseline_matches_numpy_oracle():
         ref = O.apply(plan, x)
         for threads in (1, 3):
             assert np.abs(ta(x, threads=threads) - ref).max() <= 1e-13 * np.abs(ref).max()
+
+
+def test_rk4_restatement_matches_exponential():
+    """test/test_evolution.jl:1-20: RK4 with 400 steps equals exp(tL) rho to 2e-12 for
+    N=2 local decay, and chained evolutions (0,t) then (t,2t) equal exp(2tL) rho to 3e-12."""
+    b = O.PIBasis(2, 2)
+    plan = O.Plan(O.qubit_ensemble_model(b, emission=1.0))
+    L = O.materialize(plan)
+    rho = O.iid_pure_state(b, np.array([0.0, 1.0], dtype=np.complex128))
+    t = 0.7
+    A = lambda v: O.apply(plan, v)
+    out = O.evolve_rk4(A, rho, (0.0, t), steps=400)
+    assert np.allclose(out, sla.expm(t * L) @ rho, atol=2e-12, rtol=0)
+    assert abs(O.trace(plan, out) - 1) <= 2e-12
+    out2 = O.evolve_rk4(A, out, (t, 2 * t), steps=400)
+    assert np.allclose(out2, sla.expm(2 * t * L) @ rho, atol=3e-12, rtol=0)
+    with pytest.raises(ValueError):
+        O.evolve_rk4(A, rho, (0.0, t), steps=0)
+
+
+def test_rk4_dynamics_grid_and_expv_agreement():
+    """test/test_highlevel.jl:33-60: saveat 0.05 with 40 steps per interval equals one
+    160-step evolution to 2e-11; expv at tight tolerance agrees to 2e-9; repeated saved
+    times give identical states."""
+    b = O.PIBasis(3, 2)
+    plan = O.Plan(O.qubit_ensemble_model(b, emission=0.4))
+    rho0 = O.iid_pure_state(b, np.array([0.0, 1.0], dtype=np.complex128))
+    sol = O.solve_dynamics_rk4(plan, rho0, (0.0, 0.2), saveat=0.05, steps_per_interval=40)
+    assert len(sol["t"]) == 5
+    one = O.evolve_rk4(lambda v: O.apply(plan, v), rho0, (0.0, 0.2), steps=160)
+    assert np.allclose(sol["states"][-1], one, atol=2e-11, rtol=0)
+    ex = O.solve_dynamics_expv(plan, rho0, (0.0, 0.2), saveat=sol["t"], krylovdim=12, atol=1e-12,
+                               rtol=1e-10)
+    for a, c in zip(sol["states"], ex["states"]):
+        assert np.allclose(a, c, atol=2e-9, rtol=0)
+    rep = O.solve_dynamics_rk4(plan, rho0, (0.0, 0.2), saveat=[0.0, 0.1, 0.1, 0.2])
+    assert np.array_equal(rep["states"][1], rep["states"][2])
