@@ -175,7 +175,7 @@ __device__ __forceinline__ void rmacq(Pack<Q>& acc, const float c, const Pack<Q>
 }
 
 template <bool PLUS, int Q>
-__global__ void __launch_bounds__(32 * kEmWarps)
+__global__ void __launch_bounds__(32 * kEmWarps, 4)
     k_apply_em_f32(const DevSector* __restrict__ sectors, const DevTile* __restrict__ tiles,
                    const float2* __restrict__ planes, const float4* __restrict__ x, float4* __restrict__ y,
                    unsigned ld4, int npairs, BorderArgs border) {
