@@ -12,8 +12,8 @@
 //     (-1,-1) diagonal; neighbouring sectors: two diagonal shifts each, three with pumping).
 //     Terms at one position are merged into one complex coefficient per output entry,
 //     precomputed once per plan into a coefficient plane [dim][kEmPos] (about 80 bytes per
-//     entry against 16 bytes per entry and right-hand side of x and y); the coefficients
-//     are warp-uniform loads;
+//     entry against 16 bytes per entry and right-hand side of x and y); a warp copies the
+//     coefficients of all its rows to shared memory once (cp.async) and reads them there;
 //   - the own-sector sources of rows a-1, a, a+1 and columns b-1, b, b+1 stay in registers
 //     as a sliding window, so each output row costs three new own-sector loads plus two per
 //     neighbouring sector.
@@ -233,15 +233,26 @@ __global__ void __launch_bounds__(32 * kEmWarps, 4)
     sl[d] = make_stream(ld4, off2, m2, a0 + d, b + d, qq);
   }
   constexpr int NX = PLUS ? 3 : 2;  // cross-sector streams per neighbour
-  const float4* planes4 = reinterpret_cast<const float4*>(planes);
-  unsigned ci = (unsigned)(own + a0 + b * n) * (NP / 2);
+  // The warp's merged coefficients for all its rows (contiguous in the planes: rows a0..
+  // a_end-1 of column b) go to shared memory with one round of asynchronous copies, so no
+  // row waits on a coefficient load from memory (the planes are read once per launch and
+  // miss in L2; loaded row by row they put a full memory latency into every iteration).
+  __shared__ __align__(16) float4 coef_sm[kEmWarps][kEmRows * (NP / 2)];
+  float4* cw = coef_sm[threadIdx.x >> 5];
+  {
+    const float4* src = reinterpret_cast<const float4*>(planes) + (size_t)(unsigned)(own + a0 + b * n) * (NP / 2);
+    const int cnt = (a_end - a0) * (NP / 2);
+    for (int i = lane; i < cnt; i += 32) cp_async_zfill<16>(cw + i, src + i, true);
+    cp_async_commit();
+  }
   unsigned yi = (unsigned)(own + a0 + b * n) * ld4 + (unsigned)qq;
+  cp_async_wait<0>();
+  __syncwarp();
   for (int a = a0; a < a_end; ++a) {
     // coefficient pairs: cv[k] = (c_{2k}, c_{2k+1}), used component-wise
     float4 cv[NP / 2];
 #pragma unroll
-    for (int k = 0; k < NP / 2; ++k) cv[k] = __ldg(planes4 + ci + k);
-    ci += NP / 2;
+    for (int k = 0; k < NP / 2; ++k) cv[k] = cw[(a - a0) * (NP / 2) + k];
     Pack<Q> acc;
 #pragma unroll
     for (int i = 0; i < Q; ++i) acc.v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -369,9 +380,11 @@ extern "C" int pi_apply_f32_em(pi_plan* plan, float* y_dev, const float* x_dev, 
   const int npairs = ncols / 2;
   BorderArgs border{1.0, nullptr, coords};
   cudaStream_t s = (cudaStream_t)stream;
-  // One right-hand-side pair per lane and 8-warp blocks: measured fastest on GB300 for
-  // 64..256-column batches (two pairs per lane or a one-row prefetch raise the register
-  // count past 64 and cost more in occupancy than they save in loads).
+  // One right-hand-side pair per lane, 8-warp blocks, 64 registers (4 blocks per SM):
+  // measured fastest on GB300 for 64..256-column batches.  Two pairs per lane, one pair per
+  // lane with 8-byte loads, wider blocks, L2 bulk prefetch and source loads pipelined a row
+  // ahead were all slower (the last raises the register count past 64 and costs more in
+  // occupancy than it saves in latency).
   dim3 grid((unsigned)plan->em_ntiles, (unsigned)((npairs + 31) / 32));
   const float4* x4 = (const float4*)x_dev;
   float4* y4 = (float4*)y_dev;
