@@ -11,6 +11,8 @@ from .backend import (AcceleratorCapability, CompiledPIModel, DynamicsResult, Dy
                       compile, evolve_, krylov_expv, krylov_expv_batch, mul, saved_times, solve_dynamics,
                       solve_dynamics_batch, stationary_state, stationary_state_batch, steady_state,
                       stencil_tables, time_evolve)
+from .scans import (CompiledPIModelFamily, ParameterScanPlan, ParameterScanPoint, ParameterScanResult,
+                    compile_family, parameter_scan, specialize)
 from .serving import Completion, Server
 from .core import (CollectiveHamiltonian, CollectiveJump, LocalHamiltonian, LocalJump, Models, PIBasis,
                    PIModel, PIOperator, PIState, Term, collective_operator, collective_spin,
