@@ -83,6 +83,13 @@ int pi_plan_create(int N, int d, int nsectors, const int* sector_ks, int nterms,
                    const double* hbar, pi_plan** out);
 int pi_plan_destroy(pi_plan* plan);
 
+/* The adjoint generator as a plan of its own: the conjugate transpose of the PI-coordinate
+ * matrix, the operator of apply_adjoint! (liouvillian.jl:3107-3143, 3275-3324,
+ * 4190-4266).  Built on the host from plan's lowered stencil (every term transposed:
+ * sectors swapped, offsets negated, coefficients conjugated and shifted), so every apply
+ * and solver entry point runs it; destroy it with pi_plan_destroy. */
+int pi_plan_adjoint(const pi_plan* plan, pi_plan** out);
+
 typedef struct {
   int N;
   int nsectors;
@@ -120,6 +127,12 @@ int pi_plan_sector_scales(const pi_plan* plan, double* sqrt_f);
 int pi_stencil_export(int N, int d, int nsectors, const int* sector_ks, int nterms,
                       const int* term_kind, const double* ops, const double* rates,
                       const double* hbar, long long* counts, int* term_table, double* coef);
+
+/* The same export for the adjoint plan (pi_plan_adjoint). */
+int pi_stencil_export_adjoint(int N, int d, int nsectors, const int* sector_ks, int nterms,
+                              const int* term_kind, const double* ops, const double* rates,
+                              const double* hbar, long long* counts, int* term_table,
+                              double* coef);
 
 /* Dense block of the collective operator sum_i X_i in sector (N-k, k), column-major
  * interleaved complex n x n (geometry.jl:1238-1256); op is 2x2 column-major interleaved. */
@@ -172,6 +185,31 @@ int pi_dot_f64(pi_plan* plan, const double* a_dev, const double* b_dev, double* 
  * race.  Asynchronous on `stream` (NULL = default stream). */
 int pi_mdot_f64_noalloc(const double* V_dev, long long ldv, int nv, const double* w_dev, long long n,
                         double* h_dev, void* stream);
+
+/* ---- Arnoldi factorisation for Liouvillian spectra (krylov.jl:914-962) -------------
+ * krylov_liouvillian_spectrum's Krylov process on the device: V[:,0] = v0/|v0|, then for
+ * j = 0..m-1: w = L V[:,j]; two Gram-Schmidt passes against V[:,0..j] (their sum is column
+ * j of H); H[j+1,j] = |w|; stop after step m or when H[j+1,j] <= eps * |L V[:,j]| (the
+ * reference's breakdown test); else V[:,j+1] = w / H[j+1,j].  The k x k Hessenberg
+ * eigenproblem, Ritz ordering and residual estimates stay with the caller, as the
+ * reference hands them to its LAPACK (_projected_eigen, krylov.jl:31-40).  FP64. */
+typedef struct {
+  int steps;          /* k: Arnoldi steps taken (columns of H filled) */
+  int breakdown;      /* 1 when the breakdown test stopped the process before step m */
+  int operator_applications;
+} pi_arnoldi_info_t;
+
+/* v0_dev: dim complex (not modified); V_dev: (m+1) columns of dim complex at leading
+ * dimension ldv >= dim, written; H_host: (m+1) x m complex column-major, zero-filled
+ * then written.  1 <= m <= 127. */
+int pi_arnoldi(pi_plan* plan, const double* v0_dev, int m, double* V_dev, long long ldv,
+               double* H_host, pi_arnoldi_info_t* info);
+
+/* out[:, c] = sum_i coef[i + c*k] V[:, i] for c < ncols: Ritz vectors from an Arnoldi basis
+ * (V: k columns of dim complex at ldv; coef: k x ncols complex column-major on the host;
+ * out: ncols columns at ldo, device).  FP64. */
+int pi_combine_f64(pi_plan* plan, const double* V_dev, long long ldv, int k, const double* coef_host,
+                   int ncols, double* out_dev, long long ldo);
 
 /* ---- steady state: krylov_steady_state (krylov.jl:797-891) -------------------------- */
 

@@ -1052,3 +1052,77 @@ def solve_dynamics_rk4(plan: Plan, rho0, tspan, saveat=None, observables=None,
         if save_states:
             states.append(current.copy())
     return dict(t=ts, states=states, values={k: np.array(v) for k, v in values.items()})
+
+
+# --------------------------------------------------------------------------------------
+# Adjoint and Arnoldi spectra: liouvillian.jl (apply_adjoint!), krylov.jl (spectrum)
+# --------------------------------------------------------------------------------------
+
+
+def adjoint_matrix(plan: Plan):
+    """The adjoint generator: conjugate transpose of the PI-coordinate matrix, the operator
+    apply_adjoint! applies (liouvillian.jl:3275-3324; duality in
+    test_liouvillian_properties.jl:145-150)."""
+    return materialize(plan).conj().T
+
+
+def ritz_order(values, which):
+    """_ritz_order (krylov.jl:893-898), stable like Julia's sortperm."""
+    if which == "LR":
+        return np.argsort(-values.real, kind="stable")
+    if which == "LM":
+        return np.argsort(-np.abs(values), kind="stable")
+    if which == "SM":
+        return np.argsort(np.abs(values), kind="stable")
+    raise ValueError("which must be :LR, :LM, or :SM")
+
+
+def krylov_liouvillian_spectrum(A, n, nev=6, krylovdim=None, which="LR", initial_vector=None, atol=1e-10,
+                                rtol=1e-8, vectors=False, rng=None, require_convergence=True):
+    """krylov_liouvillian_spectrum (krylov.jl:914-962): m-step Arnoldi with two modified
+    Gram-Schmidt passes per step, breakdown test |H[j+1,j]| <= eps max(|L v_j|, tiny), Ritz
+    values of H[1:k,1:k], residuals |H[k+1,k] y_k|, tolerance atol + rtol max_j |H[:,j]|."""
+    if not (0 < nev <= n):
+        raise ValueError("nev must lie between 1 and the operator dimension")
+    krylovdim = max(20, 2 * nev + 4) if krylovdim is None else krylovdim
+    m = min(n, max(krylovdim, nev + 1))
+    V = np.zeros((n, m + 1), dtype=np.complex128)
+    H = np.zeros((m + 1, m), dtype=np.complex128)
+    if initial_vector is None:
+        rng = rng if rng is not None else np.random.default_rng(0)
+        q = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+    else:
+        q = np.array(initial_vector, dtype=np.complex128)
+    nq = np.linalg.norm(q)
+    if not nq > 0:
+        raise ValueError("initial_vector must be nonzero")
+    V[:, 0] = q / nq
+    k = 0
+    eps = np.finfo(float).eps
+    for j in range(m):
+        w = A(V[:, j])
+        image_norm = np.linalg.norm(w)
+        for _ in range(2):
+            for i in range(j + 1):
+                hij = np.vdot(V[:, i], w)
+                H[i, j] += hij
+                w = w - hij * V[:, i]
+        H[j + 1, j] = np.linalg.norm(w)
+        k = j + 1
+        if j == m - 1 or abs(H[j + 1, j]) <= eps * max(image_norm, np.finfo(float).tiny):
+            break
+        V[:, j + 1] = w / H[j + 1, j]
+    vals, Y = np.linalg.eig(H[:k, :k])
+    order = ritz_order(vals, which)[:min(nev, k)]
+    vals, Y = vals[order], Y[:, order]
+    residuals = np.abs(H[k, k - 1] * Y[-1, :])
+    scale = max(max((np.linalg.norm(H[:k + 1, j]) for j in range(k)), default=0.0), np.finfo(float).tiny)
+    tol = atol + rtol * scale
+    converged = residuals <= tol
+    if require_convergence and not converged.all():
+        raise ValueError("Arnoldi spectrum did not converge")
+    out = dict(values=vals, residuals=residuals, converged=converged, iterations=k, krylov_dimension=m,
+               dimension=n, which=which, residual_scale=scale, residual_tolerance=tol)
+    if vectors:
+        out["vectors"] = V[:, :k] @ Y
+    return out

@@ -384,13 +384,9 @@ static int build_host_plan(int N, int d, int nsectors, const int* sector_ks, int
   return PI_OK;
 }
 
-int pi_stencil_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
-                      const double* ops, const double* rates, const double* hbar, long long* counts,
-                      int* term_table, double* coef) {
-  if (!counts) return fail(PI_ERR_INVALID_ARGUMENT, "null counts");
-  QubitPlan hp;
-  int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
-  if (rc) return rc;
+static QubitPlan adjoint_host_plan(const QubitPlan& hp);
+
+static int export_plan(const QubitPlan& hp, long long* counts, int* term_table, double* coef) {
   long long nt = 0, nc = 0;
   for (const auto& sec : hp.sectors)
     for (const auto& t : sec.terms) {
@@ -432,6 +428,26 @@ int pi_stencil_export(int N, int d, int nsectors, const int* sector_ks, int nter
   return PI_OK;
 }
 
+int pi_stencil_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                      const double* ops, const double* rates, const double* hbar, long long* counts,
+                      int* term_table, double* coef) {
+  if (!counts) return fail(PI_ERR_INVALID_ARGUMENT, "null counts");
+  QubitPlan hp;
+  int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
+  if (rc) return rc;
+  return export_plan(hp, counts, term_table, coef);
+}
+
+int pi_stencil_export_adjoint(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                              const double* ops, const double* rates, const double* hbar, long long* counts,
+                              int* term_table, double* coef) {
+  if (!counts) return fail(PI_ERR_INVALID_ARGUMENT, "null counts");
+  QubitPlan hp;
+  int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
+  if (rc) return rc;
+  return export_plan(adjoint_host_plan(hp), counts, term_table, coef);
+}
+
 int pi_collective_block(int N, int k, const double* op, double* out) {
   if (!op || !out) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
   if (N < 1 || k < 0 || 2 * k > N) return fail(PI_ERR_INVALID_ARGUMENT, "sector is not a two-row partition of N");
@@ -458,17 +474,9 @@ int pi_sector_multiplicity(int N, int k, double* f, double* sqrt_f) {
   return PI_OK;
 }
 
-int pi_plan_create(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
-                   const double* ops, const double* rates, const double* hbar, pi_plan** out) {
-  if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "null output handle");
-  *out = nullptr;
-  pi_plan* plan = new (std::nothrow) pi_plan();
-  if (!plan) return fail(PI_ERR_OUT_OF_MEMORY, "host allocation failed");
-  int brc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &plan->host);
-  if (brc != PI_OK) {
-    delete plan;
-    return brc;
-  }
+// Device resources and tables of a plan whose host lowering is in plan->host; takes
+// ownership of plan (freed on failure).
+static int finish_plan(pi_plan* plan, pi_plan** out) {
   if (plan->host.dim > (long long)1 << 31) {
     delete plan;
     return fail(PI_ERR_UNSUPPORTED, "PI dimension exceeds the 32-bit tile addressing of this build");
@@ -498,6 +506,70 @@ int pi_plan_create(int N, int d, int nsectors, const int* sector_ks, int nterms,
   }
   *out = plan;
   return PI_OK;
+}
+
+int pi_plan_create(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                   const double* ops, const double* rates, const double* hbar, pi_plan** out) {
+  if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "null output handle");
+  *out = nullptr;
+  pi_plan* plan = new (std::nothrow) pi_plan();
+  if (!plan) return fail(PI_ERR_OUT_OF_MEMORY, "host allocation failed");
+  int brc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &plan->host);
+  if (brc != PI_OK) {
+    delete plan;
+    return brc;
+  }
+  return finish_plan(plan, out);
+}
+
+// Conjugate transpose of a lowered plan (liouvillian.jl:3107-3143, 3275-3324: apply_adjoint!
+// is the adjoint of the PI-coordinate matrix).  A stencil term of output sector s,
+//   y_s[a, b] += c(a, b) x_r[a + e + p, b + e + q],
+// contributes to the adjoint the term of output sector r with source s
+//   y_r[a', b'] += conj(c(a' - e - p, b' - e - q)) x_s[a' - e - p, b' - e - q],
+// i.e. shift -e, offsets (-p, -q) and the coefficient arrays conjugated and shifted (zero
+// where the shifted index leaves sector s).  Kinds and coefficient classes are preserved,
+// so every kernel runs the adjoint plan unchanged.
+static QubitPlan adjoint_host_plan(const QubitPlan& hp) {
+  QubitPlan out = hp;
+  for (auto& sec : out.sectors) sec.terms.clear();
+  out.max_terms = 0;
+  for (int s = 0; s < (int)hp.sectors.size(); ++s) {
+    const int ns = hp.sectors[s].n;
+    for (const StencilTerm& t : hp.sectors[s].terms) {
+      const int r = t.src;
+      const int nr = hp.sectors[r].n;
+      auto shifted = [&](const std::vector<cd>& v, int shift) {
+        std::vector<cd> w(nr, cd(0, 0));
+        for (int i = 0; i < nr; ++i) {
+          const int src_i = i - shift;
+          if (src_i >= 0 && src_i < ns) w[i] = std::conj(v[src_i]);
+        }
+        return w;
+      };
+      StencilTerm u;
+      u.src = s;
+      u.kind = t.kind;
+      u.cls = t.cls;
+      u.e = -t.e;
+      u.p = -t.p;
+      u.q = -t.q;
+      if (t.kind != ST_RIGHT) u.alpha = shifted(t.alpha, t.e + t.p);
+      if (t.kind != ST_LEFT) u.beta = shifted(t.beta, t.e + t.q);
+      out.sectors[r].terms.push_back(std::move(u));
+    }
+  }
+  for (const auto& sec : out.sectors) out.max_terms = std::max(out.max_terms, (int)sec.terms.size());
+  return out;
+}
+
+int pi_plan_adjoint(const pi_plan* plan, pi_plan** out) {
+  if (!plan || !out) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  pi_plan* adj = new (std::nothrow) pi_plan();
+  if (!adj) return fail(PI_ERR_OUT_OF_MEMORY, "host allocation failed");
+  adj->host = adjoint_host_plan(plan->host);
+  return finish_plan(adj, out);
 }
 
 int pi_plan_destroy(pi_plan* plan) {

@@ -99,6 +99,10 @@ class pi_rk4_info_t(C.Structure):
                 ("reached_time", C.c_double)]
 
 
+class pi_arnoldi_info_t(C.Structure):
+    _fields_ = [("steps", C.c_int), ("breakdown", C.c_int), ("operator_applications", C.c_int)]
+
+
 class pi_dynamics_job_t(C.Structure):
     _fields_ = [("plan", C.c_void_p), ("state_dev", C.c_void_p), ("nt", C.c_int),
                 ("times", C.POINTER(C.c_double)), ("nobs", C.c_int), ("obs_dev", C.c_void_p),
@@ -172,6 +176,11 @@ PROTOTYPES = {
                           C.POINTER(pi_expv_info_t)]),
     "pi_solve_dynamics": (C.c_int, [_P, _P, C.c_int, _D, C.c_int, _P, _D,
                                     C.POINTER(pi_expv_opts_t), C.POINTER(pi_expv_info_t)]),
+    "pi_plan_adjoint": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
+    "pi_stencil_export_adjoint": (C.c_int, [C.c_int, C.c_int, C.c_int, _I, C.c_int, _I, _D, _D, _D, _LL,
+                                            _I, _D]),
+    "pi_arnoldi": (C.c_int, [_P, _P, C.c_int, _P, C.c_longlong, _D, C.POINTER(pi_arnoldi_info_t)]),
+    "pi_combine_f64": (C.c_int, [_P, _P, C.c_longlong, C.c_int, _D, C.c_int, _P, C.c_longlong]),
     "pi_rk4_default_opts": (None, [C.POINTER(pi_rk4_opts_t)]),
     "pi_evolve": (C.c_int, [_P, _P, _P, C.c_double, C.c_double, C.POINTER(pi_rk4_opts_t),
                             C.POINTER(pi_rk4_info_t)]),

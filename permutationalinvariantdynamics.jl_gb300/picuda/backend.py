@@ -78,18 +78,19 @@ def _term_arrays(model: PIModel):
     return kinds, np.ascontiguousarray(ops), rates, hbar, ks
 
 
-def stencil_tables(model: PIModel):
-    """Host-only export of the lowered stencil (pi_stencil_export): (terms[n,8], coef[c])."""
+def stencil_tables(model: PIModel, adjoint: bool = False):
+    """Host-only export of the lowered stencil (pi_stencil_export, or the adjoint plan's with
+    adjoint=True): (terms[n,8], coef[c])."""
     lib = _lib.load()
+    fn = lib.pi_stencil_export_adjoint if adjoint else lib.pi_stencil_export
     kinds, ops, rates, hbar, ks = _term_arrays(model)
     counts = np.zeros(2, dtype=np.int64)
     args = (model.basis.N, model.basis.d, len(ks), _lib.iptr(ks), len(model.terms), _lib.iptr(kinds),
             _lib.dptr(ops), _lib.dptr(rates), _lib.dptr(hbar), _lib.llptr(counts))
-    _lib.check(lib.pi_stencil_export(*args, None, None), "pi_stencil_export")
+    _lib.check(fn(*args, None, None), "pi_stencil_export")
     table = np.zeros((int(counts[0]), 8), dtype=np.int32)
     coef = np.zeros(int(counts[1]), dtype=np.complex128)
-    _lib.check(lib.pi_stencil_export(*args, _lib.iptr(table), _lib.dptr(coef.view(np.float64))),
-               "pi_stencil_export")
+    _lib.check(fn(*args, _lib.iptr(table), _lib.dptr(coef.view(np.float64))), "pi_stencil_export")
     return table, coef
 
 
@@ -124,6 +125,9 @@ class CompiledPIModel:
         return self._handle
 
     def close(self):
+        adj = self.__dict__.pop("_adjoint", None)
+        if adj is not None:
+            adj.close()
         if getattr(self, "_handle", None) is not None:
             _lib.load().pi_plan_destroy(self._handle)
             self._handle = None
@@ -144,6 +148,21 @@ class CompiledPIModel:
 
     def isautonomous(self):
         return True
+
+    def adjoint(self):
+        """The adjoint generator (pi_plan_adjoint), built on first use and kept with the model."""
+        adj = getattr(self, "_adjoint", None)
+        if adj is None:
+            handle = C.c_void_p()
+            _lib.check(_lib.load().pi_plan_adjoint(self.handle, C.byref(handle)), "apply_adjoint!")
+            adj = CompiledPIModel.__new__(CompiledPIModel)
+            adj.model, adj.basis, adj.backend, adj._handle = self.model, self.basis, "cuda", handle
+            info = _lib.pi_plan_info_t()
+            _lib.check(_lib.load().pi_plan_info(handle, C.byref(info)), "pi_plan_info")
+            adj.info = {f: getattr(info, f) for f, _ in info._fields_}
+            adj._primary = self  # keeps the forward plan alive while the adjoint is in use
+            self._adjoint = adj
+        return adj
 
     # -- basis maps straight from the library (bit-exact) --------------------------------
     def library_sectors(self):
@@ -239,6 +258,73 @@ def apply_(y, compiled: CompiledPIModel, x, t=0.0, p=None, precision="fp64", coo
     else:
         raise PiArgumentError("precision must be 'fp64' or 'fp32'")
     return y
+
+
+def apply_adjoint_(y, compiled: CompiledPIModel, x, t=0.0, p=None, precision="fp64", coords="reference"):
+    """apply_adjoint!(y, compiled, x, t, p) (liouvillian.jl:4266, 3275-3324): y = L^H x with
+    L^H the conjugate transpose of the PI-coordinate generator, through the adjoint plan.
+    Same arguments and checks as apply_."""
+    return apply_(y, compiled.adjoint(), x, t, p, precision=precision, coords=coords)
+
+
+def krylov_liouvillian_spectrum(L, nev=6, krylovdim=None, which="LR", initial_vector=None, atol=1e-10,
+                                rtol=1e-8, vectors=False, rng=None, require_convergence=True):
+    """krylov_liouvillian_spectrum(L; nev, krylovdim=max(20, 2nev+4), which=:LR,
+    initial_vector, atol, rtol, vectors, rng, require_convergence) (krylov.jl:914-962).
+
+    The Arnoldi process runs on the GPU (pi_arnoldi); the projected eigenproblem, the Ritz
+    ordering (:LR largest real part, :LM / :SM largest / smallest modulus, krylov.jl:893-898)
+    and the residual estimates |H[k+1,k] y_k| with tolerance atol + rtol * max_j |H[:,j]|
+    follow the reference on the host.  Returns a dict with the reference's info fields."""
+    torch = _torch()
+    compiled = _as_compiled(L)
+    n = len(compiled.basis)
+    if not (0 < nev <= n):
+        raise PiArgumentError("nev must lie between 1 and the operator dimension")
+    if which not in ("LR", "LM", "SM"):
+        raise PiArgumentError("which must be :LR, :LM, or :SM")
+    krylovdim = max(20, 2 * nev + 4) if krylovdim is None else int(krylovdim)
+    m = min(n, max(krylovdim, nev + 1))
+    if m > 127:
+        raise PiArgumentError("the CUDA Arnoldi process supports krylov dimensions up to 127")
+    if initial_vector is None:
+        rng = rng if rng is not None else np.random.default_rng()
+        q = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+    else:
+        q = np.asarray(initial_vector, dtype=np.complex128)
+        if q.shape != (n,):
+            raise PiDimensionMismatch("initial_vector has wrong length")
+    v0 = torch.from_numpy(np.ascontiguousarray(q)).cuda()
+    V = torch.zeros((m + 1, n), dtype=torch.complex128, device="cuda")
+    H = np.zeros((m, m + 1), dtype=np.complex128)  # column-major (m+1) x m
+    info = _lib.pi_arnoldi_info_t()
+    torch.cuda.synchronize()
+    lib = _lib.load()
+    _lib.check(lib.pi_arnoldi(compiled.handle, _ptr(v0), m, _ptr(V), n, _lib.dptr(H.view(np.float64)),
+                              C.byref(info)), "krylov_liouvillian_spectrum")
+    H = H.T  # (m+1) x m
+    k = info.steps
+    vals, Y = np.linalg.eig(H[:k, :k])
+    key = {"LR": -vals.real, "LM": -np.abs(vals), "SM": np.abs(vals)}[which]
+    order = np.argsort(key, kind="stable")[:min(nev, k)]
+    vals, Y = vals[order], Y[:, order]
+    residuals = np.abs(H[k, k - 1] * Y[-1, :])
+    scale = max(max((np.linalg.norm(H[:k + 1, j]) for j in range(k)), default=0.0), np.finfo(float).tiny)
+    tolerance = atol + rtol * scale
+    converged = residuals <= tolerance
+    if require_convergence and not np.all(converged):
+        raise PiArgumentError(f"Arnoldi spectrum did not converge; maximum requested Ritz residual="
+                              f"{residuals.max()}; increase krylovdim")
+    out = dict(values=vals, residuals=residuals, converged=converged, iterations=k, krylov_dimension=m,
+               dimension=n, which=which, residual_scale=scale, residual_tolerance=tolerance,
+               workspace_reused=False, operator_applications=info.operator_applications)
+    if vectors:
+        Yc = np.ascontiguousarray(Y.T)  # ncols x k == k x ncols column-major
+        vec = torch.zeros((len(order), n), dtype=torch.complex128, device="cuda")
+        _lib.check(lib.pi_combine_f64(compiled.handle, _ptr(V), n, k, _lib.dptr(Yc.view(np.float64)), len(order),
+                                      _ptr(vec), n), "krylov_liouvillian_spectrum")
+        out["vectors"] = vec.cpu().numpy().T
+    return out
 
 
 def apply_element_major_(y, compiled: CompiledPIModel, x, coords="population"):

@@ -125,3 +125,17 @@ def test_unsupported_models_raise_argument_errors():
     bad = picuda.PIModel(picuda.PIBasis(3), [picuda.LocalJump(np.array([[np.nan, 0], [0, 0]]))])
     with pytest.raises(picuda.PiArgumentError):
         picuda.stencil_tables(bad)
+
+
+@pytest.mark.parametrize("name,make", CASES, ids=[c[0] for c in CASES])
+def test_adjoint_stencil_is_the_conjugate_transpose(name, make):
+    """The adjoint plan's stencil (pi_stencil_export_adjoint) applies the conjugate
+    transpose of the oracle's PI-coordinate matrix (apply_adjoint!, liouvillian.jl:3275)."""
+    model = make()
+    table, coef = picuda.stencil_tables(model, adjoint=True)
+    LH = O.adjoint_matrix(O.Plan(M.to_oracle(model)))
+    for seed in range(2):
+        x = M.random_state_vector(len(model.basis), seed)
+        y_ref = LH @ x
+        y = evaluate(model.basis, table, coef, x)
+        assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max(), name

@@ -307,3 +307,31 @@ def test_rk4_dynamics_grid_and_expv_agreement():
         assert np.allclose(a, c, atol=2e-9, rtol=0)
     rep = O.solve_dynamics_rk4(plan, rho0, (0.0, 0.2), saveat=[0.0, 0.1, 0.1, 0.2])
     assert np.array_equal(rep["states"][1], rep["states"][2])
+
+
+def test_arnoldi_spectrum_restatement_matches_dense_spectrum():
+    """test/test_krylov.jl:131-136: with krylovdim = dim the Arnoldi Ritz values equal the
+    dense spectrum's leading values to 2e-10, residual estimates < 2e-10, and
+    |L V - V diag(values)| < 2e-9."""
+    plan = O.Plan(_general_model(3, 2))
+    L = O.materialize(plan)
+    n = L.shape[0]
+    dense = np.linalg.eigvals(L)
+    dense = dense[O.ritz_order(dense, "LR")]
+    arn = O.krylov_liouvillian_spectrum(lambda v: L @ v, n, nev=4, krylovdim=n, vectors=True)
+    # conjugate pairs tie in real part, so compare the leading values as sets
+    canon = lambda v: v[np.lexsort((np.round(v.imag, 8), np.round(v.real, 8)))]
+    assert np.allclose(canon(arn["values"]), canon(dense[:4]), atol=2e-10, rtol=0)
+    assert arn["residuals"].max() < 2e-10
+    Vv = arn["vectors"]
+    assert np.linalg.norm(L @ Vv - Vv * arn["values"][None, :]) < 2e-9
+    with pytest.raises(ValueError):
+        O.krylov_liouvillian_spectrum(lambda v: L @ v, n, nev=0)
+    # duality: <y, L x> = <L^H y, x> and the trace functional is a left null vector
+    rng = np.random.default_rng(3)
+    x, y = rng.standard_normal(n) + 1j * rng.standard_normal(n), rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    LH = O.adjoint_matrix(plan)
+    assert abs(np.vdot(y, L @ x) - np.vdot(LH @ y, x)) <= 1e-12 * np.linalg.norm(L) * np.linalg.norm(x) * np.linalg.norm(y)
+    t = np.zeros(n, dtype=np.complex128)
+    t[plan.trace_idx] = plan.trace_val
+    assert np.abs(LH @ t).max() <= 1e-12 * np.abs(L).max()
