@@ -2,8 +2,8 @@
 
 Mirrors the reference's compiled_families.jl (compile_family :154-174, specialize :260-309)
 and scans.jl (ParameterScanPlan :42-213, ParameterScanPoint :256-275, ParameterScanResult
-:285-292, parameter_scan :1457-1467) for the steady-state task.  Term indices are 0-based
-(Python), where the reference's are 1-based.
+:285-292, parameter_scan :1457-1467) for the steady-state and spectral tasks.  Term indices
+are 0-based (Python), where the reference's are 1-based.
 
 Execution modes:
   - "serial" (the reference's default): points one after another through the single-instance
@@ -143,12 +143,18 @@ class ParameterScanPlan:
 
     def __init__(self, parameters, builder, remaker=None, *, task="steady_state", algorithm=None,
                  solver_options=None, continuation=True, save_outputs=True, save_vectors=False,
-                 save_restart=True, diagnostic=None, seed=0, rate_builder=None, atol=1e-10, rtol=1e-8):
+                 save_restart=True, spectrum_target="largest_real", nev=6, diagnostic=None, seed=0,
+                 rate_builder=None, atol=1e-10, rtol=1e-8):
         from .backend import GMRESAlgorithm
         if task not in _SCAN_TASKS:
             raise PiArgumentError("task must be :steady_state or :spectrum")
-        if task == "spectrum":
-            raise PiArgumentError("spectral scans are not part of the CUDA path; use task=:steady_state")
+        if spectrum_target not in ("largest_real", "near_zero", "largest_magnitude"):
+            raise PiArgumentError("spectrum_target must be :largest_real, :near_zero, or :largest_magnitude")
+        if not isinstance(nev, Integral) or isinstance(nev, bool) or nev <= 0:
+            raise PiArgumentError("nev must be positive")
+        if task == "spectrum" and spectrum_target == "near_zero":
+            raise PiArgumentError("near-zero spectral targets use harmonic Arnoldi, which the CUDA path does not "
+                                  "provide; use :largest_real or :largest_magnitude")
         values = list(parameters)
         if not values:
             raise PiArgumentError("parameters cannot be empty")
@@ -183,16 +189,24 @@ class ParameterScanPlan:
                     return builder(parameter, index)
                 return builder(parameter)
         self.model_builder = make
-        algorithm = algorithm or GMRESAlgorithm()
-        if isinstance(algorithm, str):
-            if algorithm not in ("auto", "krylov", "gmres"):
-                raise PiArgumentError(f"unsupported steady-state scan algorithm {algorithm}")
-            algorithm = GMRESAlgorithm()
-        if not isinstance(algorithm, GMRESAlgorithm):
-            raise PiArgumentError("steady-state scans on the CUDA path use GMRESAlgorithm")
         soptions = dict(solver_options or {})
-        forbidden = [k for k in ("return_info", "initial_state", "workspace", "memory_budget", "krylovdim")
-                     if k in soptions]
+        if task == "steady_state":
+            algorithm = algorithm or GMRESAlgorithm()
+            if isinstance(algorithm, str):
+                if algorithm not in ("auto", "krylov", "gmres"):
+                    raise PiArgumentError(f"unsupported steady-state scan algorithm {algorithm}")
+                algorithm = GMRESAlgorithm()
+            if not isinstance(algorithm, GMRESAlgorithm):
+                raise PiArgumentError("steady-state scans on the CUDA path use GMRESAlgorithm")
+            managed = ("return_info", "initial_state", "workspace", "memory_budget", "krylovdim")
+        else:
+            algorithm = algorithm or "krylov"
+            if algorithm not in ("auto", "krylov", "arnoldi"):
+                raise PiArgumentError(f"unsupported spectral scan algorithm {algorithm}; the CUDA path runs Arnoldi")
+            algorithm = "arnoldi"
+            managed = ("return_info", "initial_vector", "workspace", "rng", "vectors", "nev", "subspace_dim",
+                       "target", "memory_budget")
+        forbidden = [k for k in managed if k in soptions]
         if forbidden:
             raise PiArgumentError(f"solver_options contains internally managed keyword(s): {', '.join(forbidden)}")
         if not isinstance(seed, Integral) or seed < 0 or seed >= 2 ** 64:
@@ -206,6 +220,8 @@ class ParameterScanPlan:
         self.save_vectors = bool(save_vectors)
         self.save_restart = bool(save_restart)
         self.diagnostic = diagnostic
+        self.spectrum_target = spectrum_target
+        self.nev = int(nev)
         self.seed = int(seed)
         self.atol = float(soptions.pop("atol", atol))
         self.rtol = float(soptions.pop("rtol", rtol))
@@ -319,10 +335,56 @@ def _handle_failure(on_error, err):
         raise err
 
 
+def _point_rng(seed, index):
+    """Per-point generator from the plan seed and the point index (scans.jl:1055-1060), so a
+    point's starting vector does not depend on the execution order."""
+    mixed = (seed ^ ((index * 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF)) & 0xFFFFFFFFFFFFFFFF
+    return np.random.default_rng(mixed)
+
+
+def _spectrum_points(plan, selected, callback, on_error, kw):
+    """Spectral task (scans.jl:974-1053): one device Arnoldi process per point, warm-started
+    from the previous point's leading Ritz vector when continuation=True."""
+    from .backend import krylov_liouvillian_spectrum
+    which = {"largest_real": "LR", "largest_magnitude": "LM"}[plan.spectrum_target]
+    points, seed_vec, stopped = [], None, False
+    for index in selected:
+        parameter = plan.parameters[index]
+        t0 = time.perf_counter()
+        try:
+            compiled = _compile_point(plan, parameter, index)
+            t1 = time.perf_counter()
+            warm = plan.continuation and seed_vec is not None and len(seed_vec) == len(compiled.basis)
+            res = krylov_liouvillian_spectrum(compiled, nev=plan.nev, which=which,
+                                              initial_vector=seed_vec if warm else None,
+                                              vectors=plan.save_vectors or plan.continuation,
+                                              rng=_point_rng(plan.seed, index), **kw)
+            t2 = time.perf_counter()
+            vecs = res.pop("vectors", None)
+            if plan.continuation and vecs is not None:
+                seed_vec = vecs[:, 0].copy()
+            output = dict(values=res["values"], vectors=vecs if plan.save_vectors else None, info=res)
+            user = plan.diagnostic(output, parameter, index) if plan.diagnostic is not None else None
+            point = ParameterScanPoint(index, parameter, "success", output if plan.save_outputs else None,
+                                       float(res["residuals"].max()), None, bool(res["converged"].all()),
+                                       res["iterations"], t1 - t0, t2 - t1, t2 - t0, warm, False,
+                                       dict(solver=res, user=user, backend="cuda", dimension=len(compiled.basis),
+                                            method="arnoldi"), None, None)
+        except (PiError, ValueError) as err:
+            _handle_failure(on_error, err)
+            point = _failed(index, parameter, err, time.perf_counter() - t0)
+        points.append(point)
+        if _scan_callback(callback, point) or (point.status == "failed" and on_error == "stop"):
+            stopped = True
+            break
+    return points, seed_vec, stopped
+
+
 def parameter_scan(plan: ParameterScanPlan, callback=None, indices=None, execution="serial", on_error="stop",
                    max_points=None):
     """parameter_scan(plan; callback, indices, execution, on_error, max_points)
-    (scans.jl:1457-1467) for the steady-state task."""
+    (scans.jl:1457-1467).  Steady-state points run batched for execution "threads" /
+    "batched"; spectral points run one device Arnoldi process each in every mode."""
     from .backend import stationary_state, stationary_state_batch
     if execution not in _SCAN_EXECUTIONS:
         raise PiArgumentError("execution must be :serial, :threads or :batched")
@@ -336,7 +398,9 @@ def parameter_scan(plan: ParameterScanPlan, callback=None, indices=None, executi
     seed_state = None
     stopped = False
     kw = dict(atol=plan.atol, rtol=plan.rtol, **plan.solver_options)
-    if execution == "serial":
+    if plan.task == "spectrum":
+        points, seed_state, stopped = _spectrum_points(plan, selected, callback, on_error, kw)
+    elif execution == "serial":
         for index in selected:
             parameter = plan.parameters[index]
             t0 = time.perf_counter()

@@ -67,3 +67,22 @@ def test_scan_records_nonconverged_points(torch_cuda):
     assert all(p.status == "failed" and p.error_type == "PiNotConverged" for p in res)
     with pytest.raises(picuda.PiNotConverged):
         picuda.parameter_scan(plan, execution="batched", on_error="throw")
+
+
+def test_spectral_family_scan(torch_cuda):
+    """task=:spectrum: each point's leading Ritz values equal a direct Arnoldi spectrum of the
+    specialized model; serial continuation warm-starts from the previous leading vector."""
+    proto = M.scan_model(6, 1.0, 0.2, 0.05)
+    fam = picuda.compile_family(proto, rate_indices=[0])
+    grid = [0.5, 0.8, 1.1]
+    n = len(proto.basis)
+    plan = picuda.ParameterScanPlan(grid, fam, task="spectrum", nev=3, continuation=True, save_vectors=True,
+                                    solver_options={"krylovdim": n})
+    res = picuda.parameter_scan(plan)
+    assert [p.warm_started for p in res] == [False, True, True]
+    for pt, om in zip(res, grid):
+        assert pt.status == "success" and pt.converged
+        direct = picuda.krylov_liouvillian_spectrum(picuda.specialize(fam, om), nev=3, krylovdim=n)
+        canon = lambda v: v[np.lexsort((np.round(v.imag, 8), np.round(v.real, 8)))]
+        assert np.allclose(canon(pt.output["values"]), canon(direct["values"]), atol=1e-9, rtol=0)
+        assert pt.output["vectors"].shape == (n, 3)

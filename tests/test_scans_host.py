@@ -86,3 +86,20 @@ def test_scan_failure_policies_and_callback():
     for ex in ("threads", "batched"):
         r = picuda.parameter_scan(plan, execution=ex, on_error="record")
         assert [p.status for p in r] == ["failed"] * 3
+
+
+def test_spectral_scan_plan_validation():
+    """scans.jl:93-102, 126-151 for task=:spectrum."""
+    build = lambda p: _model()
+    plan = picuda.ParameterScanPlan([1.0], build, task="spectrum", nev=3, solver_options={"krylovdim": 30})
+    assert plan.task == "spectrum" and plan.nev == 3 and plan.solver_options == {"krylovdim": 30}
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.ParameterScanPlan([1.0], build, task="spectrum", nev=0)
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.ParameterScanPlan([1.0], build, task="spectrum", spectrum_target="smallest")
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.ParameterScanPlan([1.0], build, task="spectrum", spectrum_target="near_zero")
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.ParameterScanPlan([1.0], build, task="spectrum", solver_options={"vectors": True})
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.ParameterScanPlan([1.0], build, task="spectrum", algorithm="dense")
