@@ -11,6 +11,8 @@ from .backend import (AcceleratorCapability, CompiledPIModel, DynamicsResult, Dy
                       compile, evolve_, krylov_expv, krylov_expv_batch, krylov_liouvillian_spectrum, mul, saved_times, solve_dynamics,
                       solve_dynamics_batch, stationary_state, stationary_state_batch, steady_state,
                       stencil_tables, time_evolve)
+from .checkpoints import (PI_CHECKPOINT_VERSION, PIStateCheckpoint, checkpoint_state, load_checkpoint,
+                          save_checkpoint)
 from .scans import (CompiledPIModelFamily, ParameterScanPlan, ParameterScanPoint, ParameterScanResult,
                     compile_family, parameter_scan, specialize)
 from .serving import Completion, Server

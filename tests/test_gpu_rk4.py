@@ -139,3 +139,21 @@ def test_rk4_mixed_precision_vs_fp64(torch_cuda, N):
         assert abs(O.trace(oplan, st.data) - 1) <= 1e-6
     for k in obs:
         assert _rel(full.values[k], rmx.values[k]) <= 1e-12
+
+
+def test_checkpoint_resume_of_device_state(torch_cuda, tmp_path):
+    """A device state saved mid-evolution (PIStateCheckpoint, :pid format) and loaded back
+    resumes to exactly the uninterrupted result."""
+    torch = torch_cuda
+    model = M.driven_c1(8)
+    c = picuda.compile(model)
+    rho0 = picuda.computational_product_state(model.basis, 2)
+    d = torch.from_numpy(rho0.data.copy()).cuda()
+    picuda.evolve_(d, c, d, (0.0, 0.3), steps=30)
+    picuda.save_checkpoint(tmp_path / "mid.pid", d, time=0.3, metadata={"steps": 30}, basis=model.basis)
+    picuda.evolve_(d, c, d, (0.3, 0.6), steps=30)
+    ck = picuda.load_checkpoint(tmp_path / "mid.pid")
+    assert ck.time == 0.3 and ck.metadata == {"steps": "30"}
+    r = torch.from_numpy(ck.state.data.copy()).cuda()
+    picuda.evolve_(r, c, r, (ck.time, 0.6), steps=30)
+    assert torch.equal(r, d)
