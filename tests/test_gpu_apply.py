@@ -264,3 +264,38 @@ def test_element_major_apply_padded_stride_and_errors(torch_cuda):
     with pytest.raises(picuda.PiArgumentError):
         picuda.apply_element_major_(torch.empty((ng, 2), dtype=torch.complex64, device="cuda"), general,
                                     torch.empty((ng, 2), dtype=torch.complex64, device="cuda"))
+
+
+def test_apply_largest_served_size_properties(torch_cuda):
+    """The largest served request size (N = 300, dim 4,590,551), checked through properties
+    that hold at any size: trace preservation t^H (L x) = 0, duality <y, L x> = <L^H y, x>,
+    and the FP32 population-coordinate apply agreeing with the FP64 apply."""
+    torch = torch_cuda
+    model = M.ensemble_c2(300)
+    c = picuda.compile(model)
+    n = len(model.basis)
+    assert n == 4590551
+    x = torch.from_numpy(M.random_state_vector(n, 5)).cuda()
+    y = torch.from_numpy(M.random_state_vector(n, 6)).cuda()
+    Lx, LHy = torch.empty_like(x), torch.empty_like(y)
+    picuda.apply_(Lx, c, x)
+    picuda.apply_adjoint_(LHy, c, y)
+    idx, val = c.library_trace_functional()
+    idx_d = torch.from_numpy(idx).cuda()
+    val_d = torch.from_numpy(val).cuda().to(torch.complex128)
+    tr = (val_d * Lx[idx_d]).sum()
+    assert abs(complex(tr.item())) <= 1e-11 * float((val_d.abs() * Lx[idx_d].abs()).sum())
+    lhs, rhs = complex(torch.vdot(y, Lx).item()), complex(torch.vdot(LHy, x).item())
+    assert abs(lhs - rhs) <= 1e-12 * float(torch.linalg.norm(Lx)) * float(torch.linalg.norm(y))
+    # population coordinates z = sqrt(f) x are O(1) for physical states while sqrt(f) reaches
+    # ~1e44 at N = 300: draw z, then x = z / sqrt(f)
+    scale = torch.from_numpy(np.repeat(c.sector_scales(), np.array(model.basis.dims) ** 2)).cuda()
+    z64 = torch.from_numpy(M.random_state_vector(n, 7)).cuda()
+    xz = z64 / scale
+    Lxz = torch.empty_like(xz)
+    picuda.apply_(Lxz, c, xz)
+    z = z64.to(torch.complex64)
+    Lz = torch.empty_like(z)
+    picuda.apply_(Lz, c, z, precision="fp32", coords="population")
+    ref = Lxz * scale
+    assert float((Lz.to(torch.complex128) - ref).abs().max()) <= 1e-5 * float(ref.abs().max())
