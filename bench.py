@@ -564,6 +564,8 @@ def main():
     ap.add_argument("--steady-requests", type=int, default=16)
     ap.add_argument("--only-rk4", default=None, choices=["fp64", "mixed"],
                     help="one short RK4 solve of the large time-evolution model (a profiling target)")
+    ap.add_argument("--only-expv", default=None, choices=["fp64", "mixed"],
+                    help="one short expv solve of the large time-evolution model (a profiling target)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -592,6 +594,16 @@ def main():
         return 0
     if args.only_serve:
         print(json.dumps({"only_serve": True, "serve": serve_rates(picuda, torch, args.serve_requests)}))
+        return 0
+    if args.only_expv:
+        # two saved intervals of dt = 0.05 (expv m = 30), Jz and J+J- streamed
+        sm = picuda.spin_matrices(2)
+        c2 = picuda.compile(model_c2(picuda))
+        rho0 = picuda.computational_product_state(c2.basis, 2)
+        res = picuda.solve_dynamics(c2, rho0, (0.0, 0.1), saveat=0.05, save_states=False,
+                                    algorithm=picuda.ExpvAlgorithm(krylovdim=30, precision=args.only_expv),
+                                    observables={"Jz": sm["jz"], "JpJm": sm["jp"] @ sm["jm"]})
+        print(json.dumps({"only_expv": args.only_expv, "Jz": [float(v.real) for v in res.values["Jz"]]}))
         return 0
     if args.only_rk4:
         # two saved intervals of 0.05 (64 RK4 steps each), Jz and J+J- streamed

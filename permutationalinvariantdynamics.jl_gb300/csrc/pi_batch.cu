@@ -478,7 +478,9 @@ __global__ void __launch_bounds__(kRT)
       partv[(long long)blockIdx.x * kMaxDots + g0 + k] = make_double2(acc[2 * k], acc[2 * k + 1]);
 }
 
-// which 0: hA, 1: hB
+// which 0: hA, 1: hB.  Grid (instances, column groups): warp w of block (x, y) reduces
+// column i = y * warps + w, so every column of every instance has its own warp (one warp
+// walking several columns left a single SM reducing a long chunk list per column).
 __global__ void __launch_bounds__(kRT)
     k_step_mdot_final(const DevInst* __restrict__ st, const int* __restrict__ nchunks, const double2* __restrict__ partv,
                       int which) {
@@ -486,11 +488,10 @@ __global__ void __launch_bounds__(kRT)
   if (S.done) return;
   const int nv = S.j + 1;
   double2* h = which == 0 ? S.hA : S.hB;
-  const int warp = threadIdx.x >> 5;
-  for (int i = warp; i < nv; i += blockDim.x >> 5) {
-    const double2 v = warp_chunk_sum(partv, S.chunk_begin, nchunks[blockIdx.x], i);
-    if ((threadIdx.x & 31) == 0) h[i] = v;
-  }
+  const int i = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= nv) return;  // warp-uniform
+  const double2 v = warp_chunk_sum(partv, S.chunk_begin, nchunks[blockIdx.x], i);
+  if ((threadIdx.x & 31) == 0) h[i] = v;
 }
 
 // w -= sum_i V_i h_i (which 0: hA, 1: hB); with part != nullptr also |w|^2 partials.
@@ -1690,6 +1691,7 @@ void Engine::arnoldi_step() {
   double* none = nullptr;
   const int n = (int)jobs_.size();
   const dim3 gmd(total_chunks_, (m_ + 1 + 7) / 8);
+  const dim3 gfin(n, (m_ + 1 + kRT / 32 - 1) / (kRT / 32));
   const int C = total_chunks_;
   if (f32_) {
     launch(k_step_trace<float2>, n, kRT, 0, st);
@@ -1700,13 +1702,13 @@ void Engine::arnoldi_step() {
       launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv);
     else
       launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv);
-    launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
+    launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 0, none);
     if (chunk_ == kBatchChunk)
       launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv);
     else
       launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv);
-    launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
+    launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 1, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
     launch(k_step_normalize_f32, C, kRT, 0, (const DevInst*)st, ci);
@@ -1716,10 +1718,10 @@ void Engine::arnoldi_step() {
     launch(k_step_image_partial<double2>, C, kRT, 0, (const DevInst*)st, ci, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);
     launch(k_step_mdot_partial<double2, false>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
-    launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
+    launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
     launch(k_step_maxpy<double2>, C, kRT, 0, (const DevInst*)st, ci, 0, none);
     launch(k_step_mdot_partial<double2, false>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
-    launch(k_step_mdot_final, n, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
+    launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
     launch(k_step_maxpy<double2>, C, kRT, 0, (const DevInst*)st, ci, 1, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
     launch(k_step_normalize<double2>, C, kRT, 0, (const DevInst*)st, ci);
