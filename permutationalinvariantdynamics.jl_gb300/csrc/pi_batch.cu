@@ -628,9 +628,13 @@ __device__ __forceinline__ void pair_terms(const float4 a, const float4 b, DF& r
   df_add(im, fmaf(a.x, b.y, fmaf(-a.y, b.x, fmaf(a.z, b.w, -(a.w * b.z)))));
 }
 
+// With ipart (first pass of an expv cycle step) the block also writes the double-float
+// |w|^2 partial of its chunk, the image norm |L V_j| (the same pairs in the same order as
+// former separate image-norm sweep, so the same value), while w is staged anyway.
 template <int CH>
 __global__ void __launch_bounds__(kRT, 3)
-    k_step_mdot_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv) {
+    k_step_mdot_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv,
+                    double* __restrict__ ipart) {
   constexpr int kPairs = CH / 2 / kRT;  // element pairs per thread and chunk
   __shared__ float4 wsm[CH / 2];
   __shared__ float4 red[kMaxDots][kRT / 32];  // per warp: (re.hi, re.lo, im.hi, im.lo)
@@ -643,10 +647,17 @@ __global__ void __launch_bounds__(kRT, 3)
   const float4* __restrict__ w4 = reinterpret_cast<const float4*>(S.w) + beg;
   const float4* __restrict__ V4 = reinterpret_cast<const float4*>(S.V) + beg;
   const long long ld4 = S.ldv / 2;
+  DF nrm{0.f, 0.f};
 #pragma unroll
   for (int q = 0; q < kPairs; ++q) {
     const int p = threadIdx.x + q * kRT;
-    wsm[p] = p < npair ? w4[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 wv = p < npair ? w4[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    wsm[p] = wv;
+    if (p < npair) df_add(nrm, fmaf(wv.x, wv.x, fmaf(wv.y, wv.y, fmaf(wv.z, wv.z, wv.w * wv.w))));
+  }
+  if (ipart != nullptr && !S.givens) {  // block-uniform
+    const double r = block_df_sum(nrm, reinterpret_cast<float2*>(&red[0][0]));
+    if (threadIdx.x == 0) ipart[blockIdx.x] = r;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -799,24 +810,6 @@ __global__ void __launch_bounds__(kRT)
     const double r = block_df_sum(nrm, smem);
     if (threadIdx.x == 0) part[blockIdx.x] = r;
   }
-}
-
-// |w|^2 partial of the image (expv cycles), FP32 basis.
-__global__ void __launch_bounds__(kRT)
-    k_step_image_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double* __restrict__ part) {
-  __shared__ float2 smem[32];
-  const DevInst& S = st[chunk_inst[blockIdx.x]];
-  if (S.done || S.givens) return;
-  long long beg, end;
-  pair_range(S, blockIdx.x, beg, end);
-  const float4* __restrict__ w4 = reinterpret_cast<const float4*>(S.w);
-  DF nrm{0.f, 0.f};
-  for (long long p = beg + threadIdx.x; p < end; p += blockDim.x) {
-    const float4 wv = w4[p];
-    df_add(nrm, fmaf(wv.x, wv.x, fmaf(wv.y, wv.y, fmaf(wv.z, wv.z, wv.w * wv.w))));
-  }
-  const double r = block_df_sum(nrm, smem);
-  if (threadIdx.x == 0) part[blockIdx.x] = r;
 }
 
 // V_{j+1} = w / |w| (zero on an exact breakdown), FP32 basis.
@@ -1288,6 +1281,7 @@ SteadyJob::SteadyJob(pi_plan* p, double* x, const pi_gmres_opts_t& o, unsigned l
     : x_((double2*)x), o_(o), seed_(seed), host_probes_(host_probes) {
   plan = p;
   dim = p->host.dim;
+  bordered = true;
 }
 
 bool SteadyJob::setup(cudaStream_t s, int m, bool f32) {
@@ -1582,6 +1576,9 @@ void Engine::rebuild() {
   long long total_elems = 0;
   for (int i = 0; i < n; ++i) total_elems += jobs_[i]->dim;
   chunk_ = total_elems >= 8LL * 152 * kBatchChunk ? kBatchChunk : kBatchChunkSmall;
+  // the trace of each step's input column is only needed by bordered (steady-state) cycles
+  any_border_ = false;
+  for (int i = 0; i < n; ++i) any_border_ = any_border_ || jobs_[i]->bordered;
   std::vector<int> ti, tl, ci, nc(n);
   for (int i = 0; i < n; ++i) {
     const int ntiles = jobs_[i]->plan->dev.ntiles;
@@ -1694,26 +1691,26 @@ void Engine::arnoldi_step() {
   const dim3 gfin(n, (m_ + 1 + kRT / 32 - 1) / (kRT / 32));
   const int C = total_chunks_;
   if (f32_) {
-    launch(k_step_trace<float2>, n, kRT, 0, st);
+    if (any_border_) launch(k_step_trace<float2>, n, kRT, 0, st);
     launch(k_bapply<float, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(float2), (const DevInst*)st, ti, tl);
-    launch(k_step_image_f32, C, kRT, 0, (const DevInst*)st, ci, part);
-    launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);
+    // first-pass projections; expv cycles also take the image norm |w|^2 from this sweep
     if (chunk_ == kBatchChunk)
-      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv);
+      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv, part);
     else
-      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv);
+      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv, part);
+    launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);
     launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 0, none);
     if (chunk_ == kBatchChunk)
-      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv);
+      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv, none);
     else
-      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv);
+      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv, none);
     launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 1, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
     launch(k_step_normalize_f32, C, kRT, 0, (const DevInst*)st, ci);
   } else {
-    launch(k_step_trace<double2>, n, kRT, 0, st);
+    if (any_border_) launch(k_step_trace<double2>, n, kRT, 0, st);
     launch(k_bapply<double, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(double2), (const DevInst*)st, ti, tl);
     launch(k_step_image_partial<double2>, C, kRT, 0, (const DevInst*)st, ci, part);
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);

@@ -121,6 +121,7 @@ class Job {
   int rc = PI_OK;
   std::string msg;
   bool finished = false;
+  bool bordered = false;  // cycles apply the trace-bordered operator (steady-state jobs)
   size_t bytes = 0;  // device bytes held by the job
   void* V = nullptr;
   void* w = nullptr;
@@ -287,6 +288,7 @@ class Engine {
   bool dirty_ = true;
   int total_tiles_ = 0, total_chunks_ = 0;
   int chunk_ = kBatchChunk;
+  bool any_border_ = true;  // some job of the current set runs bordered cycles
   size_t rec_stride_ = 0;  // double2 per job record
   // device work lists and scratch (capacity-managed)
   void* st_ = nullptr; size_t st_cap_ = 0;
