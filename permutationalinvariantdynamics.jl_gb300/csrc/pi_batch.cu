@@ -629,8 +629,8 @@ __device__ __forceinline__ void pair_terms(const float4 a, const float4 b, DF& r
 }
 
 // With ipart (first pass of an expv cycle step) the block also writes the double-float
-// |w|^2 partial of its chunk, the image norm |L V_j| (the same pairs in the same order as
-// former separate image-norm sweep, so the same value), while w is staged anyway.
+// |w|^2 partial of its chunk for the image norm |L V_j| -- the same pairs in the same order
+// as a separate sweep over w would take -- while w is staged anyway.
 template <int CH>
 __global__ void __launch_bounds__(kRT, 3)
     k_step_mdot_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv,
