@@ -829,71 +829,89 @@ __global__ void __launch_bounds__(kRT)
   }
 }
 
-// Per instance: records Hessenberg column j, applies the GMRES rotations and stop test
-// (krylov.jl:759-777), advances j.  One thread per instance.
-__global__ void k_step_finish(DevInst* __restrict__ st, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// Per instance (one warp): records Hessenberg column j, applies the GMRES rotations and stop
+// test (krylov.jl:759-777), advances j.  The warp gathers the column (hA + hB), the zero
+// fill and the stored rotations into shared memory in parallel; lane 0 then runs the
+// sequential rotation arithmetic on shared memory (the same operations in the same order
+// as a single-thread pass over global memory, whose dependent loads dominated the step) and
+// the warp writes the column back.
+__global__ void __launch_bounds__(32) k_step_finish(DevInst* __restrict__ st, int n) {
+  __shared__ double2 colv[kBatchMaxKrylov + 2];
+  __shared__ double csv[kBatchMaxKrylov + 2];
+  __shared__ double2 snv[kBatchMaxKrylov + 2];
+  const int i = blockIdx.x;
   if (i >= n) return;
   DevInst& S = st[i];
   if (S.done) return;
+  const int lane = threadIdx.x;
   const int j = S.j;
   const int ld = S.ldh;
   double2* col = S.H + (long long)j * ld;
-  for (int r = 0; r <= j; ++r) col[r] = make_double2(S.hA[r].x + S.hB[r].x, S.hA[r].y + S.hB[r].y);
-  const double rem = sqrt(S.rem2);
-  col[j + 1] = make_double2(rem, 0.0);
-  for (int r = j + 2; r < ld; ++r) col[r] = make_double2(0.0, 0.0);
-  S.image[j] = sqrt(S.image2);
-  S.kdone = j + 1;
-  bool stop = (j + 1 >= S.m) || rem == 0.0 || (long long)(j + 1) == S.dim;
-  if (S.givens) {
-    double2* cs = S.csn;
-    double2* sn = S.csn + ld;
-    for (int r = 0; r < j; ++r) {
-      const double2 h1 = col[r], h2 = col[r + 1];
-      const double c = cs[r].x;
-      const double2 s = sn[r];
-      const double2 sh2 = cmul(s, h2);
-      const double2 csh1 = cmul(conjd(s), h1);
-      col[r] = make_double2(c * h1.x + sh2.x, c * h1.y + sh2.y);
-      col[r + 1] = make_double2(-csh1.x + c * h2.x, -csh1.y + c * h2.y);
+  double2* cs = S.csn;
+  double2* sn = S.csn + ld;
+  for (int r = lane; r < ld; r += 32)
+    colv[r] = r <= j ? make_double2(S.hA[r].x + S.hB[r].x, S.hA[r].y + S.hB[r].y) : make_double2(0.0, 0.0);
+  if (S.givens)
+    for (int r = lane; r < j; r += 32) {
+      csv[r] = cs[r].x;
+      snv[r] = sn[r];
     }
-    // complex Givens rotation (krylov.jl:710-716)
-    const double2 a = col[j], b = col[j + 1];
-    double c;
-    double2 s;
-    if (b.x == 0.0 && b.y == 0.0) {
-      c = 1.0;
-      s = make_double2(0.0, 0.0);
-    } else if (a.x == 0.0 && a.y == 0.0) {
-      c = 0.0;
-      s = make_double2(1.0, 0.0);
-    } else {
-      const double aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
-      const double sc = aa + bb;
-      const double ax = a.x / sc, ay = a.y / sc, bx = b.x / sc, by = b.y / sc;
-      const double normab = sc * sqrt((ax * ax + ay * ay) + (bx * bx + by * by));
-      const double2 al = make_double2(a.x / aa, a.y / aa);
-      c = aa / normab;
-      const double2 t = cmul(al, conjd(b));
-      s = make_double2(t.x / normab, t.y / normab);
+  __syncwarp();
+  if (lane == 0) {
+    const double rem = sqrt(S.rem2);
+    colv[j + 1] = make_double2(rem, 0.0);
+    S.image[j] = sqrt(S.image2);
+    S.kdone = j + 1;
+    bool stop = (j + 1 >= S.m) || rem == 0.0 || (long long)(j + 1) == S.dim;
+    if (S.givens) {
+      for (int r = 0; r < j; ++r) {
+        const double2 h1 = colv[r], h2 = colv[r + 1];
+        const double c = csv[r];
+        const double2 s = snv[r];
+        const double2 sh2 = cmul(s, h2);
+        const double2 csh1 = cmul(conjd(s), h1);
+        colv[r] = make_double2(c * h1.x + sh2.x, c * h1.y + sh2.y);
+        colv[r + 1] = make_double2(-csh1.x + c * h2.x, -csh1.y + c * h2.y);
+      }
+      // complex Givens rotation (krylov.jl:710-716)
+      const double2 a = colv[j], b = colv[j + 1];
+      double c;
+      double2 s;
+      if (b.x == 0.0 && b.y == 0.0) {
+        c = 1.0;
+        s = make_double2(0.0, 0.0);
+      } else if (a.x == 0.0 && a.y == 0.0) {
+        c = 0.0;
+        s = make_double2(1.0, 0.0);
+      } else {
+        const double aa = hypot(a.x, a.y), bb = hypot(b.x, b.y);
+        const double sc = aa + bb;
+        const double ax = a.x / sc, ay = a.y / sc, bx = b.x / sc, by = b.y / sc;
+        const double normab = sc * sqrt((ax * ax + ay * ay) + (bx * bx + by * by));
+        const double2 al = make_double2(a.x / aa, a.y / aa);
+        c = aa / normab;
+        const double2 t = cmul(al, conjd(b));
+        s = make_double2(t.x / normab, t.y / normab);
+      }
+      cs[j] = make_double2(c, 0.0);
+      sn[j] = s;
+      const double2 sb = cmul(s, b);
+      colv[j] = make_double2(c * a.x + sb.x, c * a.y + sb.y);
+      colv[j + 1] = make_double2(0.0, 0.0);
+      const double2 g1 = S.g[j], g2 = S.g[j + 1];
+      const double2 sg2 = cmul(s, g2);
+      const double2 csg1 = cmul(conjd(s), g1);
+      S.g[j] = make_double2(c * g1.x + sg2.x, c * g1.y + sg2.y);
+      S.g[j + 1] = make_double2(-csg1.x + c * g2.x, -csg1.y + c * g2.y);
+      if (hypot(S.g[j + 1].x, S.g[j + 1].y) <= S.tol) stop = true;
     }
-    cs[j] = make_double2(c, 0.0);
-    sn[j] = s;
-    const double2 sb = cmul(s, b);
-    col[j] = make_double2(c * a.x + sb.x, c * a.y + sb.y);
-    col[j + 1] = make_double2(0.0, 0.0);
-    const double2 g1 = S.g[j], g2 = S.g[j + 1];
-    const double2 sg2 = cmul(s, g2);
-    const double2 csg1 = cmul(conjd(s), g1);
-    S.g[j] = make_double2(c * g1.x + sg2.x, c * g1.y + sg2.y);
-    S.g[j + 1] = make_double2(-csg1.x + c * g2.x, -csg1.y + c * g2.y);
-    if (hypot(S.g[j + 1].x, S.g[j + 1].y) <= S.tol) stop = true;
+    if (stop)
+      S.done = 1;
+    else
+      S.j = j + 1;
   }
-  if (stop)
-    S.done = 1;
-  else
-    S.j = j + 1;
+  __syncwarp();
+  for (int r = lane; r < ld; r += 32) col[r] = colv[r];
 }
 
 // Dense normalized trace vector v = t / (t^H t) in reference coordinates.
@@ -1723,7 +1741,7 @@ void Engine::arnoldi_step() {
     launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
     launch(k_step_normalize<double2>, C, kRT, 0, (const DevInst*)st, ci);
   }
-  launch(k_step_finish, (n + 63) / 64, 64, 0, st, n);
+  launch(k_step_finish, n, 32, 0, st, n);
   if (!build_) chk(cudaGetLastError());
 }
 
