@@ -159,8 +159,11 @@ int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, lon
  * Krylov vectors or initial states kept side by side).  Replaces the matrix form of
  * apply! (liouvillian.jl:3232-3251) for a batch held in this layout.  ncols and ld even,
  * both buffers 16-byte aligned.  Needs a plan whose stencil sits at the canonical
- * positions (pi_plan_info_t.batched_kernel == 2); builds and caches the merged coefficient
- * planes (about 80 bytes per PI coordinate) on first use. */
+ * positions (pi_plan_info_t.batched_kernel == 2).  Plans of up to 160 sectors (N <= 318)
+ * stage the sources in shared memory with TMA tensor maps (encoded on the host per source
+ * pointer, stride and width; the last four are kept); larger plans use plain loads.  The
+ * merged coefficients (32-48 bytes per PI coordinate, or 80-112 for plain loads) are built
+ * and cached on first use. */
 int pi_apply_f32_em(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld,
                     int coords, void* stream);
 /* Convenience with host buffers: copies x in, applies, copies y out (pinned host memory

@@ -35,6 +35,27 @@ struct pi_plan {
   const picuda::DevTile* em_tiles = nullptr;
   int em_ntiles = 0;
   const float2* em_planes32[2] = {nullptr, nullptr};
+  // Encoded per-sector TMA tensor maps of the last few element-major source batches (host
+  // copies, passed to the kernel by value), keyed by source pointer, stride and width.
+  struct EmMapSet {
+    const void* x;
+    long long ld;
+    int ncols;
+    std::vector<unsigned char> maps;  // nsectors x 128 bytes
+  };
+  std::vector<EmMapSet> em_maps;
+  // Split coefficient planes of the TMA-staged kernel (entry, row and column planes) per
+  // coordinate system, and the per-sector offsets of the row and column planes.
+  struct EmSplit {
+    const float4* eplane = nullptr;
+    const float4* lrow = nullptr;
+    const float4* rcol = nullptr;
+  };
+  EmSplit em_split[2];
+  const int* em_line_off = nullptr;
+  int em_nlines = 0;
+  const void* em_tma_tiles = nullptr;  // tile records of the TMA-staged kernel
+  int em_tma_ntiles = 0;
   // Single-instance solves run as one job of a batched engine kept with the plan (created on
   // first use for a Krylov dimension and basis precision, replaced when those change).
   picuda::Engine* engine = nullptr;

@@ -241,6 +241,42 @@ def test_element_major_apply_matches_column_apply(torch_cuda, name, make, coords
             assert np.abs(got[c] - r).max() <= TOL_F32 * np.abs(r).max(), name
 
 
+@pytest.mark.parametrize("name,make,ncols", [
+    ("c2_N61_128", lambda: M.ensemble_c2(61), 128),            # two 64-column halves, <= 64 sectors
+    ("pump_N130_130", lambda: picuda.Models.local_pump_decay(130, down=1.0, up=0.3), 130),  # 66 sectors
+    ("c2_N130_66", lambda: M.ensemble_c2(130), 66),            # ragged second half
+    ("c2_N331_2", lambda: M.ensemble_c2(331), 2),              # 166 sectors: plain-load kernel
+])
+def test_element_major_apply_wide_batches(torch_cuda, name, make, ncols):
+    """Element-major batches wider than one 64-column block, plans whose sector count selects
+    each tensor-map table size, and a plan beyond it, against the column-batch FP32 apply."""
+    torch = torch_cuda
+    model = make()
+    compiled = picuda.compile(model)
+    n = len(model.basis)
+    g = torch.Generator(device="cuda").manual_seed(11)
+    Xe = torch.randn((n, ncols), dtype=torch.complex64, device="cuda", generator=g)
+    Ye = torch.full_like(Xe, float("nan"))
+    picuda.apply_element_major_(Ye, compiled, Xe)
+    ref = torch.empty((ncols, n), dtype=torch.complex64, device="cuda")
+    picuda.apply_(ref, compiled, Xe.t().contiguous(), precision="fp32", coords="population")
+    torch.cuda.synchronize()
+    assert not torch.isnan(Ye).any().item(), name
+    err = (Ye.t() - ref).abs().max().item()
+    assert err <= 2e-6 * ref.abs().max().item(), (name, err)
+    # a second batch at another address (new tensor maps) and the first one again (kept maps)
+    X2 = torch.randn((n, ncols), dtype=torch.complex64, device="cuda", generator=g)
+    Y2 = torch.empty_like(X2)
+    picuda.apply_element_major_(Y2, compiled, X2)
+    Y3 = torch.empty_like(Xe)
+    picuda.apply_element_major_(Y3, compiled, Xe)
+    ref2 = torch.empty_like(ref)
+    picuda.apply_(ref2, compiled, X2.t().contiguous(), precision="fp32", coords="population")
+    torch.cuda.synchronize()
+    assert (Y2.t() - ref2).abs().max().item() <= 2e-6 * ref2.abs().max().item(), name
+    assert torch.equal(Y3, Ye), name  # deterministic
+
+
 def test_element_major_apply_padded_stride_and_errors(torch_cuda):
     torch = torch_cuda
     model = M.ensemble_c2(20)
