@@ -631,8 +631,9 @@ def main():
             picuda.apply_(Y32, compiled, X32, precision="fp32", coords="population")
 
     for _ in range(args.warmup):
-        step32()
+        step32()  # the first element-major call autotunes the kernel choice for this width
     torch.cuda.synchronize()
+    em_choice = picuda.element_major_tuning(compiled, BATCH) if em else None
     barrier(world)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
@@ -669,7 +670,8 @@ def main():
 
     if args.only_apply:
         if rank == 0:
-            print(json.dumps({"only_apply": True, "ms_fp32": ms, "ms_fp64": ms64, "gbs_fp32": achieved}))
+            print(json.dumps({"only_apply": True, "ms_fp32": ms, "ms_fp64": ms64, "gbs_fp32": achieved,
+                              "kernel": em_choice}))
         return 0
 
     # End to end through the host-buffer C-ABI call (pinned host memory, H2D + apply + D2H)
@@ -714,6 +716,7 @@ def main():
                                    "state vectors, FP32 population coordinates",
                        "layout": ("element-major (dim, 128): pi_apply_f32_em" if em else
                                   "columns (128, dim): pi_apply_f32"),
+                       "kernel": em_choice,
                        "model": "H=0.3Jz+1.2Jx, local decay 0.2, local dephasing 0.1, collective decay 0.05/N",
                        "batch": BATCH, "pi_dim": n, "l2": "inputs larger than L2 (310 MB per step read)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},

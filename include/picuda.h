@@ -159,13 +159,25 @@ int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, lon
  * Krylov vectors or initial states kept side by side).  Replaces the matrix form of
  * apply! (liouvillian.jl:3232-3251) for a batch held in this layout.  ncols and ld even,
  * both buffers 16-byte aligned.  Needs a plan whose stencil sits at the canonical
- * positions (pi_plan_info_t.batched_kernel == 2).  Plans of up to 160 sectors (N <= 318)
- * stage the sources in shared memory with TMA tensor maps (encoded on the host per source
- * pointer, stride and width; the last four are kept); larger plans use plain loads.  The
- * merged coefficients (32-48 bytes per PI coordinate, or 80-112 for plain loads) are built
- * and cached on first use. */
+ * positions (pi_plan_info_t.batched_kernel == 2).  Kernels: TMA-staged tiles of 16, 32 or
+ * (without pumping terms) 64 rows for plans of up to 160 sectors (N <= 318; tensor maps
+ * encoded on the host per source pointer, stride and width, the last four kept), and plain
+ * loads.  Autotuned: the first call for a batch width and coordinate system runs every
+ * candidate on the caller's batch, times them with CUDA events on `stream`, waits for that
+ * stream once and keeps the fastest for later calls; all candidates give the same y.  The
+ * coefficient planes (32-48 bytes per PI coordinate for TMA, 80-112 for plain loads) are
+ * built and cached on first use. */
 int pi_apply_f32_em(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld,
                     int coords, void* stream);
+/* The element-major kernel in use for (ncols, coords): kind 0 TMA-staged with tiles of
+ * *rows rows, 1 plain loads; *ms = the autotuner's timed duration of one apply (0 when the
+ * choice was pinned).  PI_ERR_INVALID_ARGUMENT before the first call with that width and
+ * coordinate system.  No counterpart in the reference (its autotuner-free CPU path). */
+int pi_apply_f32_em_tuning(pi_plan* plan, int ncols, int coords, int* kind, int* rows, double* ms);
+/* Pins the element-major kernel for (ncols, coords) instead of autotuning it (kind and rows
+ * as above; PI_ERR_INVALID_ARGUMENT for a choice the plan does not offer).  No counterpart
+ * in the reference. */
+int pi_apply_f32_em_select(pi_plan* plan, int ncols, int coords, int kind, int rows);
 /* Convenience with host buffers: copies x in, applies, copies y out (pinned host memory
  * gives full link bandwidth).  The FP32 variant takes PI_COORDS_* like pi_apply_f32. */
 int pi_apply_host_f64(pi_plan* plan, double* y_host, const double* x_host, int ncols);

@@ -400,12 +400,12 @@ struct alignas(16) TmTile {
 };
 static_assert(sizeof(TmTile) == 48, "tile record layout");
 
-template <bool PLUS>
+template <bool PLUS, int ROWS>
 struct TmCfg {
   static constexpr int NE = PLUS ? 3 : 2;  // float4 of the entry plane per entry
   static constexpr int RING = 6;           // two blocks of 8+1 warps per SM
-  static constexpr int ENTRY_BYTES = kTmW * kEmRows * NE * 16;  // entry-plane runs of the warps
-  static constexpr int ROW_BYTES = kEmRows * 16;                // row-plane run of the tile
+  static constexpr int ENTRY_BYTES = kTmW * ROWS * NE * 16;  // entry-plane runs of the warps
+  static constexpr int ROW_BYTES = ROWS * 16;                // row-plane run of the tile
   static constexpr int COL_BYTES = kTmW * 16;                   // column-plane values of the tile
   static constexpr int SMEM = RING * kTmSlotBytes + ENTRY_BYTES + ROW_BYTES + COL_BYTES + 2 * RING * 8;
 };
@@ -448,12 +448,12 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
-template <bool PLUS, int MAXS>
+template <bool PLUS, int MAXS, int ROWS>
 __global__ void __launch_bounds__(kTmThreads, 2)
     k_apply_em_tma(const __grid_constant__ EmMaps<MAXS> maps, const TmTile* __restrict__ tiles,
                    const float4* __restrict__ eplane, const float4* __restrict__ lrow,
                    const float4* __restrict__ rcol, float4* __restrict__ y, unsigned ld4, int npairs) {
-  using C = TmCfg<PLUS>;
+  using C = TmCfg<PLUS, ROWS>;
   constexpr int NE = C::NE;
   constexpr int RING = C::RING;
   static_assert(RING % 3 == 0, "own rows are kept in registers indexed by step modulo three");
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kTmThreads, 2)
   const TmTile tile = tiles[blockIdx.x];
   const int n = tile.n;
   const int a0 = tile.a0, b0 = tile.b0;
-  const int rows = min(kEmRows, n - a0);
+  const int rows = min(ROWS, n - a0);
   const int s0 = tile.s0, s2 = tile.s2;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(kTmThreads, 2)
       if (m_lg) tma_load_3d(dst + 2 * kTmSrcBytes, m_lg, xq, k + 1, b0, full);
       if (i == 0) {  // the warps' entry-plane runs (contiguous down a column), row and column planes
         for (int w = 0; w < nact; ++w)
-          bulk_load(ent_u32 + w * (kEmRows * NE * 16), eplane + (size_t)(tile.offset + a0 + (long long)(b0 + w) * n) * NE,
+          bulk_load(ent_u32 + w * (ROWS * NE * 16), eplane + (size_t)(tile.offset + a0 + (long long)(b0 + w) * n) * NE,
                     run_bytes, full);
         bulk_load(row_u32, lrow + tile.loff + a0, row_bytes, full);
         bulk_load(col_u32, rcol + tile.loff + b0, (uint32_t)nact * 16, full);
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(kTmThreads, 2)
   // + COL_F4 c]: with the row loop unrolled over the ring, every offset is a constant.
   constexpr int COL_F4 = kTmColBytes / 16, SRC_F4 = kTmSrcBytes / 16, SLOT_F4 = kTmSlotBytes / 16;
   const float4* rl = ring + warp * COL_F4 + lane;
-  const float4* ew = ent + warp * (kEmRows * NE);
+  const float4* ew = ent + warp * (ROWS * NE);
   unsigned yi = (unsigned)(tile.offset + a0 + (long long)(active ? b : 0) * n) * ld4 + (unsigned)(ok ? q : 0);
   int r = 0;
   // Step s carries own row s-1 (relative to a0), used by output rows s-2 .. s, and the
@@ -673,6 +673,46 @@ static int em_prepare(pi_plan* plan, int which, const float2** planes_out) {
   return PI_OK;
 }
 
+// Tile records of the TMA-staged kernel for tiles of rows x kTmW (one load per block),
+// built once per plan and tile height.  Caller holds plan->em_mu.
+static int em_tma_tiles(pi_plan* plan, int ri, const TmTile** tiles_out, int* ntiles_out) {
+  static constexpr int kRows[3] = {16, 32, 64};
+  const DevicePlan& dp = plan->dev;
+  if (!plan->em_tma_tiles[ri]) {
+    std::vector<DevSector> secs(dp.nsectors);
+    cudaError_t e = cudaMemcpy(secs.data(), dp.sectors, sizeof(DevSector) * secs.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "element-major tile list");
+    std::vector<TmTile> tiles;
+    int loff = 0;
+    for (int s = 0; s < dp.nsectors; ++s) {
+      const int n = secs[s].n;
+      for (int a0 = 0; a0 < n; a0 += kRows[ri])
+        for (int b0 = 0; b0 < n; b0 += kTmW) {
+          TmTile t{};
+          t.offset = secs[s].offset;
+          t.sector = s;
+          t.a0 = a0;
+          t.b0 = b0;
+          t.n = n;
+          t.s0 = secs[s].src[0];
+          t.s2 = secs[s].src[2];
+          t.loff = loff;
+          tiles.push_back(t);
+        }
+      loff += n;
+    }
+    void* d = plan_alloc(plan, sizeof(TmTile) * tiles.size());
+    if (!d) return fail(PI_ERR_OUT_OF_MEMORY, "element-major tile list");
+    e = cudaMemcpy(d, tiles.data(), sizeof(TmTile) * tiles.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(e, "element-major tile list");
+    plan->em_tma_tiles[ri] = d;
+    plan->em_tma_ntiles[ri] = (int)tiles.size();
+  }
+  *tiles_out = (const TmTile*)plan->em_tma_tiles[ri];
+  *ntiles_out = plan->em_tma_ntiles[ri];
+  return PI_OK;
+}
+
 // Builds (once per plan and coefficient set) the split coefficient planes of the TMA-staged
 // kernel and the per-sector line offsets of its row and column planes.
 static int em_prepare_split(pi_plan* plan, int which, pi_plan::EmSplit* out) {
@@ -694,39 +734,9 @@ static int em_prepare_split(pi_plan* plan, int which, pi_plan::EmSplit* out) {
     plan->em_line_off = (const int*)d;
     plan->em_nlines = acc;
   }
-  if (!plan->em_tma_tiles) {  // tile records (one load per block): tiles of kEmRows x kTmW
-    std::vector<DevSector> secs(dp.nsectors);
-    cudaError_t e = cudaMemcpy(secs.data(), dp.sectors, sizeof(DevSector) * secs.size(), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "element-major tile list");
-    std::vector<TmTile> tiles;
-    int loff = 0;
-    for (int s = 0; s < dp.nsectors; ++s) {
-      const int n = secs[s].n;
-      for (int a0 = 0; a0 < n; a0 += kEmRows)
-        for (int b0 = 0; b0 < n; b0 += kTmW) {
-          TmTile t{};
-          t.offset = secs[s].offset;
-          t.sector = s;
-          t.a0 = a0;
-          t.b0 = b0;
-          t.n = n;
-          t.s0 = secs[s].src[0];
-          t.s2 = secs[s].src[2];
-          t.loff = loff;
-          tiles.push_back(t);
-        }
-      loff += n;
-    }
-    void* d = plan_alloc(plan, sizeof(TmTile) * tiles.size());
-    if (!d) return fail(PI_ERR_OUT_OF_MEMORY, "element-major tile list");
-    e = cudaMemcpy(d, tiles.data(), sizeof(TmTile) * tiles.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return cuda_fail(e, "element-major tile list");
-    plan->em_tma_tiles = d;
-    plan->em_tma_ntiles = (int)tiles.size();
-  }
   pi_plan::EmSplit& sp = plan->em_split[which];
   if (!sp.eplane) {
-    const int ne = dp.canon_plus ? TmCfg<true>::NE : TmCfg<false>::NE;
+    const int ne = dp.canon_plus ? TmCfg<true, 32>::NE : TmCfg<false, 32>::NE;
     void* e_d = plan_alloc(plan, sizeof(float4) * (size_t)dp.dim * ne);
     void* l_d = plan_alloc(plan, sizeof(float4) * (size_t)plan->em_nlines);
     void* r_d = plan_alloc(plan, sizeof(float4) * (size_t)plan->em_nlines);
@@ -795,20 +805,156 @@ static const unsigned char* em_tensor_maps(pi_plan* plan, const void* x, long lo
   return plan->em_maps.back().maps.data();
 }
 
-template <bool PLUS, int MAXS>
-static cudaError_t launch_em_tma(const pi_plan* plan, const unsigned char* blob, const pi_plan::EmSplit& sp,
-                                 float4* y, unsigned ld4, int npairs, cudaStream_t s) {
+template <bool PLUS, int MAXS, int ROWS>
+static cudaError_t launch_em_tma(const unsigned char* blob, int nsectors, const TmTile* tiles, int ntiles,
+                                 const pi_plan::EmSplit& sp, float4* y, unsigned ld4, int npairs, cudaStream_t s) {
   EmMaps<MAXS> maps;
   std::memset(&maps, 0, sizeof(maps));
-  std::memcpy(maps.m, blob, (size_t)plan->dev.nsectors * sizeof(CUtensorMap));
-  auto kern = k_apply_em_tma<PLUS, MAXS>;
-  constexpr int smem = TmCfg<PLUS>::SMEM;
+  std::memcpy(maps.m, blob, (size_t)nsectors * sizeof(CUtensorMap));
+  auto kern = k_apply_em_tma<PLUS, MAXS, ROWS>;
+  constexpr int smem = TmCfg<PLUS, ROWS>::SMEM;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  dim3 grid((unsigned)plan->em_tma_ntiles, (unsigned)((npairs + 31) / 32));
-  kern<<<grid, kTmThreads, smem, s>>>(maps, (const TmTile*)plan->em_tma_tiles, sp.eplane, sp.lrow, sp.rcol, y, ld4,
-                                      npairs);
+  dim3 grid((unsigned)ntiles, (unsigned)((npairs + 31) / 32));
+  kern<<<grid, kTmThreads, smem, s>>>(maps, tiles, sp.eplane, sp.lrow, sp.rcol, y, ld4, npairs);
   return cudaGetLastError();
+}
+
+template <int MAXS, int ROWS>
+static cudaError_t launch_em_tma_rows(bool plus, const unsigned char* blob, int nsectors, const TmTile* tiles,
+                                      int ntiles, const pi_plan::EmSplit& sp, float4* y, unsigned ld4, int npairs,
+                                      cudaStream_t s) {
+  if (plus) {
+    if constexpr (ROWS <= 32)  // the pumping variant's entry plane leaves no room for 64-row runs
+      return launch_em_tma<true, MAXS, ROWS>(blob, nsectors, tiles, ntiles, sp, y, ld4, npairs, s);
+    return cudaErrorInvalidValue;
+  }
+  return launch_em_tma<false, MAXS, ROWS>(blob, nsectors, tiles, ntiles, sp, y, ld4, npairs, s);
+}
+
+// One element-major kernel choice: TMA-staged with tiles of `rows` rows (kind 0), or plain
+// loads (kind 1).
+struct EmCand {
+  int kind;
+  int rows;
+};
+
+// Runs one candidate.  Returns a PI status.
+static int em_run(pi_plan* plan, EmCand c, float* y_dev, const float* x_dev, int ncols, long long ld, int coords,
+                  cudaStream_t s) {
+  const DevicePlan& dp = plan->dev;
+  const int npairs = ncols / 2;
+  const unsigned ld4 = (unsigned)(ld / 2);
+  float4* y4 = (float4*)y_dev;
+  if (c.kind == 0) {
+    const unsigned char* maps = em_tensor_maps(plan, x_dev, ld, ncols);
+    if (!maps) return fail(PI_ERR_UNSUPPORTED, "element-major tensor maps could not be encoded");
+    pi_plan::EmSplit sp;
+    int rc = em_prepare_split(plan, coords, &sp);
+    if (rc) return rc;
+    const int ri = c.rows == 16 ? 0 : c.rows == 32 ? 1 : 2;
+    const TmTile* tiles = nullptr;
+    int ntiles = 0;
+    {
+      std::lock_guard<std::mutex> lk(plan->em_mu);
+      rc = em_tma_tiles(plan, ri, &tiles, &ntiles);
+    }
+    if (rc) return rc;
+    const bool plus = dp.canon_plus != 0, small = dp.nsectors <= kTmMapsSmall;
+    cudaError_t e;
+    switch (ri) {
+      case 0:
+        e = small ? launch_em_tma_rows<kTmMapsSmall, 16>(plus, maps, dp.nsectors, tiles, ntiles, sp, y4, ld4, npairs, s)
+                  : launch_em_tma_rows<kTmMapsLarge, 16>(plus, maps, dp.nsectors, tiles, ntiles, sp, y4, ld4, npairs, s);
+        break;
+      case 1:
+        e = small ? launch_em_tma_rows<kTmMapsSmall, 32>(plus, maps, dp.nsectors, tiles, ntiles, sp, y4, ld4, npairs, s)
+                  : launch_em_tma_rows<kTmMapsLarge, 32>(plus, maps, dp.nsectors, tiles, ntiles, sp, y4, ld4, npairs, s);
+        break;
+      default:
+        e = small ? launch_em_tma_rows<kTmMapsSmall, 64>(plus, maps, dp.nsectors, tiles, ntiles, sp, y4, ld4, npairs, s)
+                  : launch_em_tma_rows<kTmMapsLarge, 64>(plus, maps, dp.nsectors, tiles, ntiles, sp, y4, ld4, npairs, s);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "element-major apply launch (TMA)");
+    return PI_OK;
+  }
+  const float2* planes = nullptr;
+  int rc = em_prepare(plan, coords, &planes);
+  if (rc) return rc;
+  BorderArgs border{1.0, nullptr, coords};
+  // One right-hand-side pair per lane, 8-warp blocks, 64 registers (4 blocks per SM):
+  // measured fastest for plain loads on GB300 for 64..256-column batches.  Two pairs per
+  // lane, one pair per lane with 8-byte loads, wider blocks, L2 bulk prefetch and source
+  // loads pipelined a row ahead were all slower (the last raises the register count past 64
+  // and costs more in occupancy than it saves in latency).
+  dim3 grid((unsigned)plan->em_ntiles, (unsigned)((npairs + 31) / 32));
+  const float4* x4 = (const float4*)x_dev;
+  if (dp.canon_plus)
+    k_apply_em_f32<true, 1><<<grid, 32 * kEmWarps, 0, s>>>(dp.sectors, plan->em_tiles, planes, x4, y4, ld4, npairs, border);
+  else
+    k_apply_em_f32<false, 1><<<grid, 32 * kEmWarps, 0, s>>>(dp.sectors, plan->em_tiles, planes, x4, y4, ld4, npairs, border);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "element-major apply launch");
+  return PI_OK;
+}
+
+// The candidates for a plan: TMA-staged tiles of 16, 32 and (without pumping terms) 64 rows
+// when the plan's tensor maps fit the kernel-parameter table, and plain loads.
+static std::vector<EmCand> em_candidates(const pi_plan* plan) {
+  std::vector<EmCand> c;
+  if (plan->dev.nsectors <= kTmMapsLarge && tensor_map_encoder()) {
+    c.push_back({0, 32});
+    c.push_back({0, 16});
+    if (!plan->dev.canon_plus) c.push_back({0, 64});
+  }
+  c.push_back({1, 32});
+  return c;
+}
+
+// Autotuner: the first call for a batch width and coordinate system runs every candidate on
+// the caller's batch (all compute each output entry with the same operations, so y is the
+// same whichever runs), times two rounds of them with CUDA events on the caller's stream,
+// waits for that stream once, and keeps the fastest for later calls.
+static int em_tune(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld, int coords,
+                   cudaStream_t s, pi_plan::EmChoice* out) {
+  const std::vector<EmCand> cands = em_candidates(plan);
+  std::vector<cudaEvent_t> ev(2 * cands.size() * 2, nullptr);
+  for (auto& e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      for (auto& f : ev)
+        if (f) cudaEventDestroy(f);
+      return cuda_fail(cudaGetLastError(), "autotuner events");
+    }
+  int rc = PI_OK;
+  for (size_t i = 0; i < cands.size() && !rc; ++i) rc = em_run(plan, cands[i], y_dev, x_dev, ncols, ld, coords, s);
+  for (int round = 0; round < 2 && !rc; ++round)
+    for (size_t i = 0; i < cands.size() && !rc; ++i) {
+      cudaEventRecord(ev[(round * cands.size() + i) * 2], s);
+      rc = em_run(plan, cands[i], y_dev, x_dev, ncols, ld, coords, s);
+      cudaEventRecord(ev[(round * cands.size() + i) * 2 + 1], s);
+    }
+  cudaError_t e = rc ? cudaSuccess : cudaEventSynchronize(ev.back());
+  pi_plan::EmChoice best{ncols, coords, 1, 32, 0.0};
+  float best_ms = 3.4e38f;
+  if (!rc && e == cudaSuccess)
+    for (size_t i = 0; i < cands.size(); ++i) {
+      float ms = 3.4e38f;
+      for (int round = 0; round < 2; ++round) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, ev[(round * cands.size() + i) * 2], ev[(round * cands.size() + i) * 2 + 1]) ==
+            cudaSuccess)
+          ms = std::min(ms, t);
+      }
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = {ncols, coords, cands[i].kind, cands[i].rows, (double)ms};
+      }
+    }
+  for (auto& f : ev) cudaEventDestroy(f);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "autotuner timing");
+  *out = best;
+  return PI_OK;
 }
 
 }  // namespace picuda
@@ -832,47 +978,69 @@ extern "C" int pi_apply_f32_em(pi_plan* plan, float* y_dev, const float* x_dev, 
     return fail(PI_ERR_INVALID_ARGUMENT, "source and destination must not share storage");
   if ((unsigned long long)plan->host.dim * (unsigned long long)(ld / 2) >= (1ULL << 32))
     return fail(PI_ERR_UNSUPPORTED, "element-major batch larger than 2^32 16-byte rows; split the batch");
-  const DevicePlan& dp = plan->dev;
-  const int npairs = ncols / 2;
+  if (!plan->dev.canon)
+    return fail(PI_ERR_UNSUPPORTED,
+                "element-major batched apply needs a plan whose stencil sits at the canonical positions "
+                "(qubit models with real one-body operators)");
   cudaStream_t s = (cudaStream_t)stream;
-  const unsigned ld4 = (unsigned)(ld / 2);
-  // TMA-staged kernel when the per-sector tensor maps fit the kernel-parameter table and
-  // encode; else the kernel with plain loads.
-  if (dp.canon && dp.nsectors <= kTmMapsLarge) {
-    const unsigned char* maps = em_tensor_maps(plan, x_dev, ld, ncols);
-    if (maps) {
-      pi_plan::EmSplit sp;
-      int rc = em_prepare_split(plan, coords, &sp);
+  pi_plan::EmChoice ch{};
+  bool known = false;
+  {
+    std::lock_guard<std::mutex> lk(plan->em_mu);
+    for (const auto& c : plan->em_choices)
+      if (c.ncols == ncols && c.coords == coords) {
+        ch = c;
+        known = true;
+      }
+  }
+  if (!known) {
+    std::lock_guard<std::mutex> tl(plan->em_tune_mu);  // one tuning pass per key
+    {
+      std::lock_guard<std::mutex> lk(plan->em_mu);
+      for (const auto& c : plan->em_choices)
+        if (c.ncols == ncols && c.coords == coords) {
+          ch = c;
+          known = true;
+        }
+    }
+    if (!known) {
+      int rc = em_tune(plan, y_dev, x_dev, ncols, ld, coords, s, &ch);
       if (rc) return rc;
-      float4* y4 = (float4*)y_dev;
-      cudaError_t e;
-      if (dp.nsectors <= kTmMapsSmall)
-        e = dp.canon_plus ? launch_em_tma<true, kTmMapsSmall>(plan, maps, sp, y4, ld4, npairs, s)
-                          : launch_em_tma<false, kTmMapsSmall>(plan, maps, sp, y4, ld4, npairs, s);
-      else
-        e = dp.canon_plus ? launch_em_tma<true, kTmMapsLarge>(plan, maps, sp, y4, ld4, npairs, s)
-                          : launch_em_tma<false, kTmMapsLarge>(plan, maps, sp, y4, ld4, npairs, s);
-      if (e != cudaSuccess) return cuda_fail(e, "element-major apply launch (TMA)");
-      return PI_OK;
+      std::lock_guard<std::mutex> lk(plan->em_mu);
+      plan->em_choices.push_back(ch);
+      return PI_OK;  // y already holds L x from the timed runs
     }
   }
-  const float2* planes = nullptr;
-  int rc = em_prepare(plan, coords, &planes);
-  if (rc) return rc;
-  BorderArgs border{1.0, nullptr, coords};
-  // One right-hand-side pair per lane, 8-warp blocks, 64 registers (4 blocks per SM):
-  // measured fastest on GB300 for 64..256-column batches.  Two pairs per lane, one pair per
-  // lane with 8-byte loads, wider blocks, L2 bulk prefetch and source loads pipelined a row
-  // ahead were all slower (the last raises the register count past 64 and costs more in
-  // occupancy than it saves in latency).
-  dim3 grid((unsigned)plan->em_ntiles, (unsigned)((npairs + 31) / 32));
-  const float4* x4 = (const float4*)x_dev;
-  float4* y4 = (float4*)y_dev;
-  if (dp.canon_plus)
-    k_apply_em_f32<true, 1><<<grid, 32 * kEmWarps, 0, s>>>(dp.sectors, plan->em_tiles, planes, x4, y4, ld4, npairs, border);
-  else
-    k_apply_em_f32<false, 1><<<grid, 32 * kEmWarps, 0, s>>>(dp.sectors, plan->em_tiles, planes, x4, y4, ld4, npairs, border);
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "element-major apply launch");
+  return em_run(plan, EmCand{ch.kind, ch.rows}, y_dev, x_dev, ncols, ld, coords, s);
+}
+
+extern "C" int pi_apply_f32_em_tuning(pi_plan* plan, int ncols, int coords, int* kind, int* rows, double* ms) {
+  if (!plan || !kind || !rows || !ms) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  std::lock_guard<std::mutex> lk(plan->em_mu);
+  for (const auto& c : plan->em_choices)
+    if (c.ncols == ncols && c.coords == coords) {
+      *kind = c.kind;
+      *rows = c.rows;
+      *ms = c.ms;
+      return PI_OK;
+    }
+  return fail(PI_ERR_INVALID_ARGUMENT, "no element-major apply with this width and coordinate system has run yet");
+}
+
+extern "C" int pi_apply_f32_em_select(pi_plan* plan, int ncols, int coords, int kind, int rows) {
+  if (!plan) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  if (coords != PI_COORDS_REFERENCE && coords != PI_COORDS_POPULATION)
+    return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
+  bool listed = false;
+  for (const EmCand& c : em_candidates(plan)) listed = listed || (c.kind == kind && (kind == 1 || c.rows == rows));
+  if (!listed) return fail(PI_ERR_INVALID_ARGUMENT, "this element-major kernel choice is not available for the plan");
+  std::lock_guard<std::mutex> lk(plan->em_mu);
+  pi_plan::EmChoice ch{ncols, coords, kind, kind == 1 ? 32 : rows, 0.0};
+  for (auto& c : plan->em_choices)
+    if (c.ncols == ncols && c.coords == coords) {
+      c = ch;
+      return PI_OK;
+    }
+  plan->em_choices.push_back(ch);
   return PI_OK;
 }

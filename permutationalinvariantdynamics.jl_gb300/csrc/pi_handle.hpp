@@ -54,8 +54,16 @@ struct pi_plan {
   EmSplit em_split[2];
   const int* em_line_off = nullptr;
   int em_nlines = 0;
-  const void* em_tma_tiles = nullptr;  // tile records of the TMA-staged kernel
-  int em_tma_ntiles = 0;
+  const void* em_tma_tiles[3] = {nullptr, nullptr, nullptr};  // tile records, tiles of 16 / 32 / 64 rows
+  int em_tma_ntiles[3] = {0, 0, 0};
+  // Element-major kernel chosen by the autotuner (or pinned by the caller) per batch width
+  // and coordinate system: kind 0 TMA-staged with tiles of `rows` rows, 1 plain loads.
+  struct EmChoice {
+    int ncols, coords, kind, rows;
+    double ms;  // timed duration of one apply (0 when pinned)
+  };
+  std::vector<EmChoice> em_choices;
+  std::mutex em_tune_mu;
   // Single-instance solves run as one job of a batched engine kept with the plan (created on
   // first use for a Krylov dimension and basis precision, replaced when those change).
   picuda::Engine* engine = nullptr;

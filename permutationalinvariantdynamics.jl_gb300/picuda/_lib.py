@@ -165,6 +165,8 @@ PROTOTYPES = {
     "pi_apply_f64": (C.c_int, [_P, _P, _P, C.c_int, C.c_longlong, _P]),
     "pi_apply_f32": (C.c_int, [_P, _P, _P, C.c_int, C.c_longlong, C.c_int, _P]),
     "pi_apply_f32_em": (C.c_int, [_P, _P, _P, C.c_int, C.c_longlong, C.c_int, _P]),
+    "pi_apply_f32_em_tuning": (C.c_int, [_P, C.c_int, C.c_int, _I, _I, _D]),
+    "pi_apply_f32_em_select": (C.c_int, [_P, C.c_int, C.c_int, C.c_int, C.c_int]),
     "pi_apply_host_f64": (C.c_int, [_P, _P, _P, C.c_int]),
     "pi_apply_host_f32": (C.c_int, [_P, _P, _P, C.c_int, C.c_int]),
     "pi_dot_f64": (C.c_int, [_P, _P, _P, _D]),

@@ -349,6 +349,32 @@ def apply_element_major_(y, compiled: CompiledPIModel, x, coords="population"):
     return y
 
 
+EM_KERNELS = {0: "tma", 1: "plain"}
+
+
+def element_major_tuning(compiled: CompiledPIModel, ncols, coords="population"):
+    """The element-major kernel in use for a batch width and coordinate system, as chosen by
+    the autotuner on the first apply_element_major_ call (or pinned with
+    select_element_major_kernel): {"kernel": "tma" | "plain", "rows": tile rows, "ms": timed
+    duration of one apply (0 when pinned)}."""
+    lib = _lib.load()
+    cc = _lib.PI_COORDS_POPULATION if coords == "population" else _lib.PI_COORDS_REFERENCE
+    kind, rows, ms = C.c_int(), C.c_int(), C.c_double()
+    _lib.check(lib.pi_apply_f32_em_tuning(compiled.handle, int(ncols), cc, C.byref(kind), C.byref(rows),
+                                          C.byref(ms)), "element-major tuning")
+    return {"kernel": EM_KERNELS[kind.value], "rows": rows.value, "ms": ms.value}
+
+
+def select_element_major_kernel(compiled: CompiledPIModel, ncols, kernel="tma", rows=32, coords="population"):
+    """Pins the element-major kernel for a batch width and coordinate system instead of
+    autotuning it: kernel "tma" (tile rows 16, 32 or, without pumping terms, 64) or "plain"."""
+    lib = _lib.load()
+    cc = _lib.PI_COORDS_POPULATION if coords == "population" else _lib.PI_COORDS_REFERENCE
+    kind = {v: k for k, v in EM_KERNELS.items()}[kernel]
+    _lib.check(lib.pi_apply_f32_em_select(compiled.handle, int(ncols), cc, kind, int(rows)),
+               "element-major kernel choice")
+
+
 def mul(compiled: CompiledPIModel, x):
     """L * x for a host vector (allocating wrapper of apply!)."""
     y = np.empty_like(np.asarray(x, dtype=np.complex128))

@@ -277,6 +277,44 @@ def test_element_major_apply_wide_batches(torch_cuda, name, make, ncols):
     assert torch.equal(Y3, Ye), name  # deterministic
 
 
+@pytest.mark.parametrize("name,make,rows", [
+    ("c2_N40", lambda: M.ensemble_c2(40), (16, 32, 64)),
+    ("pump_decay_N30", lambda: picuda.Models.local_pump_decay(30, down=1.0, up=0.3), (16, 32)),
+])
+def test_element_major_autotuner(torch_cuda, name, make, rows):
+    """The first element-major call times every candidate kernel and keeps the fastest; every
+    candidate (TMA-staged tiles of each height, plain loads) gives the same y, bit for bit."""
+    torch = torch_cuda
+    compiled = picuda.compile(make())
+    n = len(compiled.basis)
+    ncols = 128
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.element_major_tuning(compiled, ncols)  # nothing tuned yet
+    g = torch.Generator(device="cuda").manual_seed(5)
+    X = torch.randn((n, ncols), dtype=torch.complex64, device="cuda", generator=g)
+    Y = torch.full_like(X, float("nan"))
+    picuda.apply_element_major_(Y, compiled, X)  # tunes
+    ref = torch.empty((ncols, n), dtype=torch.complex64, device="cuda")
+    picuda.apply_(ref, compiled, X.t().contiguous(), precision="fp32", coords="population")
+    torch.cuda.synchronize()
+    assert (Y.t() - ref).abs().max().item() <= 2e-6 * ref.abs().max().item(), name
+    choice = picuda.element_major_tuning(compiled, ncols)
+    assert choice["kernel"] in ("tma", "plain") and choice["ms"] > 0, choice
+    assert choice["kernel"] == "plain" or choice["rows"] in rows, choice
+    for kernel, r in [("tma", r) for r in rows] + [("plain", 32)]:
+        picuda.select_element_major_kernel(compiled, ncols, kernel, r)
+        Yk = torch.full_like(X, float("nan"))
+        picuda.apply_element_major_(Yk, compiled, X)
+        torch.cuda.synchronize()
+        assert torch.equal(Yk, Y), (name, kernel, r)
+        assert picuda.element_major_tuning(compiled, ncols) == {"kernel": kernel, "rows": r, "ms": 0.0}
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.select_element_major_kernel(compiled, ncols, "tma", 48)
+    if 64 not in rows:
+        with pytest.raises(picuda.PiArgumentError):
+            picuda.select_element_major_kernel(compiled, ncols, "tma", 64)
+
+
 def test_element_major_apply_padded_stride_and_errors(torch_cuda):
     torch = torch_cuda
     model = M.ensemble_c2(20)
