@@ -315,6 +315,36 @@ def test_element_major_autotuner(torch_cuda, name, make, rows):
             picuda.select_element_major_kernel(compiled, ncols, "tma", 64)
 
 
+@pytest.mark.parametrize("name,make,ncols", [
+    ("c2_N1", lambda: M.ensemble_c2(1), 2),
+    ("c2_N2", lambda: M.ensemble_c2(2), 4),
+    ("pump_decay_N3", lambda: picuda.Models.local_pump_decay(3, down=1.0, up=0.3), 66),
+    ("c2_N318", lambda: M.ensemble_c2(318), 2),  # 160 sectors: the largest TMA map table
+])
+def test_element_major_apply_edge_sizes(torch_cuda, name, make, ncols):
+    """Plans whose sectors are all smaller than one tile and the largest plan the TMA-staged
+    kernel takes: every candidate kernel against the column-batch apply."""
+    torch = torch_cuda
+    model = make()
+    compiled = picuda.compile(model)
+    n = len(model.basis)
+    g = torch.Generator(device="cuda").manual_seed(3)
+    X = torch.randn((n, ncols), dtype=torch.complex64, device="cuda", generator=g)
+    Y = torch.full_like(X, float("nan"))
+    picuda.apply_element_major_(Y, compiled, X)
+    ref = torch.empty((ncols, n), dtype=torch.complex64, device="cuda")
+    picuda.apply_(ref, compiled, X.t().contiguous(), precision="fp32", coords="population")
+    torch.cuda.synchronize()
+    assert not torch.isnan(Y).any().item(), name
+    assert (Y.t() - ref).abs().max().item() <= 2e-6 * max(ref.abs().max().item(), 1e-30), name
+    for kernel, r in [("tma", 16), ("tma", 32), ("plain", 32)]:
+        picuda.select_element_major_kernel(compiled, ncols, kernel, r)
+        Yk = torch.full_like(X, float("nan"))
+        picuda.apply_element_major_(Yk, compiled, X)
+        torch.cuda.synchronize()
+        assert torch.equal(Yk, Y), (name, kernel, r)
+
+
 def test_element_major_apply_padded_stride_and_errors(torch_cuda):
     torch = torch_cuda
     model = M.ensemble_c2(20)
