@@ -398,24 +398,6 @@ __global__ void __launch_bounds__(kRT)
   if (threadIdx.x == 0) part[blockIdx.x] = acc[0];
 }
 
-// which 0: image2 (expv cycles only), 1: rem2
-__global__ void __launch_bounds__(kRT)
-    k_step_norm_final(DevInst* __restrict__ st, const int* __restrict__ nchunks, const double* __restrict__ part,
-                      int which) {
-  __shared__ double smem[32];
-  DevInst& S = st[blockIdx.x];
-  if (S.done || (which == 0 && S.givens)) return;
-  double acc[1] = {0};
-  for (int c = threadIdx.x; c < nchunks[blockIdx.x]; c += blockDim.x) acc[0] += part[S.chunk_begin + c];
-  block_sum<1>(acc, smem);
-  if (threadIdx.x == 0) {
-    if (which == 0)
-      S.image2 = acc[0];
-    else
-      S.rem2 = acc[0];
-  }
-}
-
 // CGS2 projections: partv[c][i] = sum over chunk c of conj(V_i) w, i in [8 y, 8 y + 8).
 template <typename T2, bool DFACC>
 __global__ void __launch_bounds__(kRT)
@@ -494,6 +476,45 @@ __global__ void __launch_bounds__(kRT)
   if ((threadIdx.x & 31) == 0) h[i] = v;
 }
 
+// The first-pass reductions of a step in one launch: blocks (x, y < gridDim.y - 1) reduce the
+// projections into hA as k_step_mdot_final(which 0) does, blocks (x, gridDim.y - 1) the
+// image norm |w|^2 into image2 (expv cycles): thread t sums the chunk partials t, t + 256,
+// ... and a deterministic block sum combines the threads.
+__global__ void __launch_bounds__(kRT)
+    k_step_first_final(DevInst* __restrict__ st, const int* __restrict__ nchunks, const double2* __restrict__ partv,
+                       const double* __restrict__ part) {
+  __shared__ double smem[32];
+  DevInst& S = st[blockIdx.x];
+  if (S.done) return;
+  if (blockIdx.y == gridDim.y - 1) {  // image norm (block-uniform)
+    if (S.givens) return;
+    double acc[1] = {0};
+    for (int c = threadIdx.x; c < nchunks[blockIdx.x]; c += blockDim.x) acc[0] += part[S.chunk_begin + c];
+    block_sum<1>(acc, smem);
+    if (threadIdx.x == 0) S.image2 = acc[0];
+    return;
+  }
+  const int nv = S.j + 1;
+  const int i = blockIdx.y * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= nv) return;  // warp-uniform
+  const double2 v = warp_chunk_sum(partv, S.chunk_begin, nchunks[blockIdx.x], i);
+  if ((threadIdx.x & 31) == 0) S.hA[i] = v;
+}
+
+// |w|^2 of job S from its chunk partials (thread t sums partials t, t + 256, ..., then a
+// deterministic block sum), broadcast to the whole block: every block of the job obtains
+// the same value.
+__device__ __forceinline__ double job_norm2(const DevInst& S, int nchunks, const double* __restrict__ part) {
+  __shared__ double smem[32];
+  __shared__ double total;
+  double acc[1] = {0};
+  for (int c = threadIdx.x; c < nchunks; c += blockDim.x) acc[0] += part[S.chunk_begin + c];
+  block_sum<1>(acc, smem);
+  if (threadIdx.x == 0) total = acc[0];
+  __syncthreads();
+  return total;
+}
+
 // w -= sum_i V_i h_i (which 0: hA, 1: hB); with part != nullptr also |w|^2 partials.
 template <typename T2>
 __global__ void __launch_bounds__(kRT)
@@ -548,12 +569,18 @@ __global__ void __launch_bounds__(kRT)
   }
 }
 
-// V_{j+1} = w / |w| (zero on an exact breakdown).
+// V_{j+1} = w / |w| (zero on an exact breakdown).  Every block reduces the job's |w|^2
+// partials itself (the job's first block stores rem2 for the step finish), so no separate
+// reduction launch sits between the second-pass update and the normalisation.
 template <typename T2>
-__global__ void __launch_bounds__(kRT) k_step_normalize(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst) {
-  const DevInst& S = st[chunk_inst[blockIdx.x]];
+__global__ void __launch_bounds__(kRT) k_step_normalize(DevInst* __restrict__ st, const int* __restrict__ chunk_inst,
+                                                        const int* __restrict__ nchunks, const double* __restrict__ part) {
+  const int inst = chunk_inst[blockIdx.x];
+  DevInst& S = st[inst];
   if (S.done) return;
-  const double r = sqrt(S.rem2);
+  const double rem2 = job_norm2(S, nchunks[inst], part);
+  if (blockIdx.x == S.chunk_begin && threadIdx.x == 0) S.rem2 = rem2;
+  const double r = sqrt(rem2);
   const double f = r > 0 ? 1.0 / r : 0.0;
   long long beg, end;
   chunk_range(S, blockIdx.x, beg, end);
@@ -812,12 +839,16 @@ __global__ void __launch_bounds__(kRT)
   }
 }
 
-// V_{j+1} = w / |w| (zero on an exact breakdown), FP32 basis.
+// V_{j+1} = w / |w| (zero on an exact breakdown), FP32 basis; |w|^2 as in k_step_normalize.
 __global__ void __launch_bounds__(kRT)
-    k_step_normalize_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst) {
-  const DevInst& S = st[chunk_inst[blockIdx.x]];
+    k_step_normalize_f32(DevInst* __restrict__ st, const int* __restrict__ chunk_inst, const int* __restrict__ nchunks,
+                         const double* __restrict__ part) {
+  const int inst = chunk_inst[blockIdx.x];
+  DevInst& S = st[inst];
   if (S.done) return;
-  const double r = sqrt(S.rem2);
+  const double rem2 = job_norm2(S, nchunks[inst], part);
+  if (blockIdx.x == S.chunk_begin && threadIdx.x == 0) S.rem2 = rem2;
+  const double r = sqrt(rem2);
   const float f = r > 0 ? (float)(1.0 / r) : 0.f;
   long long beg, end;
   pair_range(S, blockIdx.x, beg, end);
@@ -1707,6 +1738,7 @@ void Engine::arnoldi_step() {
   const int n = (int)jobs_.size();
   const dim3 gmd(total_chunks_, (m_ + 1 + 7) / 8);
   const dim3 gfin(n, (m_ + 1 + kRT / 32 - 1) / (kRT / 32));
+  const dim3 gfirst(n, gfin.y + 1);  // projections into hA plus one row of image-norm blocks
   const int C = total_chunks_;
   if (f32_) {
     if (any_border_) launch(k_step_trace<float2>, n, kRT, 0, st);
@@ -1716,8 +1748,7 @@ void Engine::arnoldi_step() {
       launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv, part);
     else
       launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv, part);
-    launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);
-    launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
+    launch(k_step_first_final, gfirst, kRT, 0, st, nc, (const double2*)partv, (const double*)part);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 0, none);
     if (chunk_ == kBatchChunk)
       launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv, none);
@@ -1725,21 +1756,18 @@ void Engine::arnoldi_step() {
       launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv, none);
     launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
     launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 1, part);
-    launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
-    launch(k_step_normalize_f32, C, kRT, 0, (const DevInst*)st, ci);
+    launch(k_step_normalize_f32, C, kRT, 0, st, ci, nc, (const double*)part);
   } else {
     if (any_border_) launch(k_step_trace<double2>, n, kRT, 0, st);
     launch(k_bapply<double, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(double2), (const DevInst*)st, ti, tl);
     launch(k_step_image_partial<double2>, C, kRT, 0, (const DevInst*)st, ci, part);
-    launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 0);
     launch(k_step_mdot_partial<double2, false>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
-    launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 0);
+    launch(k_step_first_final, gfirst, kRT, 0, st, nc, (const double2*)partv, (const double*)part);
     launch(k_step_maxpy<double2>, C, kRT, 0, (const DevInst*)st, ci, 0, none);
     launch(k_step_mdot_partial<double2, false>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
     launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
     launch(k_step_maxpy<double2>, C, kRT, 0, (const DevInst*)st, ci, 1, part);
-    launch(k_step_norm_final, n, kRT, 0, st, nc, (const double*)part, 1);
-    launch(k_step_normalize<double2>, C, kRT, 0, (const DevInst*)st, ci);
+    launch(k_step_normalize<double2>, C, kRT, 0, st, ci, nc, (const double*)part);
   }
   launch(k_step_finish, n, 32, 0, st, n);
   if (!build_) chk(cudaGetLastError());
