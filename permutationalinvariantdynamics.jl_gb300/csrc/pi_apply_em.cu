@@ -189,10 +189,6 @@ __device__ __forceinline__ Stream make_stream(unsigned ld4, int off, int m, int 
   s.idx = (unsigned)(off + r + (s.col_ok ? c : 0) * m) * ld4 + (unsigned)q;
   return s;
 }
-__device__ __forceinline__ float4 take(const float4* __restrict__ x, const Stream& s) {
-  if (s.col_ok && (unsigned)s.row < (unsigned)s.m) return __ldg(x + s.idx);
-  return make_float4(0.f, 0.f, 0.f, 0.f);
-}
 __device__ __forceinline__ void advance(Stream& s, unsigned ld4) {
   s.idx += ld4;
   ++s.row;

@@ -348,7 +348,9 @@ int pi_capability(pi_capability_t* out) {
   out->cc_major = prop.major;
   out->cc_minor = prop.minor;
   out->total_memory = prop.totalGlobalMem;
-  std::strncpy(out->device_name, prop.name, sizeof(out->device_name) - 1);
+  size_t nl = 0;  // device name, truncated to the field
+  for (; nl + 1 < sizeof(out->device_name) && prop.name[nl]; ++nl) out->device_name[nl] = prop.name[nl];
+  out->device_name[nl] = '\0';
   // The kernels are built for sm_103a only.
   out->functional = (prop.major == 10 && prop.minor == 3) ? 1 : 0;
   out->supports_matrixfree_pi = out->functional;

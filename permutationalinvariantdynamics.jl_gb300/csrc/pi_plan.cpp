@@ -22,17 +22,6 @@ struct Rational {
   long long num = 0, den = 1;
 };
 
-long long gcd_ll(long long a, long long b) {
-  if (a < 0) a = -a;
-  if (b < 0) b = -b;
-  while (b) {
-    long long t = a % b;
-    a = b;
-    b = t;
-  }
-  return a;
-}
-
 Rational make_rat(__int128 n, __int128 d) {
   if (d == 0) throw std::invalid_argument("singular CG product");
   if (d < 0) {

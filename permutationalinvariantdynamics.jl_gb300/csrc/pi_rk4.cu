@@ -215,8 +215,7 @@ struct StepGraph {
     void* args[] = {&arg};
     for (int s = 0; s < steps && e == cudaSuccess; ++s)
       for (int stage = 0; stage < 4 && e == cudaSuccess; ++stage) {
-        cudaKernelNodeParams kp;
-        std::memset(&kp, 0, sizeof(kp));
+        cudaKernelNodeParams kp{};
         kp.func = (void*)k[stage];
         kp.gridDim = dim3((unsigned)ntiles);
         kp.blockDim = dim3(kApplyThreads);

@@ -88,11 +88,6 @@ struct Run {
     chk(launch_apply_f32(p->dev, (const float*)x, (float*)y, 1, n, b, s));
     ++applications;
   }
-  void apply_f32(const float2* x, float2* y, int coords) {
-    BorderArgs b{1.0, nullptr, coords};
-    chk(launch_apply_f32(p->dev, (const float*)x, (float*)y, 1, n, b, s));
-    ++applications;
-  }
   cd trace(const double2* x) {
     double2* out = p->rs.result;
     chk(trace_dot(p->dev, x, 0, 0, out, s));
