@@ -164,11 +164,11 @@ int pi_apply_f32(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, lon
  * encoded on the host per source pointer, stride and width, the last four kept), and plain
  * loads.  Autotuned: the first call for a batch width and coordinate system runs every
  * candidate on the caller's batch, times them with CUDA events on `stream`, waits for that
- * stream once and keeps the fastest for later calls; all candidates give the same y.  A
- * caller that captures the apply into a CUDA graph makes that first call outside the
- * capture (or pins the kernel with pi_apply_f32_em_select).  The coefficient planes
- * (32-48 bytes per PI coordinate for TMA, 80-112 for plain loads) are built and cached on
- * first use. */
+ * stream once and keeps the fastest for later calls; all candidates give the same y.  The
+ * coefficient planes (32-48 bytes per PI coordinate for TMA, 80-112 for plain loads) are
+ * built and cached on first use, with a synchronisation of their own.  A caller that
+ * captures the apply into a CUDA graph therefore makes one call per batch width and
+ * coordinate system before the capture. */
 int pi_apply_f32_em(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld,
                     int coords, void* stream);
 /* The element-major kernel in use for (ncols, coords): kind 0 TMA-staged with tiles of
