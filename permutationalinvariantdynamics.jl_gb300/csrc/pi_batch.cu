@@ -482,12 +482,12 @@ __global__ void __launch_bounds__(kRT)
 // ... and a deterministic block sum combines the threads.
 __global__ void __launch_bounds__(kRT)
     k_step_first_final(DevInst* __restrict__ st, const int* __restrict__ nchunks, const double2* __restrict__ partv,
-                       const double* __restrict__ part) {
+                       const double* __restrict__ part, int all_images) {
   __shared__ double smem[32];
   DevInst& S = st[blockIdx.x];
   if (S.done) return;
   if (blockIdx.y == gridDim.y - 1) {  // image norm (block-uniform)
-    if (S.givens) return;
+    if (S.givens && !all_images) return;
     double acc[1] = {0};
     for (int c = threadIdx.x; c < nchunks[blockIdx.x]; c += blockDim.x) acc[0] += part[S.chunk_begin + c];
     block_sum<1>(acc, smem);
@@ -655,19 +655,38 @@ __device__ __forceinline__ void pair_terms(const float4 a, const float4 b, DF& r
   df_add(im, fmaf(a.x, b.y, fmaf(-a.y, b.x, fmaf(a.z, b.w, -(a.w * b.z)))));
 }
 
-// With ipart (first pass of an expv cycle step) the block also writes the double-float
-// |w|^2 partial of its chunk for the image norm |L V_j| -- the same pairs in the same order
-// as a separate sweep over w would take -- while w is staged anyway.
+// With ipart (first pass of a step) the block also writes the double-float |w|^2 partial of
+// its chunk for the image norm |L V_j| (the expv error estimate and the reorthogonalisation
+// test) -- the same pairs in the same order as a separate sweep over w would take -- while w
+// is staged anyway.
+//
+// Second pass with npart1 (selective reorthogonalisation, Daniel-Gragg-Kaufman-Stewart): the
+// block first sums its job's |w1|^2 partials of the first-pass update; when |w1|^2 >= |w0|^2
+// / 2 (w0 = L V_j before any projection, image2) the first pass left w orthogonal to the
+// basis to working precision, so the block writes zero projections instead of sweeping the
+// basis again, and the job's first block records the choice in reorth for the update.
 template <int CH>
 __global__ void __launch_bounds__(kRT, 3)
-    k_step_mdot_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv,
-                    double* __restrict__ ipart) {
+    k_step_mdot_f32(DevInst* __restrict__ st, const int* __restrict__ chunk_inst, double2* __restrict__ partv,
+                    double* __restrict__ ipart, const int* __restrict__ nchunks, const double* __restrict__ npart1) {
   constexpr int kPairs = CH / 2 / kRT;  // element pairs per thread and chunk
   __shared__ float4 wsm[CH / 2];
-  __shared__ float4 red[kMaxDots][kRT / 32];  // per warp: (re.hi, re.lo, im.hi, im.lo)
-  const DevInst& S = st[chunk_inst[blockIdx.x]];
+  // per warp: (re.hi, re.lo, im.hi, im.lo) of each basis column (at most kBatchMaxKrylov + 1);
+  // sized to the engine's Krylov limit so the block stays inside 48 KB of static shared memory
+  __shared__ float4 red[kBatchMaxKrylov + 2][kRT / 32];
+  const int inst = chunk_inst[blockIdx.x];
+  DevInst& S = st[inst];
   if (S.done) return;
   const int nv = S.j + 1;
+  if (npart1 != nullptr) {
+    const bool reorth = job_norm2(S, nchunks[inst], npart1) < 0.5 * S.image2;  // block-uniform
+    if (blockIdx.x == S.chunk_begin && threadIdx.x == 0) S.reorth = reorth ? 1 : 0;
+    if (!reorth) {
+      for (int kk = threadIdx.x; kk < nv; kk += blockDim.x)
+        partv[(long long)blockIdx.x * kMaxDots + kk] = make_double2(0.0, 0.0);
+      return;
+    }
+  }
   long long beg, end;
   pair_range(S, blockIdx.x, beg, end);
   const int npair = (int)(end - beg);
@@ -682,7 +701,7 @@ __global__ void __launch_bounds__(kRT, 3)
     wsm[p] = wv;
     if (p < npair) df_add(nrm, fmaf(wv.x, wv.x, fmaf(wv.y, wv.y, fmaf(wv.z, wv.z, wv.w * wv.w))));
   }
-  if (ipart != nullptr && !S.givens) {  // block-uniform
+  if (ipart != nullptr) {  // block-uniform
     const double r = block_df_sum(nrm, reinterpret_cast<float2*>(&red[0][0]));
     if (threadIdx.x == 0) ipart[blockIdx.x] = r;
   }
@@ -798,13 +817,19 @@ __global__ void __launch_bounds__(kRT)
 
 // w -= sum_i V_i h_i for an FP32 basis (which 0: hA, 1: hB), FP32 update; with part also
 // the double-float |w|^2 partial of the result.
+// With npart1 (second pass under selective reorthogonalisation) a job that skipped the second
+// projection keeps w and forwards its first-pass |w1|^2 partials as this pass's partials.
 __global__ void __launch_bounds__(kRT)
     k_step_maxpy_f32(const DevInst* __restrict__ st, const int* __restrict__ chunk_inst, int which,
-                     double* __restrict__ part) {
+                     double* __restrict__ part, const double* __restrict__ npart1) {
   __shared__ float2 hs[kMaxDots];
   __shared__ float2 smem[32];
   const DevInst& S = st[chunk_inst[blockIdx.x]];
   if (S.done) return;
+  if (npart1 != nullptr && !S.reorth) {
+    if (threadIdx.x == 0) part[blockIdx.x] = npart1[blockIdx.x];
+    return;
+  }
   const int nv = S.j + 1;
   const double2* h = which == 0 ? S.hA : S.hB;
   for (int i = threadIdx.x; i < nv; i += blockDim.x) hs[i] = make_float2((float)h[i].x, (float)h[i].y);
@@ -1743,26 +1768,33 @@ void Engine::arnoldi_step() {
   if (f32_) {
     if (any_border_) launch(k_step_trace<float2>, n, kRT, 0, st);
     launch(k_bapply<float, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(float2), (const DevInst*)st, ti, tl);
-    // first-pass projections; expv cycles also take the image norm |w|^2 from this sweep
+    // CGS with selective reorthogonalisation: the first pass also takes the image norm
+    // |w0|^2 (every job) and the first update the |w1|^2 partials (second half of part);
+    // the second pass runs only for jobs whose first projection removed more than half of
+    // |w0|^2 (k_step_mdot_f32)
+    double* npart1 = part + C;
+    const int* ncn = nullptr;
+    const double* npn = nullptr;
     if (chunk_ == kBatchChunk)
-      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv, part);
+      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, st, ci, partv, part, ncn, npn);
     else
-      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv, part);
-    launch(k_step_first_final, gfirst, kRT, 0, st, nc, (const double2*)partv, (const double*)part);
-    launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 0, none);
+      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, st, ci, partv, part, ncn, npn);
+    launch(k_step_first_final, gfirst, kRT, 0, st, nc, (const double2*)partv, (const double*)part, 1);
+    launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 0, npart1, npn);
+    double* noi = nullptr;
     if (chunk_ == kBatchChunk)
-      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, (const DevInst*)st, ci, partv, none);
+      launch(k_step_mdot_f32<kBatchChunk>, C, kRT, 0, st, ci, partv, noi, nc, (const double*)npart1);
     else
-      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, (const DevInst*)st, ci, partv, none);
+      launch(k_step_mdot_f32<kBatchChunkSmall>, C, kRT, 0, st, ci, partv, noi, nc, (const double*)npart1);
     launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);
-    launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 1, part);
+    launch(k_step_maxpy_f32, C, kRT, 0, (const DevInst*)st, ci, 1, part, (const double*)npart1);
     launch(k_step_normalize_f32, C, kRT, 0, st, ci, nc, (const double*)part);
   } else {
     if (any_border_) launch(k_step_trace<double2>, n, kRT, 0, st);
     launch(k_bapply<double, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(double2), (const DevInst*)st, ti, tl);
     launch(k_step_image_partial<double2>, C, kRT, 0, (const DevInst*)st, ci, part);
     launch(k_step_mdot_partial<double2, false>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
-    launch(k_step_first_final, gfirst, kRT, 0, st, nc, (const double2*)partv, (const double*)part);
+    launch(k_step_first_final, gfirst, kRT, 0, st, nc, (const double2*)partv, (const double*)part, 0);
     launch(k_step_maxpy<double2>, C, kRT, 0, (const DevInst*)st, ci, 0, none);
     launch(k_step_mdot_partial<double2, false>, gmd, kRT, 0, (const DevInst*)st, ci, partv);
     launch(k_step_mdot_final, gfin, kRT, 0, (const DevInst*)st, nc, (const double2*)partv, 1);

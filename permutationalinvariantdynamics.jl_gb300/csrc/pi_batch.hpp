@@ -82,6 +82,7 @@ struct DevInst {
   int j;         // input column of the next step
   int done;      // no further steps this cycle
   int kdone;     // completed steps
+  int reorth;    // FP32 basis: this step's second CGS projection ran (selective reorthogonalisation)
   double scale;  // multiplies L V_j
   double tol;    // GMRES: stop when |g[j+1]| <= tol
   double rem2;
