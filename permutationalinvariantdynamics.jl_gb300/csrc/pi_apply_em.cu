@@ -751,6 +751,18 @@ static int em_prepare_split(pi_plan* plan, int which, pi_plan::EmSplit* out) {
   return PI_OK;
 }
 
+int em_split_planes(pi_plan* plan, int which, SplitPlanes* out) {
+  pi_plan::EmSplit sp;
+  const int rc = em_prepare_split(plan, which, &sp);
+  if (rc) return rc;
+  out->eplane = sp.eplane;
+  out->lrow = sp.lrow;
+  out->rcol = sp.rcol;
+  out->line_off = plan->em_line_off;
+  out->plus = plan->dev.canon_plus ? 1 : 0;
+  return PI_OK;
+}
+
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link-time dependency on
 // the driver library); nullptr when the driver does not provide it.
 static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {

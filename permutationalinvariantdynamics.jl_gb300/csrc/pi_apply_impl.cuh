@@ -117,31 +117,18 @@ struct StoreSink {
   __device__ __forceinline__ void operator()(long long e, T2 v) const { y[e] = v; }
 };
 
-// One 32 x 32 output tile of scale * (L x) (+ alpha * v on the diagonal) for the sector
-// block `tile`: stage the source windows and the sector's grouped terms in shared memory,
-// then evaluate every stencil term and hand each output entry, with its element index, to
-// `sink` (a plain store, or a fused epilogue such as an RK4 stage update).  `alpha` is the
-// device trace value of this column (or nullptr).  Shared by the single-plan and the
-// multi-instance kernels.
-template <typename T, typename Sink>
-__device__ __forceinline__ void apply_tile_to(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
-                                              const typename Vec2<T>::type* __restrict__ coef, const DevTile tile,
-                                              const typename Vec2<T>::type* __restrict__ x, const Sink& sink,
-                                              const BorderArgs& border, const double2* alpha,
-                                              typename Vec2<T>::type* win, int4* st, int* ge) {
+// Stages the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every source
+// sector (e = -1, 0, +1) of `tile` into win (slot e + 1): lane = window row (plus rows 32..35
+// on lanes 0..3), warps stride over the 36 window columns.  Every element is one
+// asynchronous copy with hardware zero fill (cp.async), so all of a thread's ~30 copies are
+// in flight at once and the block waits for memory once, not once per window column.
+template <typename T>
+__device__ __forceinline__ void stage_windows(const DevSector* __restrict__ sectors, const DevSector& sec,
+                                              const DevTile tile, const typename Vec2<T>::type* __restrict__ x,
+                                              typename Vec2<T>::type* win) {
   using T2 = typename Vec2<T>::type;
-  const DevSector& sec = sectors[tile.sector];
-  const int tb = sec.term_begin;
-  const int nt = sec.group_end[G_COUNT - 1] - tb;
-  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
-  if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
   const int la = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
-  // Stage the zero-padded windows x_src[a0+e-2 .. a0+e+33, b0+e-2 .. b0+e+33] of every
-  // source sector (e = -1, 0, +1): lane = window row (plus rows 32..35 on lanes 0..3),
-  // warps stride over the 36 window columns.  Every element is one asynchronous copy with
-  // hardware zero fill (cp.async), so all of a thread's ~30 copies are in flight at once
-  // and the block waits for memory once, not once per window column.
   const bool extra = la < kWinRows - 32;
 #pragma unroll 1
   for (int slot = 0; slot < 3; ++slot) {
@@ -165,6 +152,29 @@ __device__ __forceinline__ void apply_tile_to(const DevSector* __restrict__ sect
   cp_async_commit();
   cp_async_wait<0>();
   __syncthreads();
+}
+
+// One 32 x 32 output tile of scale * (L x) (+ alpha * v on the diagonal) for the sector
+// block `tile`: stage the source windows and the sector's grouped terms in shared memory,
+// then evaluate every stencil term and hand each output entry, with its element index, to
+// `sink` (a plain store, or a fused epilogue such as an RK4 stage update).  `alpha` is the
+// device trace value of this column (or nullptr).  Shared by the single-plan and the
+// multi-instance kernels.
+template <typename T, typename Sink>
+__device__ __forceinline__ void apply_tile_to(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
+                                              const typename Vec2<T>::type* __restrict__ coef, const DevTile tile,
+                                              const typename Vec2<T>::type* __restrict__ x, const Sink& sink,
+                                              const BorderArgs& border, const double2* alpha,
+                                              typename Vec2<T>::type* win, int4* st, int* ge) {
+  using T2 = typename Vec2<T>::type;
+  const DevSector& sec = sectors[tile.sector];
+  const int tb = sec.term_begin;
+  const int nt = sec.group_end[G_COUNT - 1] - tb;
+  for (int i = threadIdx.x; i < nt; i += blockDim.x) st[i] = reinterpret_cast<const int4*>(terms)[tb + i];
+  if (threadIdx.x <= G_COUNT) ge[threadIdx.x] = threadIdx.x == 0 ? 0 : sec.group_end[threadIdx.x - 1] - tb;
+  stage_windows<T>(sectors, sec, tile, x, win);
+  const int la = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int n = sec.n;
   const int lb = warp * kColsPerThread;
   const int a = tile.a0 + la;
@@ -208,6 +218,90 @@ __device__ __forceinline__ void apply_tile_to(const DevSector* __restrict__ sect
       out.y += (T)(al.y * v);
     }
     sink(e0 + (long long)k * n, out);
+  }
+}
+
+
+__device__ __forceinline__ void pmac(float2& acc, float cr, float ci, float2 v) {
+  acc.x = fmaf(cr, v.x, acc.x);
+  acc.x = fmaf(-ci, v.y, acc.x);
+  acc.y = fmaf(cr, v.y, acc.y);
+  acc.y = fmaf(ci, v.x, acc.y);
+}
+__device__ __forceinline__ void prmac(float2& acc, float c, float2 v) {
+  acc.x = fmaf(c, v.x, acc.x);
+  acc.y = fmaf(c, v.y, acc.y);
+}
+
+// The 32 x 32 FP32 tile of apply_tile_to for a canonical plan with its merged coefficients
+// read from the split planes: per output entry two coalesced 16-byte entry-plane loads (the
+// row and column values are shared) and ten staged source reads, instead of forming every
+// stencil term's coefficient product.  A merged position reads the staged window of slot
+// e + 1 at offset p + 36 q (x_src[a + e + p, b + e + q]); the window of a missing neighbour
+// sector is not staged (stale shared memory), so its positions are skipped, not multiplied
+// by their zero coefficients.
+template <bool PLUS, typename Sink>
+__device__ __forceinline__ void apply_tile_planes_to(const DevSector* __restrict__ sectors, const DevTile tile,
+                                                     const float2* __restrict__ x, const Sink& sink,
+                                                     const BorderArgs& border, const double2* alpha,
+                                                     const SplitPlanes& pl, float2* win) {
+  constexpr int NE = PLUS ? 3 : 2;
+  const DevSector& sec = sectors[tile.sector];
+  stage_windows<float>(sectors, sec, tile, x, win);
+  const int la = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int n = sec.n;
+  const int lb = warp * kColsPerThread;
+  const int a = tile.a0 + la;
+  const int b0 = tile.b0 + lb;
+  if (a >= n || b0 >= n) return;
+  const int ncol = min(kColsPerThread, n - b0);
+  const int loff = __ldg(pl.line_off + tile.sector);
+  const float4 lv = __ldg(pl.lrow + loff + a);  // LEFT -1, +1 of row a
+  const float2* wb = win + (la + kHalo) + (lb + kHalo) * kWinRows;
+  const long long e0 = sec.offset + a + (long long)b0 * n;
+  const float scale = (float)border.scale;
+  const bool has_sm = sec.src[0] >= 0, has_lg = sec.src[2] >= 0;  // block-uniform
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) {
+    if (k >= ncol) break;
+    const float4* ep = pl.eplane + (e0 + (long long)k * n) * NE;
+    const float4 c0 = __ldg(ep), c1 = __ldg(ep + 1);
+    const float4 rc = __ldg(pl.rcol + loff + b0 + k);  // RIGHT -1, +1 of column b
+    const float2* w = wb + k * kWinRows;
+    const float2* own = w + kWinElems;
+    float2 acc = make_float2(0.f, 0.f);
+    pmac(acc, c0.x, c0.y, own[0]);                      // centre
+    pmac(acc, lv.x, lv.y, own[-1]);                     // LEFT -1
+    pmac(acc, lv.z, lv.w, own[1]);                      // LEFT +1
+    pmac(acc, rc.x, rc.y, own[-kWinRows]);              // RIGHT -1
+    pmac(acc, rc.z, rc.w, own[kWinRows]);               // RIGHT +1
+    prmac(acc, c0.z, own[-1 - kWinRows]);               // own (-1,-1)
+    if (has_sm) {
+      prmac(acc, c0.w, w[-1 - kWinRows]);               // smaller (-2,-2)
+      prmac(acc, c1.x, w[0]);                           // smaller (-1,-1)
+    }
+    if (has_lg) {
+      prmac(acc, c1.y, w[2 * kWinElems - 1 - kWinRows]);  // larger (0,0)
+      prmac(acc, c1.z, w[2 * kWinElems]);                 // larger (1,1)
+    }
+    if (PLUS) {
+      const float4 c2 = __ldg(ep + 2);
+      prmac(acc, c1.w, own[1 + kWinRows]);                  // own (1,1)
+      if (has_sm) prmac(acc, c2.x, w[1 + kWinRows]);        // smaller (0,0)
+      if (has_lg) prmac(acc, c2.y, w[2 * kWinElems + 1 + kWinRows]);  // larger (2,2)
+    }
+    if (border.scale != 1.0) {
+      acc.x *= scale;
+      acc.y *= scale;
+    }
+    if (b0 + k == a && alpha != nullptr) {
+      const double2 al = *alpha;
+      const double v = border.coords ? sec.border_z : sec.border_x;
+      acc.x += (float)(al.x * v);
+      acc.y += (float)(al.y * v);
+    }
+    sink(e0 + (long long)k * n, acc);
   }
 }
 

@@ -191,8 +191,19 @@ __global__ void __launch_bounds__(kApplyThreads)
     if (S.done) return;
     const DevTile tile = S.tiles[tile_local[blockIdx.x]];
     BorderArgs b{S.scale, nullptr, S.coords};
-    apply_tile<T>(S.sectors, S.terms, (const T2*)S.coefb, tile, (const T2*)S.V + (long long)S.j * S.ldv, (T2*)S.w, b,
-                  S.border ? &S.alpha : nullptr, win, sterms, ge);
+    const T2* xin = (const T2*)S.V + (long long)S.j * S.ldv;
+    if constexpr (sizeof(T) == sizeof(float)) {
+      if (S.planes.eplane != nullptr && S.coords == S.pwhich) {  // block-uniform
+        const StoreSink<float2> sink{(float2*)S.w};
+        if (S.planes.plus)
+          apply_tile_planes_to<true>(S.sectors, tile, xin, sink, b, S.border ? &S.alpha : nullptr, S.planes, win);
+        else
+          apply_tile_planes_to<false>(S.sectors, tile, xin, sink, b, S.border ? &S.alpha : nullptr, S.planes, win);
+        return;
+      }
+    }
+    apply_tile<T>(S.sectors, S.terms, (const T2*)S.coefb, tile, xin, (T2*)S.w, b, S.border ? &S.alpha : nullptr, win,
+                  sterms, ge);
   }
 }
 
@@ -1684,6 +1695,12 @@ void Engine::rebuild() {
     d.ndiag = dp.ndiag;
     d.chunk_begin = (int)ci.size();
     d.chunk = chunk_;
+    // FP32 Arnoldi applies of canonical plans read merged coefficients: dynamics cycles run in
+    // population coordinates, steady-state cycles in reference coordinates
+    d.planes = SplitPlanes{nullptr, nullptr, nullptr, nullptr, 0};
+    d.pwhich = J->bordered ? 0 : 1;
+    if (f32_ && dp.canon && em_split_planes(J->plan, d.pwhich, &d.planes) != PI_OK)
+      d.planes = SplitPlanes{nullptr, nullptr, nullptr, nullptr, 0};
     for (int c = 0; c < nc[i]; ++c) ci.push_back(i);
     d.V = J->V;
     d.w = J->w;

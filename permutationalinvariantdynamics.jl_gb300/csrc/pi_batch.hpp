@@ -83,6 +83,10 @@ struct DevInst {
   int done;      // no further steps this cycle
   int kdone;     // completed steps
   int reorth;    // FP32 basis: this step's second CGS projection ran (selective reorthogonalisation)
+  // FP32 basis, canonical plan: merged coefficients of the Arnoldi applies in the coordinate
+  // system pwhich (eplane == nullptr: the generic stencil terms)
+  SplitPlanes planes;
+  int pwhich;
   double scale;  // multiplies L V_j
   double tol;    // GMRES: stop when |g[j+1]| <= tol
   double rem2;

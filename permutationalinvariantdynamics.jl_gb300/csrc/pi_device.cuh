@@ -71,4 +71,16 @@ struct BorderArgs {
   int coords;              // 0: x coordinates (border_x), 1: population coordinates (border_z)
 };
 
+// Split coefficient planes of a plan whose stencil sits at the canonical positions (built by
+// the element-major apply): per entry (centre re, centre im, own (-1,-1), smaller (-2,-2)),
+// (smaller (-1,-1), larger (0,0), larger (1,1), own (1,1)) [, (smaller (0,0), larger (2,2))];
+// per row (LEFT -1, LEFT +1); per column (RIGHT -1, RIGHT +1).
+struct SplitPlanes {
+  const float4* eplane;
+  const float4* lrow;
+  const float4* rcol;
+  const int* line_off;  // per sector: start of its row and column planes
+  int plus;             // three entry float4 (pumping terms at the +1 diagonal shifts)
+};
+
 }  // namespace picuda

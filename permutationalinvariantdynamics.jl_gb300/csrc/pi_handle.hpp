@@ -94,4 +94,9 @@ struct BusyGuard {
 // Device allocation tracked by the plan; returns nullptr on failure.
 void* plan_alloc(pi_plan* plan, size_t bytes);
 
+// Split coefficient planes of a canonical plan in reference (which 0) or population (which 1)
+// FP32 coordinates, built on first use (pi_apply_em.cu); PI_ERR_UNSUPPORTED for a plan whose
+// stencil does not sit at the canonical positions.
+int em_split_planes(pi_plan* plan, int which, SplitPlanes* out);
+
 }  // namespace picuda
