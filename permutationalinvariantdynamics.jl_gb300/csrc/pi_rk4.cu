@@ -49,6 +49,7 @@ struct Rk4Params {
   void* ta;        // stage inputs: double2 (FP64) or float2 (mixed)
   void* tb;
   const double* h; // step size (device)
+  SplitPlanes planes;  // mixed, canonical plan: merged population-coordinate coefficients
 };
 
 // Epilogue of one FP64 RK4 stage for output entry e with stage derivative k = (L input)[e].
@@ -151,6 +152,13 @@ __global__ void __launch_bounds__(kApplyThreads) k_rk4_stage_mixed(Rk4Params p) 
   const Rk4SinkDF<STAGE> sink{(float2*)p.dest, p.dlo, (float2*)p.acc, next, (float)(STAGE == 2 ? h : h / 2), c6_hi,
                               (float)(h6 - (double)c6_hi)};
   const BorderArgs none{1.0, nullptr, 1};
+  if (p.planes.eplane != nullptr) {  // merged coefficients: ten staged reads per entry
+    if (p.planes.plus)
+      apply_tile_planes_to<true>(p.sectors, p.tiles[blockIdx.x], x, sink, none, nullptr, p.planes, win);
+    else
+      apply_tile_planes_to<false>(p.sectors, p.tiles[blockIdx.x], x, sink, none, nullptr, p.planes, win);
+    return;
+  }
   apply_tile_to<float>(p.sectors, p.terms, (const float2*)p.coef, p.tiles[blockIdx.x], x, sink, none, nullptr, win,
                        st, ge);
 }
@@ -308,8 +316,11 @@ int rk4_run(pi_plan* plan, double2* rho, int nt, const double* times, int steps,
     const int reps = steps / gsteps, rem = steps % gsteps;
     StepGraph main, tail;
     // Only the step size changes between intervals: the graphs read it from hcur.
+    SplitPlanes planes{nullptr, nullptr, nullptr, nullptr, 0};
+    if (mixed && dp.canon && em_split_planes(plan, 1, &planes) != PI_OK)
+      planes = SplitPlanes{nullptr, nullptr, nullptr, nullptr, 0};
     const Rk4Params prm{dp.sectors, dp.terms, mixed ? (const void*)dp.coef32z : (const void*)dp.coef64, dp.tiles,
-                        dest, dlo, acc, ta, tb, hcur};
+                        dest, dlo, acc, ta, tb, hcur, planes};
     const size_t smem = 3 * kWinElems * es;
     if (err == cudaSuccess && dp.ntiles > 0) {
       chk(main.build(k, prm, dp.ntiles, smem, gsteps));
