@@ -19,15 +19,19 @@
 //     neighbouring sector.
 //
 // Two kernels implement this:
-//   - k_apply_em_tma (default): the sources are staged in shared memory by the Tensor
-//     Memory Accelerator.  Every sector block of the batch is a 3-D tensor (right-hand side,
-//     row, column) with its own tensor map, so one cp.async.bulk.tensor per row step and
-//     source sector brings the 10 staged columns of a block's 8 output columns, and rows or
-//     columns outside the sector block arrive as zeros from the hardware (no bounds checks).
-//     A producer thread keeps a ring of row steps in flight ahead of the 8 consumer warps
+//   - k_apply_em_tma: the sources are staged in shared memory by the Tensor Memory
+//     Accelerator.  Every sector block of the batch is a 3-D tensor (right-hand side, row,
+//     column) with its own tensor map, so one cp.async.bulk.tensor per row step and source
+//     sector brings the 10 staged columns of a block's 8 output columns, and rows or columns
+//     outside the sector block arrive as zeros from the hardware (no bounds checks).  A
+//     producer thread keeps a ring of row steps in flight ahead of the 8 consumer warps
 //     (full/empty mbarriers), so no warp holds loads in registers to hide memory latency.
-//   - k_apply_em_f32: the same stencil with plain coalesced loads from global memory, for
-//     plans with more sectors than the kernel-parameter map table holds.
+//     Tiles of 16, 32 or 64 rows.
+//   - k_apply_em_f32: the same stencil with plain coalesced loads from global memory; the
+//     only kernel for plans with more sectors than the kernel-parameter map table holds.
+// Every candidate computes each output entry with the same operations in the same order, so
+// the autotuner (em_tune) may pick any of them per batch width by timing: the first call
+// times them on the caller's batch and later calls launch the fastest.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
