@@ -439,12 +439,15 @@ class ClockSampler:
 
 
 def dist_setup():
+    """One process per GPU (torchrun): NCCL on GPUs, gloo where CUDA is absent (the CPU tests
+    of the replica path)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     return world, rank, local
 
 
@@ -459,9 +462,17 @@ def max_over_ranks(value, world):
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(bytes_per_rank, ms_per_step, world):
+    """Whole-job throughput of independent replicas (weak scaling): every rank processes
+    bytes_per_rank per step, and the job takes the slowest rank's time (max over ranks)."""
+    ms = max_over_ranks(ms_per_step, world)
+    return world * bytes_per_rank / (ms * 1e-3) / 1e9, ms
 
 
 def stencil_flops(picuda, model):
@@ -645,9 +656,8 @@ def main():
         torch.cuda.synchronize()
     barrier(world)
     ms = e0.elapsed_time(e1) / args.steps
-    ms = max_over_ranks(ms, world)
     bytes32 = 2 * 8 * n * BATCH
-    value = world * bytes32 / (ms * 1e-3) / 1e9
+    value, ms = replica_throughput(bytes32, ms, world)
     peak, peak_kind = measured_peaks()
     achieved = bytes32 / (ms * 1e-3) / 1e9
 
