@@ -139,3 +139,18 @@ def test_adjoint_stencil_is_the_conjugate_transpose(name, make):
         y_ref = LH @ x
         y = evaluate(model.basis, table, coef, x)
         assert np.abs(y - y_ref).max() <= 1e-13 * np.abs(y_ref).max(), name
+
+
+def test_element_major_entry_points_reject_null_arguments():
+    """The element-major apply and its tuning entry points validate arguments on the host
+    before any device work."""
+    import ctypes as C
+
+    from picuda import _lib
+    lib = picuda.load_library()
+    kind, rows, ms = C.c_int(), C.c_int(), C.c_double()
+    assert lib.pi_apply_f32_em_tuning(None, 128, 1, C.byref(kind), C.byref(rows), C.byref(ms)) == \
+        _lib.PI_ERR_INVALID_ARGUMENT
+    assert lib.pi_apply_f32_em_select(None, 128, 1, 0, 32) == _lib.PI_ERR_INVALID_ARGUMENT
+    assert lib.pi_apply_f32_em(None, None, None, 128, 128, 1, None) == _lib.PI_ERR_INVALID_ARGUMENT
+    assert "null" in _lib.last_error()
