@@ -925,11 +925,22 @@ static std::vector<EmCand> em_candidates(const pi_plan* plan) {
 
 // Autotuner: the first call for a batch width and coordinate system runs every candidate on
 // the caller's batch (all compute each output entry with the same operations, so y is the
-// same whichever runs), times two rounds of them with CUDA events on the caller's stream,
-// waits for that stream once, and keeps the fastest for later calls.
+// same whichever runs; a candidate that fails to launch drops out), times two rounds of the
+// rest with CUDA events on the caller's stream, waits for that stream once, and keeps the
+// fastest for later calls.
 static int em_tune(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, long long ld, int coords,
                    cudaStream_t s, pi_plan::EmChoice* out) {
-  const std::vector<EmCand> cands = em_candidates(plan);
+  // a candidate that cannot run on this batch (its tensor maps do not encode, say) drops out
+  std::vector<EmCand> cands;
+  int first_rc = PI_OK;
+  for (const EmCand& c : em_candidates(plan)) {
+    const int rc = em_run(plan, c, y_dev, x_dev, ncols, ld, coords, s);
+    if (rc == PI_OK)
+      cands.push_back(c);
+    else if (first_rc == PI_OK)
+      first_rc = rc;
+  }
+  if (cands.empty()) return first_rc;
   std::vector<cudaEvent_t> ev(2 * cands.size() * 2, nullptr);
   for (auto& e : ev)
     if (cudaEventCreate(&e) != cudaSuccess) {
@@ -938,7 +949,6 @@ static int em_tune(pi_plan* plan, float* y_dev, const float* x_dev, int ncols, l
       return cuda_fail(cudaGetLastError(), "autotuner events");
     }
   int rc = PI_OK;
-  for (size_t i = 0; i < cands.size() && !rc; ++i) rc = em_run(plan, cands[i], y_dev, x_dev, ncols, ld, coords, s);
   for (int round = 0; round < 2 && !rc; ++round)
     for (size_t i = 0; i < cands.size() && !rc; ++i) {
       cudaEventRecord(ev[(round * cands.size() + i) * 2], s);
