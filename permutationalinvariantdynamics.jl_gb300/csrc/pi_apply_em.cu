@@ -368,13 +368,14 @@ __global__ void __launch_bounds__(32 * kEmWarps, 4)
 // ---------------------------------------------------------------------------------------
 // TMA-staged kernel.
 //
-// Block = one tile (32 rows x 8 columns of one sector block) and one half of the batch row
-// (64 complex right-hand sides = 512 bytes).  Row step k stages, in one ring slot:
+// Block = one tile (16, 32 or 64 rows x 8 columns of one sector block) and one half of the
+// batch row (64 complex right-hand sides = 512 bytes).  Row step k stages, in one ring slot:
 //   source 0: smaller sector, row k-1, columns b0-2 .. b0+7
 //   source 1: own sector,     row k,   columns b0-1 .. b0+8
 //   source 2: larger sector,  row k+1, columns b0   .. b0+9
-// so output row a reads exactly the slots of steps a-1, a, a+1 and is the last reader of
-// step a-1.  A tile of R rows takes R + 2 steps (a0-1 .. a0+R).
+// so output row a reads the slots of steps a-1, a and a+1; a consumer warp reads each step's
+// own row when it lands and its neighbour columns one row later, then releases the slot.  A
+// tile of R rows takes R + 2 steps (a0-1 .. a0+R).
 constexpr int kTmW = kEmWarps;                      // consumer warps = output columns
 constexpr int kTmCols = kTmW + 2;                   // staged columns per source sector
 constexpr int kTmHalf = 64;                         // complex right-hand sides per block
