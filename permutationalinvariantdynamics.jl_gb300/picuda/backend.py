@@ -368,10 +368,14 @@ def element_major_tuning(compiled: CompiledPIModel, ncols, coords="population"):
 def select_element_major_kernel(compiled: CompiledPIModel, ncols, kernel="tma", rows=32, coords="population"):
     """Pins the element-major kernel for a batch width and coordinate system instead of
     autotuning it: kernel "tma" (tile rows 16, 32 or, without pumping terms, 64) or "plain"."""
+    kinds = {v: k for k, v in EM_KERNELS.items()}
+    if kernel not in kinds:
+        raise PiArgumentError(f"element-major kernel must be one of {sorted(kinds)}, got {kernel!r}")
+    if coords not in ("population", "reference"):
+        raise PiArgumentError(f"coords must be 'population' or 'reference', got {coords!r}")
     lib = _lib.load()
     cc = _lib.PI_COORDS_POPULATION if coords == "population" else _lib.PI_COORDS_REFERENCE
-    kind = {v: k for k, v in EM_KERNELS.items()}[kernel]
-    _lib.check(lib.pi_apply_f32_em_select(compiled.handle, int(ncols), cc, kind, int(rows)),
+    _lib.check(lib.pi_apply_f32_em_select(compiled.handle, int(ncols), cc, kinds[kernel], int(rows)),
                "element-major kernel choice")
 
 

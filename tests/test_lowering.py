@@ -154,3 +154,10 @@ def test_element_major_entry_points_reject_null_arguments():
     assert lib.pi_apply_f32_em_select(None, 128, 1, 0, 32) == _lib.PI_ERR_INVALID_ARGUMENT
     assert lib.pi_apply_f32_em(None, None, None, 128, 128, 1, None) == _lib.PI_ERR_INVALID_ARGUMENT
     assert "null" in _lib.last_error()
+
+
+def test_element_major_kernel_choice_validates_names():
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.select_element_major_kernel(object(), 128, "fastest")
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.select_element_major_kernel(object(), 128, "tma", 32, coords="spherical")
