@@ -1126,3 +1126,167 @@ def krylov_liouvillian_spectrum(A, n, nev=6, krylovdim=None, which="LR", initial
     if vectors:
         out["vectors"] = V[:, :k] @ Y
     return out
+
+
+def _mgs2(q, V, k):
+    """_orthogonalize! (krylov.jl:973-978): two modified Gram-Schmidt passes against the
+    first k columns of V; returns |q|."""
+    for _ in range(2):
+        for i in range(k):
+            q -= np.vdot(V[:, i], q) * V[:, i]
+    return np.linalg.norm(q)
+
+
+def _orthonormalize_columns(R, ncols):
+    """_orthonormalize_columns! (krylov.jl:980-995): two-pass Gram-Schmidt over the columns,
+    dropping those whose norm falls to sqrt(eps) of their initial norm; returns the count
+    kept in the leading columns."""
+    kept = 0
+    threshold = np.sqrt(np.finfo(float).eps)
+    for j in range(ncols):
+        col = R[:, j].copy()
+        initial = np.linalg.norm(col)
+        for _ in range(2):
+            for i in range(kept):
+                col -= np.vdot(R[:, i], col) * R[:, i]
+        beta = np.linalg.norm(col)
+        if beta <= threshold * max(initial, np.finfo(float).tiny):
+            continue
+        R[:, kept] = col / beta
+        kept += 1
+    return kept
+
+
+def harmonic_arnoldi_spectrum(A, n, nev=6, krylovdim=None, thickdim=None, maxrestarts=20, target=0.0,
+                              initial_vector=None, initial_subspace=None, atol=1e-10, rtol=1e-8,
+                              vectors=False, rng=None, require_convergence=True):
+    """harmonic_arnoldi_spectrum without a projector (krylov.jl:1378-1551): thick-restarted
+    Arnoldi whose Ritz pairs come from the harmonic pencil (Z^H Z, Z^H V), Z = L V - sigma V,
+    sigma = target, or -max(sqrt(eps) * scale, atol) for target 0 (scale = the largest
+    basis-image norm).  Once the basis spans the whole space (k == n) the extraction is
+    ordinary Rayleigh-Ritz on V^H L V.  Pairs are ordered by distance to the target; the
+    converged pairs plus the nearest others (up to thickdim) seed the next cycle."""
+    eps = np.finfo(float).eps
+    tiny = np.finfo(float).tiny
+    if not (0 < nev <= n):
+        raise ValueError("nev must lie between 1 and the operator dimension")
+    if maxrestarts < 0:
+        raise ValueError("maxrestarts must be nonnegative")
+    krylovdim = max(30, 3 * nev + 6) if krylovdim is None else krylovdim
+    thickdim = max(nev + 2, 2 * nev) if thickdim is None else thickdim
+    m = min(n, max(krylovdim, nev + 2))
+    keep = min(m - 1, max(thickdim, nev))
+    if initial_vector is not None and initial_subspace is not None:
+        raise ValueError("initial_vector and initial_subspace are mutually exclusive")
+    rng = rng if rng is not None else np.random.default_rng(0)
+
+    def randn():
+        return (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+
+    breakfactor = np.sqrt(eps)
+    V = np.zeros((n, m), dtype=np.complex128)
+    LV = np.zeros((n, m), dtype=np.complex128)
+    nkeep = 0
+    if initial_subspace is not None:
+        S = np.asarray(initial_subspace, dtype=np.complex128)
+        for column in range(min(S.shape[1], keep)):
+            q = S[:, column].copy()
+            seednorm = np.linalg.norm(q)
+            beta = _mgs2(q, V, nkeep)
+            if beta <= breakfactor * max(seednorm, seednorm * eps, tiny):
+                continue
+            V[:, nkeep] = q / beta
+            nkeep += 1
+        if nkeep == 0:
+            raise ValueError("initial_subspace has no independent component in the selected symmetry sector")
+    else:
+        q = randn() if initial_vector is None else np.array(initial_vector, dtype=np.complex128)
+        nq = np.linalg.norm(q)
+        if not nq > breakfactor * max(nq, tiny):
+            raise ValueError("initial_vector has zero component in the selected symmetry sector")
+        V[:, 0] = q / nq
+        nkeep = 1
+    initial_retained = nkeep
+    applications = 0
+    best = None
+    history = []
+    requested = complex(target)
+    for cycle in range(maxrestarts + 1):
+        k = nkeep
+        for j in range(nkeep):
+            LV[:, j] = A(V[:, j])
+            applications += 1
+        while k < m:
+            q = LV[:, k - 1].copy()
+            image_norm = np.linalg.norm(q)
+            beta = _mgs2(q, V, k)
+            if beta <= breakfactor * max(image_norm, tiny):
+                q = randn()
+                seednorm = np.linalg.norm(q)
+                beta = _mgs2(q, V, k)
+                if beta <= breakfactor * max(seednorm, seednorm * eps, tiny):
+                    break
+            V[:, k] = q / beta
+            k += 1
+            LV[:, k - 1] = A(V[:, k - 1])
+            applications += 1
+        exhausted = k == n
+        Vk, LVk = V[:, :k], LV[:, :k]
+        scale = max(max(np.linalg.norm(LVk[:, j]) for j in range(k)), tiny)
+        sigma = complex(-max(np.sqrt(eps) * scale, atol)) if requested == 0 else requested
+        if exhausted:
+            lam, Y = sla.eig(Vk.conj().T @ LVk)
+        else:
+            Z = LVk - sigma * Vk
+            mu, Y = sla.eig(Z.conj().T @ Z, Z.conj().T @ Vk)
+            lam = sigma + mu
+        finite = np.flatnonzero(np.isfinite(lam.real) & np.isfinite(lam.imag))
+        if finite.size == 0:
+            raise ValueError("Ritz extraction returned no finite eigenvalues; enlarge krylovdim or change the "
+                             "initial vector")
+        order = finite[np.argsort(np.abs(lam[finite] - requested), kind="stable")]
+        sel = order[:min(nev, order.size)]
+        vals = lam[sel]
+        X = Vk @ Y[:, sel]
+        LX = LVk @ Y[:, sel]
+        nx = np.linalg.norm(X, axis=0)
+        X, LX = X / nx, LX / nx
+        residuals = np.linalg.norm(LX - X * vals, axis=0)
+        tol = atol + rtol * scale
+        converged = residuals <= tol
+        history.append(dict(cycle=cycle, subspace_dimension=k, locked=int(converged.sum()),
+                            maximum_residual=float(residuals.max()), residual_scale=scale,
+                            ritz_extraction="rayleigh_ritz" if exhausted else "harmonic",
+                            search_space_exhausted=exhausted))
+        best = dict(values=vals, residuals=residuals, converged=converged, restarts=cycle,
+                    iterations=applications, krylov_dimension=m, retained_dimension=keep,
+                    final_retained_dimension=nkeep, initial_retained_dimension=initial_retained,
+                    locked=int(converged.sum()), dimension=n, target=requested, harmonic_shift=sigma,
+                    algorithm="harmonic", ritz_extraction="rayleigh_ritz" if exhausted else "harmonic",
+                    search_space_exhausted=exhausted, residual_scale=scale, residual_tolerance=tol,
+                    restart_history=list(history))
+        if vectors:
+            best["vectors"] = X
+        if vals.size >= nev and converged.all():
+            return best
+        if exhausted:
+            if require_convergence:
+                raise ValueError("Rayleigh--Ritz extraction in the complete search space did not converge")
+            return best
+        if cycle == maxrestarts:
+            break
+        retain = [int(idx) for j, idx in enumerate(sel) if converged[j]]
+        for idx in order:
+            if int(idx) in retain:
+                continue
+            retain.append(int(idx))
+            if len(retain) >= min(keep, order.size):
+                break
+        R = Vk @ Y[:, retain]
+        nkeep = _orthonormalize_columns(R, len(retain))
+        if nkeep == 0:
+            raise ValueError("harmonic restart lost the retained invariant subspace")
+        V[:, :nkeep] = R[:, :nkeep]
+    if require_convergence:
+        raise ValueError("thick-restarted harmonic Arnoldi did not converge")
+    return best

@@ -7,8 +7,8 @@ libpicuda.so (include/picuda.h), whose sm_103a kernels do all numerical work.
 from ._lib import (PI_FP32, PI_FP64, PiArgumentError, PiDimensionMismatch, PiError, PiNotConverged,
                    load as load_library)
 from .backend import (AcceleratorCapability, CompiledPIModel, DynamicsResult, DynamicsStreamResult,
-                      ExpvAlgorithm, GMRESAlgorithm, SteadyStateResult, accelerator_capability, apply_, apply_adjoint_, apply_element_major_, element_major_tuning, select_element_major_kernel,
-                      compile, evolve_, krylov_expv, krylov_expv_batch, krylov_liouvillian_spectrum, mul, saved_times, solve_dynamics,
+                      ExpvAlgorithm, GMRESAlgorithm, HarmonicArnoldiAlgorithm, SteadyStateResult, accelerator_capability, apply_, apply_adjoint_, apply_element_major_, element_major_tuning, select_element_major_kernel,
+                      compile, evolve_, krylov_expv, krylov_expv_batch, krylov_liouvillian_spectrum, harmonic_arnoldi_spectrum, mul, saved_times, solve_dynamics,
                       solve_dynamics_batch, stationary_state, stationary_state_batch, steady_state,
                       stencil_tables, time_evolve)
 from .checkpoints import (PI_CHECKPOINT_VERSION, PIStateCheckpoint, checkpoint_state, load_checkpoint,

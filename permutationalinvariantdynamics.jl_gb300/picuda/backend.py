@@ -327,6 +327,318 @@ def krylov_liouvillian_spectrum(L, nev=6, krylovdim=None, which="LR", initial_ve
     return out
 
 
+# Vectors per pi_mdot_f64_noalloc call (the capacity of its static scratch) and the largest
+# basis pi_combine_f64 combines.
+_MDOT_VECTORS = 32
+_COMBINE_VECTORS = 128
+
+
+class _DeviceKrylovSpace:
+    """Vector storage and vector operations of the harmonic Arnoldi process on the GPU.
+
+    A block of m vectors is an (m, dim) complex128 CUDA tensor, one vector per row.  L x runs
+    through pi_apply_f64 and projections and norms through pi_mdot_f64_noalloc, both on
+    torch's current stream; basis combinations run through pi_combine_f64, which works on
+    the plan's own stream and returns after it finished, so the current stream is drained
+    before each combination."""
+
+    def __init__(self, compiled: CompiledPIModel, m: int):
+        self.torch = _torch()
+        self.compiled = compiled
+        self.n = len(compiled.basis)
+        self.lib = _lib.load()
+        self.h = self.torch.empty(max(m, 1), dtype=self.torch.complex128, device="cuda")
+        self.tmp = self.torch.empty(self.n, dtype=self.torch.complex128, device="cuda")
+
+    def block(self, m):
+        return self.torch.zeros((m, self.n), dtype=self.torch.complex128, device="cuda")
+
+    def upload(self, v):
+        return self.torch.from_numpy(np.ascontiguousarray(v, dtype=np.complex128)).cuda()
+
+    def copy(self, v):
+        return v.clone()
+
+    def download(self, rows):
+        """(dim, c) numpy array of the c rows."""
+        return rows.cpu().numpy().T.copy()
+
+    def apply(self, dst, src):
+        apply_(dst, self.compiled, src)
+
+    def _stream(self):
+        return C.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def _mdot(self, M, k, q):
+        for s in range(0, k, _MDOT_VECTORS):
+            c = min(_MDOT_VECTORS, k - s)
+            _lib.check(self.lib.pi_mdot_f64_noalloc(_ptr(M[s]), self.n, c, _ptr(q), self.n, _ptr(self.h[s:]),
+                                                    self._stream()), "harmonic_arnoldi_spectrum")
+
+    def dots(self, M, k, q):
+        """conj(M[i]) . q for i < k, as a numpy vector."""
+        self._mdot(M, k, q)
+        return self.h[:k].cpu().numpy()
+
+    def norm(self, q):
+        _lib.check(self.lib.pi_mdot_f64_noalloc(_ptr(q), self.n, 1, _ptr(q), self.n, _ptr(self.h), self._stream()),
+                   "harmonic_arnoldi_spectrum")
+        return float(np.sqrt(max(self.h[0].item().real, 0.0)))
+
+    def combine(self, M, k, Y):
+        """Rows sum_i Y[i, c] M[i] for the columns c of the k x c matrix Y."""
+        Yc = np.ascontiguousarray(np.asarray(Y, dtype=np.complex128).T)  # c x k row-major = k x c column-major
+        out = self.torch.empty((Yc.shape[0], self.n), dtype=self.torch.complex128, device="cuda")
+        self.torch.cuda.synchronize()
+        _lib.check(self.lib.pi_combine_f64(self.compiled.handle, _ptr(M), self.n, k, _lib.dptr(Yc.view(np.float64)),
+                                           Yc.shape[0], _ptr(out), self.n), "harmonic_arnoldi_spectrum")
+        return out
+
+    def subtract(self, q, M, k, coef):
+        """q -= sum_i coef[i] M[i]."""
+        c = np.ascontiguousarray(coef, dtype=np.complex128)
+        self.torch.cuda.synchronize()
+        _lib.check(self.lib.pi_combine_f64(self.compiled.handle, _ptr(M), self.n, k, _lib.dptr(c.view(np.float64)),
+                                           1, _ptr(self.tmp), self.n), "harmonic_arnoldi_spectrum")
+        q.sub_(self.tmp)
+
+
+def _orthogonalize(space, q, V, k):
+    """_orthogonalize! (krylov.jl:973-978): two Gram-Schmidt passes of q against the first
+    k basis vectors; returns |q|.  The passes are classical (one multi-dot and one
+    combination each) where the reference's are modified; two passes leave q orthogonal to
+    working precision either way."""
+    for _ in range(2):
+        if k:
+            space.subtract(q, V, k, space.dots(V, k, q))
+    return space.norm(q)
+
+
+def _orthonormalize_rows(space, R, ncols):
+    """_orthonormalize_columns! (krylov.jl:980-995): two-pass Gram-Schmidt over the vectors,
+    dropping those whose norm falls to sqrt(eps) of their initial norm; returns the count
+    kept in the leading rows."""
+    kept = 0
+    threshold = np.sqrt(np.finfo(float).eps)
+    for j in range(ncols):
+        col = space.copy(R[j])
+        initial = space.norm(col)
+        for _ in range(2):
+            if kept:
+                space.subtract(col, R, kept, space.dots(R, kept, col))
+        beta = space.norm(col)
+        if beta <= threshold * max(initial, np.finfo(float).tiny):
+            continue
+        R[kept] = col / beta
+        kept += 1
+    return kept
+
+
+def _harmonic_arnoldi(space, n, nev, krylovdim, thickdim, maxrestarts, target, initial_vector, initial_subspace,
+                      atol, rtol, vectors, rng, require_convergence):
+    """Thick-restarted harmonic Arnoldi without a projector (krylov.jl:1378-1551) over the
+    vector operations of `space`.  The full space is the projector range, so the basis
+    spanning it (k == dim) switches the extraction to ordinary Rayleigh-Ritz."""
+    import scipy.linalg as sla
+    eps = np.finfo(float).eps
+    tiny = np.finfo(float).tiny
+    m = min(n, max(krylovdim, nev + 2))
+    keep = min(m - 1, max(thickdim, nev))
+    breakfactor = np.sqrt(eps)
+
+    def randn():
+        return (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+
+    V = space.block(m)
+    LV = space.block(m)
+    nkeep = 0
+    if initial_subspace is not None:
+        for column in range(min(initial_subspace.shape[1], keep)):
+            q = space.upload(initial_subspace[:, column])
+            seednorm = space.norm(q)
+            beta = _orthogonalize(space, q, V, nkeep)
+            if beta <= breakfactor * max(seednorm, seednorm * eps, tiny):
+                continue
+            V[nkeep] = q / beta
+            nkeep += 1
+        if nkeep == 0:
+            raise PiArgumentError("initial_subspace has no independent component in the selected symmetry sector")
+    else:
+        q = space.upload(randn() if initial_vector is None else initial_vector)
+        nq = space.norm(q)
+        if not nq > breakfactor * max(nq, tiny):
+            raise PiArgumentError("initial_vector has zero component in the selected symmetry sector")
+        V[0] = q / nq
+        nkeep = 1
+    initial_retained = nkeep
+    applications = 0
+    history = []
+    best = None
+    X = None
+    requested = complex(target)
+    for cycle in range(maxrestarts + 1):
+        k = nkeep
+        # Images of the retained vectors are recomputed once per restart; the newest image
+        # continues the Krylov sequence.
+        for j in range(nkeep):
+            space.apply(LV[j], V[j])
+            applications += 1
+        while k < m:
+            q = space.copy(LV[k - 1])
+            image_norm = space.norm(q)
+            beta = _orthogonalize(space, q, V, k)
+            if beta <= breakfactor * max(image_norm, tiny):
+                q = space.upload(randn())
+                seednorm = space.norm(q)
+                beta = _orthogonalize(space, q, V, k)
+                if beta <= breakfactor * max(seednorm, seednorm * eps, tiny):
+                    break
+            V[k] = q / beta
+            k += 1
+            space.apply(LV[k - 1], V[k - 1])
+            applications += 1
+        exhausted = k == n
+        scale = max(max(space.norm(LV[j]) for j in range(k)), tiny)
+        # At an exact eigenvalue (the stationary zero mode) the harmonic pencil is singular;
+        # a shift of sqrt(eps) times the image scale makes it regular.
+        sigma = complex(-max(np.sqrt(eps) * scale, atol)) if requested == 0 else requested
+        A = np.empty((k, k), dtype=np.complex128)
+        if exhausted:
+            for j in range(k):
+                A[:, j] = space.dots(V, k, LV[j])
+            lam, Y = sla.eig(A)
+        else:
+            Z = LV[:k] - sigma * V[:k]
+            B = np.empty((k, k), dtype=np.complex128)
+            for j in range(k):
+                A[:, j] = space.dots(Z, k, Z[j])
+                B[:, j] = space.dots(Z, k, V[j])
+            del Z
+            mu, Y = sla.eig(A, B)
+            lam = sigma + mu
+        finite = np.flatnonzero(np.isfinite(lam.real) & np.isfinite(lam.imag))
+        if finite.size == 0:
+            raise PiArgumentError("Ritz extraction returned no finite eigenvalues; enlarge krylovdim or change the "
+                                  "initial vector")
+        order = finite[np.argsort(np.abs(lam[finite] - requested), kind="stable")]
+        sel = order[:min(nev, order.size)]
+        vals = lam[sel]
+        X = space.combine(V, k, Y[:, sel])
+        LX = space.combine(LV, k, Y[:, sel])
+        residuals = np.empty(sel.size)
+        for j in range(sel.size):
+            nx = space.norm(X[j])
+            X[j] = X[j] / nx
+            LX[j] = LX[j] / nx
+            residuals[j] = space.norm(LX[j] - complex(vals[j]) * X[j])
+        del LX
+        tolerance = atol + rtol * scale
+        converged = residuals <= tolerance
+        extraction = "rayleigh_ritz" if exhausted else "harmonic"
+        history.append(dict(cycle=cycle, subspace_dimension=k, locked=int(converged.sum()),
+                            maximum_residual=float(residuals.max()), residual_scale=scale,
+                            ritz_extraction=extraction, search_space_exhausted=exhausted))
+        best = dict(values=vals, residuals=residuals, converged=converged, restarts=cycle, iterations=applications,
+                    krylov_dimension=m, retained_dimension=keep, final_retained_dimension=nkeep,
+                    initial_retained_dimension=initial_retained, locked=int(converged.sum()), dimension=n,
+                    target=requested, harmonic_shift=sigma, algorithm="harmonic", ritz_extraction=extraction,
+                    search_space_exhausted=exhausted, residual_scale=scale, residual_tolerance=tolerance,
+                    restart_history=list(history), workspace_reused=False, operator_applications=applications)
+        if vals.size >= nev and converged.all():
+            break
+        if exhausted:
+            if require_convergence:
+                raise PiArgumentError("Rayleigh--Ritz extraction in the complete search space did not converge; "
+                                      f"maximum requested Ritz residual={residuals.max()}")
+            break
+        if cycle == maxrestarts:
+            if require_convergence:
+                raise PiArgumentError(f"thick-restarted harmonic Arnoldi did not converge in {maxrestarts} restarts; "
+                                      f"maximum requested Ritz residual={residuals.max()}")
+            break
+        retain = [int(idx) for j, idx in enumerate(sel) if converged[j]]
+        for idx in order:
+            if int(idx) in retain:
+                continue
+            retain.append(int(idx))
+            if len(retain) >= min(keep, order.size):
+                break
+        R = space.combine(V, k, Y[:, retain])
+        nkeep = _orthonormalize_rows(space, R, len(retain))
+        if nkeep == 0:
+            raise PiArgumentError("harmonic restart lost the retained invariant subspace")
+        V[:nkeep] = R[:nkeep]
+        del R
+    if vectors:
+        best["vectors"] = space.download(X)
+    return best
+
+
+def _check_harmonic_arguments(n, nev, krylovdim, thickdim, maxrestarts, target, initial_vector, initial_subspace,
+                              projector):
+    """Argument checks of harmonic_arnoldi_spectrum (krylov.jl:1378-1412, 53-58); returns
+    the resolved krylovdim, thickdim, initial vector and initial subspace."""
+    if projector is not None:
+        raise PiArgumentError("the CUDA path does not implement symmetry projectors; pass projector=None")
+    for name, value in (("nev", nev), ("maxrestarts", maxrestarts)):
+        if isinstance(value, bool) or not isinstance(value, (int, np.integer)):
+            raise PiArgumentError(f"{name} must be an integer")
+    if not (0 < nev <= n):
+        raise PiArgumentError("nev must lie between 1 and the operator dimension")
+    if maxrestarts < 0:
+        raise PiArgumentError("maxrestarts must be nonnegative")
+    krylovdim = max(30, 3 * nev + 6) if krylovdim is None else int(krylovdim)
+    thickdim = max(nev + 2, 2 * nev) if thickdim is None else int(thickdim)
+    if min(n, max(krylovdim, nev + 2)) > _COMBINE_VECTORS:
+        raise PiArgumentError(f"the CUDA harmonic Arnoldi process supports krylov dimensions up to {_COMBINE_VECTORS}")
+    try:
+        t = complex(target)
+    except TypeError:
+        raise PiArgumentError("Krylov target must be a finite number") from None
+    if not (np.isfinite(t.real) and np.isfinite(t.imag)):
+        raise PiArgumentError("Krylov target must be a finite number")
+    if initial_vector is not None and initial_subspace is not None:
+        raise PiArgumentError("initial_vector and initial_subspace are mutually exclusive")
+    if initial_vector is not None:
+        initial_vector = np.asarray(initial_vector, dtype=np.complex128)
+        if initial_vector.shape != (n,):
+            raise PiDimensionMismatch("initial_vector has wrong length")
+    if initial_subspace is not None:
+        initial_subspace = np.asarray(initial_subspace, dtype=np.complex128)
+        if initial_subspace.ndim != 2:
+            raise PiArgumentError("initial_subspace must be a matrix or nothing")
+        if initial_subspace.shape[0] != n:
+            raise PiDimensionMismatch("initial_subspace has the wrong row dimension")
+        if initial_subspace.shape[1] == 0:
+            raise PiArgumentError("initial_subspace cannot have zero columns")
+    return krylovdim, thickdim, t, initial_vector, initial_subspace
+
+
+def harmonic_arnoldi_spectrum(L, nev=6, krylovdim=None, thickdim=None, maxrestarts=20, target=0, initial_vector=None,
+                              initial_subspace=None, projector=None, atol=1e-10, rtol=1e-8, vectors=False, rng=None,
+                              require_convergence=True):
+    """harmonic_arnoldi_spectrum(L; nev=6, krylovdim=max(30, 3nev+6), thickdim=max(nev+2, 2nev),
+    maxrestarts=20, target=0, initial_vector, initial_subspace, projector, atol, rtol, vectors,
+    rng, require_convergence) (krylov.jl:1378-1551): eigenvalues nearest `target` by
+    thick-restarted harmonic Arnoldi.
+
+    Every L x is a device apply of the compiled plan and every projection a device multi-dot;
+    the basis, its images and the Ritz vectors stay on the GPU.  The small harmonic pencil
+    (Z^H Z, Z^H V) with Z = L V - sigma V, its eigenproblem, the ordering by distance to the
+    target and the restart selection run on the host, as the reference hands them to LAPACK.
+    Symmetry projectors are not provided (projector must be None).  Returns a dict with the
+    reference's result fields; `vectors` adds the (dim, nev) Ritz vectors."""
+    compiled = _as_compiled(L)
+    n = len(compiled.basis)
+    krylovdim, thickdim, t, v0, s0 = _check_harmonic_arguments(n, nev, krylovdim, thickdim, maxrestarts, target,
+                                                               initial_vector, initial_subspace, projector)
+    rng = rng if rng is not None else np.random.default_rng()
+    m = min(n, max(krylovdim, nev + 2))
+    space = _DeviceKrylovSpace(compiled, m)
+    return _harmonic_arnoldi(space, n, int(nev), krylovdim, thickdim, int(maxrestarts), t, v0, s0, float(atol),
+                             float(rtol), bool(vectors), rng, bool(require_convergence))
+
+
 def apply_element_major_(y, compiled: CompiledPIModel, x, coords="population"):
     """Batched FP32 apply on an element-major batch: y[e, c] = (L x[:, c])[e].
 
@@ -407,6 +719,32 @@ class GMRESAlgorithm:
             raise PiArgumentError("the CUDA backend runs unpreconditioned GMRES")
         if self.precision not in ("fp64", "mixed"):
             raise PiArgumentError("precision must be 'fp64' or 'mixed'")
+
+
+@dataclass(frozen=True)
+class HarmonicArnoldiAlgorithm:
+    """Thick-restarted harmonic Arnoldi parameters for modes near zero (highlevel.jl:126-150):
+    krylovdim defaults to max(30, 3nev+6) and thickdim to max(nev+2, 2nev)."""
+    nev: int = 6
+    krylovdim: int = None
+    thickdim: int = None
+    maxrestarts: int = 20
+
+    def __post_init__(self):
+        for name, minimum in (("nev", 1), ("krylovdim", 1), ("thickdim", 1), ("maxrestarts", 0)):
+            value = getattr(self, name)
+            if value is None and name in ("krylovdim", "thickdim"):
+                continue
+            if isinstance(value, bool):
+                raise PiArgumentError(f"{name} must be an integer, not a Bool")
+            if not isinstance(value, (int, np.integer)):
+                raise PiArgumentError(f"{name} must be an integer or nothing")
+            if value < minimum:
+                raise PiArgumentError(f"{name} must be at least {minimum}")
+        if self.krylovdim is None:
+            object.__setattr__(self, "krylovdim", max(30, 3 * self.nev + 6))
+        if self.thickdim is None:
+            object.__setattr__(self, "thickdim", max(self.nev + 2, 2 * self.nev))
 
 
 @dataclass(frozen=True)

@@ -145,16 +145,13 @@ class ParameterScanPlan:
                  solver_options=None, continuation=True, save_outputs=True, save_vectors=False,
                  save_restart=True, spectrum_target="largest_real", nev=6, diagnostic=None, seed=0,
                  rate_builder=None, atol=1e-10, rtol=1e-8):
-        from .backend import GMRESAlgorithm
+        from .backend import GMRESAlgorithm, HarmonicArnoldiAlgorithm
         if task not in _SCAN_TASKS:
             raise PiArgumentError("task must be :steady_state or :spectrum")
         if spectrum_target not in ("largest_real", "near_zero", "largest_magnitude"):
             raise PiArgumentError("spectrum_target must be :largest_real, :near_zero, or :largest_magnitude")
         if not isinstance(nev, Integral) or isinstance(nev, bool) or nev <= 0:
             raise PiArgumentError("nev must be positive")
-        if task == "spectrum" and spectrum_target == "near_zero":
-            raise PiArgumentError("near-zero spectral targets use harmonic Arnoldi, which the CUDA path does not "
-                                  "provide; use :largest_real or :largest_magnitude")
         values = list(parameters)
         if not values:
             raise PiArgumentError("parameters cannot be empty")
@@ -200,10 +197,21 @@ class ParameterScanPlan:
                 raise PiArgumentError("steady-state scans on the CUDA path use GMRESAlgorithm")
             managed = ("return_info", "initial_state", "workspace", "memory_budget", "krylovdim")
         else:
-            algorithm = algorithm or "krylov"
-            if algorithm not in ("auto", "krylov", "arnoldi"):
-                raise PiArgumentError(f"unsupported spectral scan algorithm {algorithm}; the CUDA path runs Arnoldi")
-            algorithm = "arnoldi"
+            # _spectrum_algorithm (highlevel.jl:735-746): automatic selection takes harmonic
+            # Arnoldi for modes near zero and Arnoldi otherwise (the CUDA path has no dense
+            # spectrum); an explicit Arnoldi request for modes near zero orders by smallest
+            # modulus.
+            algorithm = algorithm or "auto"
+            if not isinstance(algorithm, HarmonicArnoldiAlgorithm):
+                if algorithm not in ("auto", "krylov", "arnoldi", "harmonic"):
+                    raise PiArgumentError(f"unsupported spectral scan algorithm {algorithm}; the CUDA path runs "
+                                          "Arnoldi and harmonic Arnoldi")
+                if algorithm == "harmonic" or (algorithm == "auto" and spectrum_target == "near_zero"):
+                    algorithm = HarmonicArnoldiAlgorithm(nev=int(nev), krylovdim=soptions.pop("krylovdim", None),
+                                                         thickdim=soptions.pop("thickdim", None),
+                                                         maxrestarts=soptions.pop("maxrestarts", 20))
+                else:
+                    algorithm = "arnoldi"
             managed = ("return_info", "initial_vector", "workspace", "rng", "vectors", "nev", "subspace_dim",
                        "target", "memory_budget")
         forbidden = [k for k in managed if k in soptions]
@@ -343,33 +351,44 @@ def _point_rng(seed, index):
 
 
 def _spectrum_points(plan, selected, callback, on_error, kw):
-    """Spectral task (scans.jl:974-1053): one device Arnoldi process per point, warm-started
-    from the previous point's leading Ritz vector when continuation=True."""
-    from .backend import krylov_liouvillian_spectrum
-    which = {"largest_real": "LR", "largest_magnitude": "LM"}[plan.spectrum_target]
-    points, seed_vec, stopped = [], None, False
+    """Spectral task (scans.jl:974-1053): one device Arnoldi or harmonic Arnoldi process per
+    point.  With continuation=True, harmonic Arnoldi starts from the previous point's Ritz
+    vectors as an initial subspace; Arnoldi starts from their combination v_1 + sum_c v_c / c,
+    normalised (scans.jl:1020-1041)."""
+    from .backend import HarmonicArnoldiAlgorithm, harmonic_arnoldi_spectrum, krylov_liouvillian_spectrum
+    harmonic = isinstance(plan.algorithm, HarmonicArnoldiAlgorithm)
+    which = {"largest_real": "LR", "largest_magnitude": "LM", "near_zero": "SM"}[plan.spectrum_target]
+    points, seed, stopped = [], None, False
     for index in selected:
         parameter = plan.parameters[index]
         t0 = time.perf_counter()
         try:
             compiled = _compile_point(plan, parameter, index)
+            n = len(compiled.basis)
             t1 = time.perf_counter()
-            warm = plan.continuation and seed_vec is not None and len(seed_vec) == len(compiled.basis)
-            res = krylov_liouvillian_spectrum(compiled, nev=plan.nev, which=which,
-                                              initial_vector=seed_vec if warm else None,
-                                              vectors=plan.save_vectors or plan.continuation,
-                                              rng=_point_rng(plan.seed, index), **kw)
+            warm = plan.continuation and seed is not None and seed.shape[0] == n
+            want_vectors = plan.save_vectors or plan.continuation
+            if harmonic:
+                a = plan.algorithm
+                opts = dict(nev=a.nev, krylovdim=a.krylovdim, thickdim=a.thickdim, maxrestarts=a.maxrestarts)
+                opts.update(kw)
+                res = harmonic_arnoldi_spectrum(compiled, initial_subspace=seed if warm else None,
+                                                vectors=want_vectors, rng=_point_rng(plan.seed, index), **opts)
+            else:
+                res = krylov_liouvillian_spectrum(compiled, nev=plan.nev, which=which,
+                                                  initial_vector=seed if warm else None, vectors=want_vectors,
+                                                  rng=_point_rng(plan.seed, index), **kw)
             t2 = time.perf_counter()
             vecs = res.pop("vectors", None)
-            if plan.continuation and vecs is not None:
-                seed_vec = vecs[:, 0].copy()
+            if plan.continuation and vecs is not None and vecs.shape[1] > 0:
+                seed = vecs.copy() if harmonic else _arnoldi_continuation(vecs)
             output = dict(values=res["values"], vectors=vecs if plan.save_vectors else None, info=res)
             user = plan.diagnostic(output, parameter, index) if plan.diagnostic is not None else None
             point = ParameterScanPoint(index, parameter, "success", output if plan.save_outputs else None,
                                        float(res["residuals"].max()), None, bool(res["converged"].all()),
                                        res["iterations"], t1 - t0, t2 - t1, t2 - t0, warm, False,
-                                       dict(solver=res, user=user, backend="cuda", dimension=len(compiled.basis),
-                                            method="arnoldi"), None, None)
+                                       dict(solver=res, user=user, backend="cuda", dimension=n,
+                                            method="harmonic" if harmonic else "arnoldi"), None, None)
         except (PiError, ValueError) as err:
             _handle_failure(on_error, err)
             point = _failed(index, parameter, err, time.perf_counter() - t0)
@@ -377,7 +396,18 @@ def _spectrum_points(plan, selected, callback, on_error, kw):
         if _scan_callback(callback, point) or (point.status == "failed" and on_error == "stop"):
             stopped = True
             break
-    return points, seed_vec, stopped
+    return points, seed, stopped
+
+
+def _arnoldi_continuation(vecs):
+    """The Arnoldi continuation vector (scans.jl:1026-1041): an exactly converged single
+    eigenvector would make the next factorisation break down after one step, so the seed is
+    v_1 + sum_{c >= 2} v_c / c over the selected modes, normalised (v_1 when that vanishes)."""
+    vector = vecs[:, 0].copy()
+    for column in range(1, vecs.shape[1]):
+        vector += vecs[:, column] / (column + 1)
+    norm = np.linalg.norm(vector)
+    return vecs[:, 0].copy() if norm == 0 else vector / norm
 
 
 def parameter_scan(plan: ParameterScanPlan, callback=None, indices=None, execution="serial", on_error="stop",

@@ -105,3 +105,89 @@ def test_spectrum_agrees_with_oracle_arnoldi_and_rejects_bad_input(torch_cuda):
         picuda.krylov_liouvillian_spectrum(model, which="XX")
     with pytest.raises(picuda.PiArgumentError):
         picuda.krylov_liouvillian_spectrum(model, initial_vector=np.zeros(n))
+
+
+# ---- thick-restarted harmonic Arnoldi (harmonic_arnoldi_spectrum, krylov.jl:1378-1551) ----
+
+SM = np.array([[0, 1], [0, 0]], dtype=np.complex128)
+
+
+@pytest.mark.parametrize("name,make", [("driven8", lambda: M.driven_c1(8)), ("general6", lambda: M.general(6, seed=4))])
+def test_harmonic_spectrum_matches_oracle(torch_cuda, name, make):
+    """Restarted harmonic Arnoldi (krylovdim 30 < dim) on the device: the values nearest zero
+    agree with the oracle's restatement from the same initial vector and with the dense
+    spectrum, every residual is below atol + rtol * scale, and the returned Ritz vectors
+    satisfy |L x - lambda x| within that tolerance under the oracle's operator."""
+    model = make()
+    L = O.materialize(O.Plan(M.to_oracle(model)))
+    n = L.shape[0]
+    v0 = M.random_state_vector(n, 11)
+    kw = dict(nev=3, krylovdim=30, maxrestarts=100, initial_vector=v0, vectors=True)
+    ref = O.harmonic_arnoldi_spectrum(lambda v: L @ v, n, **kw)
+    got = picuda.harmonic_arnoldi_spectrum(model, **kw)
+    tol = got["residual_tolerance"]
+    assert got["algorithm"] == "harmonic" and got["ritz_extraction"] == "harmonic"
+    assert got["converged"].all() and (got["residuals"] <= tol).all()
+    assert abs(got["restarts"] - ref["restarts"]) <= 1, (got["restarts"], ref["restarts"])
+    assert np.allclose(got["values"], ref["values"], atol=10 * tol, rtol=0), (got["values"], ref["values"])
+    dense = np.linalg.eigvals(L)
+    for v in got["values"]:
+        assert np.abs(dense - v).min() <= 10 * tol + 1e-9
+    X = got["vectors"]
+    assert X.shape == (n, 3)
+    resid = np.linalg.norm(L @ X - X * got["values"][None, :], axis=0)
+    assert (resid <= 1.01 * tol + 1e-12).all(), (resid, tol)
+
+
+def test_harmonic_spectrum_complete_space_and_continuation(torch_cuda):
+    """test/test_krylov.jl:154-165 on the device: three qubits with local (0.7) and
+    collective (0.2) decay, nev=3, krylovdim=dim, atol=1e-9, rtol=1e-7 -- residuals below
+    2e-7 and the stationary value within 3 residuals (+ eps * scale) of the dense one.  The
+    Ritz vectors then seed a second solve as an initial subspace (the spectral scan's
+    continuation), which retains all three and returns the same values."""
+    model = picuda.PIModel(picuda.PIBasis(3, 2), [picuda.LocalJump(SM, rate=0.7), picuda.CollectiveJump(SM, rate=0.2)])
+    L = O.materialize(O.Plan(M.to_oracle(model)))
+    n = L.shape[0]
+    dense = np.linalg.eigvals(L)
+    dense = dense[O.ritz_order(dense, "LR")]
+    h = picuda.harmonic_arnoldi_spectrum(model, nev=3, krylovdim=n, initial_vector=M.random_state_vector(n, 10),
+                                         vectors=True, atol=1e-9, rtol=1e-7)
+    assert h["residuals"].max() < 2e-7
+    assert h["search_space_exhausted"] and h["ritz_extraction"] == "rayleigh_ritz"
+    i = int(np.argmin(np.abs(h["values"] - dense[0])))
+    floor = np.finfo(float).eps * max(1.0, h["residual_scale"])
+    assert abs(h["values"][i] - dense[0]) <= 3 * h["residuals"][i] + floor
+    again = picuda.harmonic_arnoldi_spectrum(model, nev=3, krylovdim=n, initial_subspace=h["vectors"],
+                                             atol=1e-9, rtol=1e-7)
+    assert again["initial_retained_dimension"] == 3
+    assert np.allclose(np.sort_complex(again["values"]), np.sort_complex(h["values"]), atol=1e-6, rtol=0)
+    with pytest.raises(picuda.PiArgumentError, match="symmetry projectors"):
+        picuda.harmonic_arnoldi_spectrum(model, projector=np.eye(n))
+    with pytest.raises(picuda.PiArgumentError):
+        picuda.harmonic_arnoldi_spectrum(model, nev=n + 1)
+    with pytest.raises(picuda.PiArgumentError, match="zero component"):
+        picuda.harmonic_arnoldi_spectrum(model, nev=2, initial_vector=np.zeros(n))
+
+
+def test_harmonic_spectral_scan_continuation(torch_cuda):
+    """test/test_compiled_families.jl:170-188: a near-zero spectral scan of a one-qubit family
+    (decay 1.0, pumping p) with HarmonicArnoldiAlgorithm(nev=2, krylovdim=4, thickdim=2,
+    maxrestarts=4) warm-starts the second point from both Ritz vectors of the first and
+    keeps the restart seed as a matrix."""
+    spin = picuda.spin_matrices()
+    fam = picuda.compile_family(picuda.PIModel(picuda.PIBasis(1, 2), [picuda.LocalJump(spin["jm"], rate=1.0),
+                                                                      picuda.LocalJump(spin["jp"], rate=0.2)]))
+    alg = picuda.HarmonicArnoldiAlgorithm(nev=2, krylovdim=4, thickdim=2, maxrestarts=4)
+    plan = picuda.ParameterScanPlan([0.2, 0.25], fam, rate_builder=lambda p: (1.0, p), task="spectrum",
+                                    algorithm=alg, spectrum_target="near_zero", nev=2, save_vectors=False,
+                                    solver_options=dict(require_convergence=False))
+    res = picuda.parameter_scan(plan, on_error="throw")
+    assert [p.status for p in res] == ["success", "success"]
+    assert res.points[1].warm_started
+    assert res.points[1].diagnostics["solver"]["initial_retained_dimension"] == 2
+    assert isinstance(res.restart_seed, np.ndarray) and res.restart_seed.shape == (4, 2)
+    # the slowest modes of decay 1 and pumping p: 0 and -(1 + p)/2
+    for p, pt in zip([0.2, 0.25], res.points):
+        vals = pt.output["values"]
+        assert abs(vals[0]) <= 1e-9
+        assert abs(vals[1] + (1 + p) / 2) <= 1e-9

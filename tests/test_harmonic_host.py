@@ -1,0 +1,291 @@
+"""Thick-restarted harmonic Arnoldi (harmonic_arnoldi_spectrum, krylov.jl:1378-1551) on the CPU.
+
+Three layers, no GPU:
+  * the oracle's restatement pinned to the reference's own known answers
+    (test/test_krylov.jl:154-214);
+  * the library's algorithm (picuda.backend._harmonic_arnoldi) run over a numpy vector
+    space that stands in for the device one, against the oracle on the same operator and
+    starting vectors -- the same host logic the GPU path drives through pi_apply_f64,
+    pi_mdot_f64_noalloc and pi_combine_f64;
+  * argument checks and the algorithm record (HarmonicArnoldiAlgorithm, highlevel.jl:126-150).
+"""
+import numpy as np
+import pytest
+
+import picuda
+from picuda import backend as B
+from oracle import pi_oracle as O
+
+SM = np.array([[0, 1], [0, 0]], dtype=np.complex128)
+
+
+class NumpySpace:
+    """The vector operations of the device Krylov space over numpy rows."""
+
+    def __init__(self, A):
+        self.A = A
+        self.n = A.shape[0]
+        self.applications = 0
+
+    def block(self, m):
+        return np.zeros((m, self.n), dtype=np.complex128)
+
+    def upload(self, v):
+        return np.array(v, dtype=np.complex128)
+
+    def copy(self, v):
+        return v.copy()
+
+    def download(self, rows):
+        return rows.T.copy()
+
+    def apply(self, dst, src):
+        dst[:] = self.A @ src
+        self.applications += 1
+
+    def dots(self, M, k, q):
+        return M[:k].conj() @ q
+
+    def norm(self, q):
+        return float(np.linalg.norm(q))
+
+    def combine(self, M, k, Y):
+        return (M[:k].T @ np.asarray(Y)).T.copy()
+
+    def subtract(self, q, M, k, coef):
+        q -= M[:k].T @ coef
+
+
+def _host_harmonic(A, nev=6, krylovdim=None, thickdim=None, maxrestarts=20, target=0, initial_vector=None,
+                   initial_subspace=None, atol=1e-10, rtol=1e-8, vectors=False, seed=0, require_convergence=True):
+    n = A.shape[0]
+    kd, td, t, v0, s0 = B._check_harmonic_arguments(n, nev, krylovdim, thickdim, maxrestarts, target,
+                                                    initial_vector, initial_subspace, None)
+    return B._harmonic_arnoldi(NumpySpace(A), n, nev, kd, td, maxrestarts, t, v0, s0, atol, rtol, vectors,
+                               np.random.default_rng(seed), require_convergence)
+
+
+def _pi_matrix():
+    """test/test_krylov.jl:2-4: three qubits with local (0.7) and collective (0.2) decay."""
+    model = O.PIModel(O.PIBasis(3, 2), [O.LocalJump(SM, 0.7), O.CollectiveJump(SM, 0.2)])
+    return O.materialize(O.Plan(model))
+
+
+def _nonnormal(n, seed):
+    rng = np.random.default_rng(seed)
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
+    return A - 2.5 * np.eye(n)
+
+
+def _seed(n, seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal(n) + 1j * rng.standard_normal(n)
+
+
+# ---- the oracle against the reference's known answers ---------------------------------
+
+def test_oracle_harmonic_stationary_mode():
+    """test/test_krylov.jl:154-165: nev=3, krylovdim=dim, atol=1e-9, rtol=1e-7 -> residuals
+    below 2e-7 and the stationary value within 3 residuals (+ eps * scale) of the dense one."""
+    L = _pi_matrix()
+    n = L.shape[0]
+    dense = np.linalg.eigvals(L)
+    dense = dense[O.ritz_order(dense, "LR")]
+    h = O.harmonic_arnoldi_spectrum(lambda v: L @ v, n, nev=3, krylovdim=n, initial_vector=_seed(n, 10),
+                                    vectors=True, atol=1e-9, rtol=1e-7)
+    assert h["residuals"].max() < 2e-7
+    i = int(np.argmin(np.abs(h["values"] - dense[0])))
+    floor = np.finfo(float).eps * max(1.0, h["residual_scale"])
+    assert abs(h["values"][i] - dense[0]) <= 3 * h["residuals"][i] + floor
+    assert h["algorithm"] == "harmonic"
+
+
+def test_oracle_harmonic_complete_space_uses_rayleigh_ritz():
+    """test/test_krylov.jl:170-192: the nonnormal 4 x 4 operator whose harmonic pencil is
+    singular at zero.  The reference restricts it to a two-dimensional symmetry sector; with
+    no projector the whole space is the range, and once it is spanned the extraction is
+    Rayleigh-Ritz with the same two values nearest zero, 0 and -0.7."""
+    L = np.zeros((4, 4), dtype=np.complex128)
+    L[0, 3], L[3, 3], L[1, 1], L[2, 2] = 1, -0.7, -2, -3
+    h = O.harmonic_arnoldi_spectrum(lambda v: L @ v, 4, nev=2, krylovdim=4, maxrestarts=0,
+                                    initial_vector=np.array([1, 2, 3, 4], dtype=np.complex128), vectors=True,
+                                    atol=1e-12, rtol=1e-10)
+    assert np.allclose(h["values"], [0, -0.7], atol=1e-11, rtol=0)
+    assert h["residuals"].max() < 1e-11
+    X = h["vectors"]
+    assert np.linalg.norm(L @ X - X * h["values"][None, :]) < 2e-11
+    assert h["ritz_extraction"] == "rayleigh_ritz" and h["search_space_exhausted"]
+
+
+def test_oracle_harmonic_restarts():
+    """test/test_krylov.jl:209-214: krylovdim 8 with atol = rtol = 0 runs every restart."""
+    L = _pi_matrix()
+    n = L.shape[0]
+    h = O.harmonic_arnoldi_spectrum(lambda v: L @ v, n, nev=2, krylovdim=8, initial_vector=_seed(n, 10),
+                                    maxrestarts=2, require_convergence=False, atol=0, rtol=0)
+    assert h["restarts"] == 2
+    assert h["ritz_extraction"] == "harmonic" and not h["search_space_exhausted"]
+
+
+def test_oracle_harmonic_restarted_converges_to_nearest_eigenvalues():
+    A = _nonnormal(60, 3)
+    ev = np.linalg.eigvals(A)
+    ev = ev[np.argsort(np.abs(ev))]
+    h = O.harmonic_arnoldi_spectrum(lambda v: A @ v, 60, nev=3, krylovdim=20, maxrestarts=200,
+                                    initial_vector=_seed(60, 1))
+    assert h["restarts"] > 0
+    assert np.allclose(h["values"], ev[:3], atol=1e-7, rtol=0)
+
+
+# ---- the library's algorithm over a numpy vector space against the oracle ---------------
+
+# Value tolerance per case: two converged runs agree to about the residual tolerance times
+# the eigenvalues' condition; the restarted PI case holds the nonnormal pair -0.65 / -0.7
+# (condition ~1e2 at a residual tolerance of 3e-8).
+@pytest.mark.parametrize("case,vtol", [("pi_full", 1e-9), ("pi_restarted", 1e-5), ("nonnormal", 1e-8),
+                                       ("target", 1e-8)])
+def test_library_harmonic_matches_oracle(case, vtol):
+    if case == "pi_full":
+        A, kw = _pi_matrix(), dict(nev=3, atol=1e-9, rtol=1e-7)
+        kw["krylovdim"] = A.shape[0]
+    elif case == "pi_restarted":
+        A, kw = _pi_matrix(), dict(nev=3, krylovdim=10, maxrestarts=100)
+    elif case == "nonnormal":
+        A, kw = _nonnormal(60, 3), dict(nev=3, krylovdim=20, maxrestarts=200)
+    else:
+        A, kw = _nonnormal(50, 5), dict(nev=4, krylovdim=24, target=-2.0 + 0.5j, maxrestarts=200)
+    n = A.shape[0]
+    v0 = _seed(n, 11)
+    ref = O.harmonic_arnoldi_spectrum(lambda v: A @ v, n, initial_vector=v0, vectors=True, **kw)
+    got = _host_harmonic(A, initial_vector=v0, vectors=True, **kw)
+    assert got["restarts"] == ref["restarts"]
+    assert got["ritz_extraction"] == ref["ritz_extraction"]
+    assert got["iterations"] == ref["iterations"]
+    assert np.allclose(got["values"], ref["values"], atol=vtol, rtol=0)
+    # each value is an eigenvalue (the PI case's -0.65 is a defective double eigenvalue with
+    # one eigenvector, so the values nearest zero are 0, -0.65 and -0.7)
+    dense = np.linalg.eigvals(A)
+    for v in got["values"]:
+        assert np.abs(dense - v).min() <= max(vtol, 10 * got["residual_tolerance"])
+    assert (got["residuals"] <= got["residual_tolerance"]).all()
+    X = got["vectors"]
+    resid = np.linalg.norm(A @ X - X * got["values"][None, :], axis=0)
+    assert (resid <= 1.01 * got["residual_tolerance"] + 1e-12).all()
+
+
+def test_library_harmonic_subspace_continuation():
+    """A converged set of Ritz vectors as initial_subspace (the spectral scan's continuation,
+    scans.jl:983-1000, 1020-1025) converges in the first cycle with the same values."""
+    A = _nonnormal(60, 3)
+    first = _host_harmonic(A, nev=3, krylovdim=20, maxrestarts=200, initial_vector=_seed(60, 1), vectors=True)
+    again = _host_harmonic(A, nev=3, krylovdim=20, maxrestarts=200, initial_subspace=first["vectors"])
+    assert again["initial_retained_dimension"] == 3
+    assert again["restarts"] <= first["restarts"]
+    assert np.allclose(again["values"], first["values"], atol=1e-7, rtol=0)
+    ref = O.harmonic_arnoldi_spectrum(lambda v: A @ v, 60, nev=3, krylovdim=20, maxrestarts=200,
+                                      initial_subspace=first["vectors"])
+    assert np.allclose(again["values"], ref["values"], atol=1e-9, rtol=0)
+
+
+def test_library_harmonic_not_converged():
+    A = _nonnormal(60, 3)
+    with pytest.raises(picuda.PiArgumentError, match="did not converge in 1 restarts"):
+        _host_harmonic(A, nev=3, krylovdim=8, maxrestarts=1, initial_vector=_seed(60, 1), atol=0, rtol=0)
+    out = _host_harmonic(A, nev=3, krylovdim=8, maxrestarts=1, initial_vector=_seed(60, 1), atol=0, rtol=0,
+                         require_convergence=False, vectors=True)
+    assert out["restarts"] == 1 and not out["converged"].any()
+    assert out["vectors"].shape == (60, 3)
+    assert [r["cycle"] for r in out["restart_history"]] == [0, 1]
+
+
+# ---- argument checks -----------------------------------------------------------------------
+
+def test_harmonic_argument_checks():
+    chk = B._check_harmonic_arguments
+    with pytest.raises(picuda.PiArgumentError, match="symmetry projectors"):
+        chk(10, 2, None, None, 20, 0, None, None, np.eye(10))
+    with pytest.raises(picuda.PiArgumentError, match="nev must lie"):
+        chk(10, 0, None, None, 20, 0, None, None, None)
+    with pytest.raises(picuda.PiArgumentError, match="nev must lie"):
+        chk(10, 11, None, None, 20, 0, None, None, None)
+    with pytest.raises(picuda.PiArgumentError, match="maxrestarts"):
+        chk(10, 2, None, None, -1, 0, None, None, None)
+    with pytest.raises(picuda.PiArgumentError, match="finite"):
+        chk(10, 2, None, None, 20, complex(np.inf, 0), None, None, None)
+    with pytest.raises(picuda.PiArgumentError, match="mutually exclusive"):
+        chk(10, 2, None, None, 20, 0, np.ones(10), np.ones((10, 1)), None)
+    with pytest.raises(picuda.PiDimensionMismatch):
+        chk(10, 2, None, None, 20, 0, np.ones(9), None, None)
+    with pytest.raises(picuda.PiDimensionMismatch):
+        chk(10, 2, None, None, 20, 0, None, np.ones((9, 2)), None)
+    with pytest.raises(picuda.PiArgumentError, match="zero columns"):
+        chk(10, 2, None, None, 20, 0, None, np.ones((10, 0)), None)
+    with pytest.raises(picuda.PiArgumentError, match="up to 128"):
+        chk(1000, 2, 129, None, 20, 0, None, None, None)
+    assert chk(1000, 6, None, None, 20, 0, None, None, None)[:2] == (30, 12)
+    assert chk(10, 2, None, None, 20, 0, None, None, None)[:2] == (30, 4)
+    with pytest.raises(picuda.PiArgumentError, match="zero component"):
+        _host_harmonic(np.eye(5, dtype=np.complex128), nev=1, initial_vector=np.zeros(5))
+    with pytest.raises(picuda.PiArgumentError, match="no independent component"):
+        _host_harmonic(np.eye(5, dtype=np.complex128), nev=1, initial_subspace=np.zeros((5, 2)))
+
+
+def test_harmonic_algorithm_record():
+    a = picuda.HarmonicArnoldiAlgorithm()
+    assert (a.nev, a.krylovdim, a.thickdim, a.maxrestarts) == (6, 30, 12, 20)
+    a = picuda.HarmonicArnoldiAlgorithm(nev=12)
+    assert (a.krylovdim, a.thickdim) == (42, 24)
+    with pytest.raises(picuda.PiArgumentError, match="Bool"):
+        picuda.HarmonicArnoldiAlgorithm(nev=True)
+    with pytest.raises(picuda.PiArgumentError, match="at least 0"):
+        picuda.HarmonicArnoldiAlgorithm(maxrestarts=-1)
+    with pytest.raises(picuda.PiArgumentError, match="at least 1"):
+        picuda.HarmonicArnoldiAlgorithm(krylovdim=0)
+
+
+def test_near_zero_spectral_scan_host_logic(monkeypatch):
+    """The spectral scan's harmonic branch (scans.jl:974-1053) with the device solve replaced
+    by the library's algorithm over a numpy space: test/test_compiled_families.jl:170-188's
+    one-qubit family (decay 1.0, pumping p) warm-starts the second point from both Ritz
+    vectors of the first and keeps the restart seed as a matrix."""
+    import types
+    from picuda import scans as S
+    from tests import models as M
+    spin = picuda.spin_matrices()
+    fam = picuda.compile_family(picuda.PIModel(picuda.PIBasis(1, 2), [picuda.LocalJump(spin["jm"], rate=1.0),
+                                                                      picuda.LocalJump(spin["jp"], rate=0.2)]))
+    seen = []
+
+    def compile_point(plan, parameter, index):
+        made = plan.model_builder(parameter, index)
+        model = S._family_model(made.family, S._family_rates(made.family, made.rates))
+        return types.SimpleNamespace(basis=model.basis, matrix=O.materialize(O.Plan(M.to_oracle(model))))
+
+    def solve(compiled, nev=6, krylovdim=None, thickdim=None, maxrestarts=20, target=0, initial_vector=None,
+              initial_subspace=None, atol=1e-10, rtol=1e-8, vectors=False, rng=None, require_convergence=True):
+        n = len(compiled.basis)
+        kd, td, t, v0, s0 = B._check_harmonic_arguments(n, nev, krylovdim, thickdim, maxrestarts, target,
+                                                        initial_vector, initial_subspace, None)
+        seen.append(dict(nev=nev, krylovdim=kd, thickdim=td, maxrestarts=maxrestarts, warm=s0 is not None))
+        return B._harmonic_arnoldi(NumpySpace(compiled.matrix), n, nev, kd, td, maxrestarts, t, v0, s0, atol, rtol,
+                                   vectors, rng, require_convergence)
+
+    monkeypatch.setattr(S, "_compile_point", compile_point)
+    monkeypatch.setattr(B, "harmonic_arnoldi_spectrum", solve)
+    alg = picuda.HarmonicArnoldiAlgorithm(nev=2, krylovdim=4, thickdim=2, maxrestarts=4)
+    plan = picuda.ParameterScanPlan([0.2, 0.25], fam, rate_builder=lambda p: (1.0, p), task="spectrum",
+                                    algorithm=alg, spectrum_target="near_zero", nev=2, save_vectors=False,
+                                    solver_options=dict(require_convergence=False))
+    res = picuda.parameter_scan(plan, on_error="throw")
+    assert [p.status for p in res] == ["success", "success"]
+    assert seen == [dict(nev=2, krylovdim=4, thickdim=2, maxrestarts=4, warm=False),
+                    dict(nev=2, krylovdim=4, thickdim=2, maxrestarts=4, warm=True)]
+    assert res.points[1].warm_started and not res.points[0].warm_started
+    assert res.points[1].diagnostics["solver"]["initial_retained_dimension"] == 2
+    assert res.points[1].diagnostics["method"] == "harmonic"
+    assert isinstance(res.restart_seed, np.ndarray) and res.restart_seed.shape == (4, 2)
+    for p, pt in zip([0.2, 0.25], res.points):
+        vals = pt.output["values"]
+        assert pt.output["vectors"] is None
+        assert abs(vals[0]) <= 1e-9
+        assert abs(vals[1] + (1 + p) / 2) <= 1e-9

@@ -97,9 +97,33 @@ def test_spectral_scan_plan_validation():
         picuda.ParameterScanPlan([1.0], build, task="spectrum", nev=0)
     with pytest.raises(picuda.PiArgumentError):
         picuda.ParameterScanPlan([1.0], build, task="spectrum", spectrum_target="smallest")
-    with pytest.raises(picuda.PiArgumentError):
-        picuda.ParameterScanPlan([1.0], build, task="spectrum", spectrum_target="near_zero")
+    # automatic selection near zero is harmonic Arnoldi (highlevel.jl:735-746); its Krylov
+    # options move from solver_options into the algorithm record
+    near = picuda.ParameterScanPlan([1.0], build, task="spectrum", spectrum_target="near_zero", nev=2,
+                                    solver_options={"krylovdim": 12, "maxrestarts": 5, "require_convergence": False})
+    assert near.algorithm == picuda.HarmonicArnoldiAlgorithm(nev=2, krylovdim=12, maxrestarts=5)
+    assert near.solver_options == {"require_convergence": False}
+    explicit = picuda.HarmonicArnoldiAlgorithm(nev=2, krylovdim=4, thickdim=2, maxrestarts=4)
+    assert picuda.ParameterScanPlan([1.0], build, task="spectrum", algorithm=explicit).algorithm is explicit
+    assert picuda.ParameterScanPlan([1.0], build, task="spectrum", algorithm="harmonic",
+                                    nev=3).algorithm == picuda.HarmonicArnoldiAlgorithm(nev=3)
+    assert picuda.ParameterScanPlan([1.0], build, task="spectrum", spectrum_target="near_zero",
+                                    algorithm="arnoldi").algorithm == "arnoldi"
+    assert picuda.ParameterScanPlan([1.0], build, task="spectrum").algorithm == "arnoldi"
     with pytest.raises(picuda.PiArgumentError):
         picuda.ParameterScanPlan([1.0], build, task="spectrum", solver_options={"vectors": True})
     with pytest.raises(picuda.PiArgumentError):
         picuda.ParameterScanPlan([1.0], build, task="spectrum", algorithm="dense")
+
+
+def test_arnoldi_continuation_vector():
+    """scans.jl:1026-1041: v_1 + sum_{c >= 2} v_c / c over the selected modes, normalised;
+    v_1 itself when the combination vanishes."""
+    from picuda.scans import _arnoldi_continuation
+    V = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [0, 0, 0]], dtype=np.complex128)
+    got = _arnoldi_continuation(V)
+    ref = np.array([1, 1 / 2, 1 / 3, 0]) / np.linalg.norm([1, 1 / 2, 1 / 3])
+    assert np.allclose(got, ref, atol=1e-15, rtol=0)
+    W = np.array([[1, -2], [1, -2]], dtype=np.complex128)
+    assert np.array_equal(_arnoldi_continuation(W), W[:, 0])
+    assert np.array_equal(_arnoldi_continuation(V[:, :1]), V[:, 0])
