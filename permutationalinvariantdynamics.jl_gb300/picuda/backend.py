@@ -639,6 +639,75 @@ def harmonic_arnoldi_spectrum(L, nev=6, krylovdim=None, thickdim=None, maxrestar
                              float(rtol), bool(vectors), rng, bool(require_convergence))
 
 
+def _liouvillian_gap_info(values, atol, rtol, check_stability):
+    """_liouvillian_gap_info (spectra.jl:289-308): the gap -max Re(lambda) over the values
+    outside the stationary cluster |lambda| <= atol + rtol * max(max |lambda|, 1)."""
+    values = np.asarray(values, dtype=np.complex128)
+    scale = max(float(np.abs(values).max(initial=0.0)), 1.0)
+    tol = atol + rtol * scale
+    stationary = np.abs(values) <= tol
+    nullity = int(stationary.sum())
+    if nullity == 0:
+        raise PiArgumentError(f"no stationary eigenvalue was found within tolerance {tol}")
+    abscissa = float(values.real.max())
+    stable = abscissa <= tol
+    if check_stability and not stable:
+        raise PiArgumentError(f"Liouvillian is unstable: spectral abscissa is {abscissa}")
+    candidates = values[~stationary]
+    if candidates.size == 0:
+        gap, mode, frequency = float("inf"), None, float("nan")
+    else:
+        mode = complex(candidates[int(np.argmax(candidates.real))])
+        gap = -mode.real
+        if abs(gap) <= tol:
+            gap = 0.0
+        frequency = mode.imag
+    return dict(gap=gap, decay_eigenvalue=mode, oscillation_frequency=frequency, stationary_multiplicity=nullity,
+                unique_stationary_mode=nullity == 1, stable=stable, spectral_abscissa=abscissa, tolerance=tol,
+                dimension=values.size)
+
+
+_GAP_METHODS = {"krylov": "arnoldi", "ordinary_arnoldi": "arnoldi", "arnoldi": "arnoldi"}
+
+
+def pi_liouvillian_gap(x, atol=1e-12, rtol=1e-10, check_stability=True, return_info=False, symmetry=None,
+                       method="krylov", nev=6, krylovdim=None, require_convergence=True, initial_vector=None,
+                       rng=None):
+    """pi_liouvillian_gap(x; method=:krylov, nev, krylovdim=max(20, 2nev+4), atol, rtol,
+    check_stability, return_info, initial_vector, rng) (spectra.jl:262-470, the Arnoldi
+    branch :441-466): the asymptotic decay gap -max Re(lambda) outside the stationary
+    cluster, from the nev largest-real Ritz values of the device Arnoldi process.  The count
+    of stationary modes is certified when fewer than nev of the returned values are
+    stationary.
+
+    The CUDA path provides the Arnoldi method only: the reference's default method=:dense
+    materialises the matrix, and harmonic selection cannot certify a global gap without a
+    symmetry projector (spectra.jl:414-422), which the CUDA path does not provide."""
+    if not isinstance(method, str):
+        raise PiArgumentError("method must be a Symbol")
+    if method == "harmonic":
+        raise PiArgumentError("method=:harmonic selects modes nearest zero in modulus and cannot certify the global "
+                              "largest-real Liouvillian gap; use method=:krylov")
+    if method not in _GAP_METHODS:
+        raise PiArgumentError(f"the CUDA path computes Liouvillian gaps with method=:krylov, not :{method}")
+    if symmetry is not None:
+        raise PiArgumentError("use method=:harmonic for matrix-free symmetry projection")
+    if isinstance(nev, bool) or not isinstance(nev, (int, np.integer)):
+        raise PiArgumentError("nev must be an integer")
+    krylovdim = max(20, 2 * nev + 4) if krylovdim is None else krylovdim
+    arn = krylov_liouvillian_spectrum(x, nev=nev, krylovdim=krylovdim, which="LR", initial_vector=initial_vector,
+                                      atol=atol, rtol=rtol, rng=rng, require_convergence=require_convergence)
+    info = _liouvillian_gap_info(arn["values"], atol, rtol, check_stability)
+    # A partial spectrum certifies the returned slow mode, but not that every stationary
+    # mode was counted when all nev returned values are stationary.
+    complete = info["stationary_multiplicity"] < nev
+    info.update(dimension=arn["dimension"], symmetry_used=False, symmetry_name=None, symmetry_sectors=None,
+                symmetry_residual=None, method=_GAP_METHODS[method], ritz_residuals=arn["residuals"],
+                stationary_multiplicity_certified=complete, krylov_dimension=arn["krylov_dimension"],
+                scope="global", selection="largest_real", gap_certified=complete, stability_certified=complete)
+    return info if return_info else info["gap"]
+
+
 def apply_element_major_(y, compiled: CompiledPIModel, x, coords="population"):
     """Batched FP32 apply on an element-major batch: y[e, c] = (L x[:, c])[e].
 

@@ -289,3 +289,58 @@ def test_near_zero_spectral_scan_host_logic(monkeypatch):
         assert pt.output["vectors"] is None
         assert abs(vals[0]) <= 1e-9
         assert abs(vals[1] + (1 + p) / 2) <= 1e-9
+
+
+# ---- the Liouvillian gap (pi_liouvillian_gap, spectra.jl:262-470) ------------------------
+
+def _dense_gap(L, atol=1e-12, rtol=1e-10):
+    """spectra.jl:289-308 on the dense spectrum (the reference's default method=:dense)."""
+    vals = np.linalg.eigvals(L)
+    tol = atol + rtol * max(np.abs(vals).max(), 1.0)
+    return -max(v.real for v in vals if abs(v) > tol)
+
+
+def test_gap_info_known_values():
+    """spectra.jl:289-308: the oscillatory counterexample of test/test_krylov.jl:324-330
+    (gap 0.1 from -0.1+100i, not the -1 mode), the stationary-count and stability rules."""
+    info = B._liouvillian_gap_info([0, -0.1 + 100j, -1], 1e-12, 1e-10, True)
+    assert abs(info["gap"] - 0.1) < 1e-15 and info["oscillation_frequency"] == 100.0
+    assert info["stationary_multiplicity"] == 1 and info["unique_stationary_mode"] and info["stable"]
+    assert info["decay_eigenvalue"] == -0.1 + 100j
+    with pytest.raises(picuda.PiArgumentError, match="no stationary eigenvalue"):
+        B._liouvillian_gap_info([-1.0, -2.0], 1e-12, 1e-10, True)
+    with pytest.raises(picuda.PiArgumentError, match="unstable"):
+        B._liouvillian_gap_info([0.0, 0.5, -1.0], 1e-12, 1e-10, True)
+    info = B._liouvillian_gap_info([0.0, 0.5, -1.0], 1e-12, 1e-10, False)
+    assert not info["stable"] and info["gap"] == -0.5
+    info = B._liouvillian_gap_info([0.0, 1e-13], 1e-12, 1e-10, True)
+    assert info["gap"] == float("inf") and info["decay_eigenvalue"] is None
+    assert info["stationary_multiplicity"] == 2 and not info["unique_stationary_mode"]
+
+
+def test_gap_from_arnoldi_host_logic(monkeypatch):
+    """test/test_krylov.jl:145-152 with the device Arnoldi replaced by the oracle's
+    restatement: method=:krylov, nev=4, krylovdim=dim gives the dense gap to 2e-10 with the
+    stationary count certified; a symmetry with method=:krylov is rejected."""
+    L = _pi_matrix()
+    n = L.shape[0]
+
+    def spectrum(x, nev=6, krylovdim=None, which="LR", initial_vector=None, atol=1e-10, rtol=1e-8, vectors=False,
+                 rng=None, require_convergence=True):
+        assert x == "model" and which == "LR"
+        return O.krylov_liouvillian_spectrum(lambda v: L @ v, n, nev=nev, krylovdim=krylovdim, which=which,
+                                             initial_vector=initial_vector, atol=atol, rtol=rtol,
+                                             require_convergence=require_convergence)
+
+    monkeypatch.setattr(B, "krylov_liouvillian_spectrum", spectrum)
+    info = picuda.pi_liouvillian_gap("model", method="krylov", nev=4, krylovdim=n, return_info=True)
+    assert abs(info["gap"] - _dense_gap(L)) <= 2e-10
+    assert info["method"] == "arnoldi" and info["stationary_multiplicity_certified"]
+    assert info["scope"] == "global" and info["selection"] == "largest_real" and info["dimension"] == n
+    assert picuda.pi_liouvillian_gap("model", nev=4, krylovdim=n) == info["gap"]
+    with pytest.raises(picuda.PiArgumentError, match="symmetry"):
+        picuda.pi_liouvillian_gap("model", method="krylov", symmetry="auto")
+    with pytest.raises(picuda.PiArgumentError, match="cannot certify"):
+        picuda.pi_liouvillian_gap("model", method="harmonic")
+    with pytest.raises(picuda.PiArgumentError, match="method=:krylov"):
+        picuda.pi_liouvillian_gap("model", method="dense")
