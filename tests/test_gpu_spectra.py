@@ -210,3 +210,21 @@ def test_liouvillian_gap_from_device_arnoldi(torch_cuda):
         assert info["method"] == "arnoldi" and info["stationary_multiplicity_certified"]
     with pytest.raises(picuda.PiArgumentError):
         picuda.pi_liouvillian_gap(model, method="krylov", symmetry="auto")
+
+
+def test_liouvillian_spectrum_high_level(torch_cuda):
+    """liouvillian_spectrum (highlevel.jl:735-835) on the device: near zero it selects
+    harmonic Arnoldi, otherwise Arnoldi; with the default krylovdim = dim of the three-qubit
+    model both return the dense spectrum's selected values."""
+    model = picuda.PIModel(picuda.PIBasis(3, 2), [picuda.LocalJump(SM, rate=0.7), picuda.CollectiveJump(SM, rate=0.2)])
+    L = O.materialize(O.Plan(M.to_oracle(model)))
+    n = L.shape[0]
+    dense = np.linalg.eigvals(L)
+    near = picuda.liouvillian_spectrum(model, target="near_zero", nev=3, return_info=True, vectors=True)
+    assert near.info["selected_algorithm"] == "harmonic" and near.vectors.shape == (n, 3)
+    for v in near.values:
+        assert np.abs(dense - v).min() <= 1e-6
+    assert abs(near.values[0]) <= 1e-9
+    lr = picuda.liouvillian_spectrum(model, nev=3)
+    ref = dense[np.argsort(-dense.real, kind="stable")][:3]
+    assert np.allclose(np.sort_complex(lr), np.sort_complex(ref), atol=1e-6, rtol=0)

@@ -344,3 +344,66 @@ def test_gap_from_arnoldi_host_logic(monkeypatch):
         picuda.pi_liouvillian_gap("model", method="harmonic")
     with pytest.raises(picuda.PiArgumentError, match="method=:krylov"):
         picuda.pi_liouvillian_gap("model", method="dense")
+
+
+# ---- the high-level spectral command (liouvillian_spectrum, highlevel.jl:735-835) ---------
+
+def test_liouvillian_spectrum_dispatch(monkeypatch):
+    """Automatic selection (highlevel.jl:735-746): harmonic Arnoldi near zero, Arnoldi
+    otherwise; an explicit Arnoldi request near zero orders by smallest modulus; the
+    HarmonicArnoldiAlgorithm record fixes nev and the Krylov sizes.  The device solvers are
+    replaced by the oracle's Arnoldi and the library's harmonic algorithm over numpy."""
+    import types
+    L = _nonnormal(40, 7)  # a nonnormal matrix stands in for a compiled plan
+    n = L.shape[0]
+    calls = []
+
+    def arnoldi(compiled, nev=6, krylovdim=None, which="LR", initial_vector=None, atol=1e-10, rtol=1e-8,
+                vectors=False, rng=None, require_convergence=True):
+        calls.append(("arnoldi", which, nev, krylovdim))
+        return O.krylov_liouvillian_spectrum(lambda v: L @ v, n, nev=nev, krylovdim=krylovdim, which=which,
+                                             atol=atol, rtol=rtol, vectors=vectors, rng=rng,
+                                             require_convergence=require_convergence)
+
+    def harmonic(compiled, nev=6, krylovdim=None, thickdim=None, maxrestarts=20, target=0, initial_vector=None,
+                 initial_subspace=None, atol=1e-10, rtol=1e-8, vectors=False, rng=None, require_convergence=True):
+        calls.append(("harmonic", nev, krylovdim, thickdim, maxrestarts))
+        kd, td, t, v0, s0 = B._check_harmonic_arguments(n, nev, krylovdim, thickdim, maxrestarts, target,
+                                                        initial_vector, initial_subspace, None)
+        return B._harmonic_arnoldi(NumpySpace(L), n, nev, kd, td, maxrestarts, t, v0, s0, atol, rtol, vectors, rng,
+                                   require_convergence)
+
+    monkeypatch.setattr(B, "_as_compiled", lambda x: types.SimpleNamespace(basis=range(n)))
+    monkeypatch.setattr(B, "krylov_liouvillian_spectrum", arnoldi)
+    monkeypatch.setattr(B, "harmonic_arnoldi_spectrum", harmonic)
+    dense = np.linalg.eigvals(L)
+
+    near = picuda.liouvillian_spectrum("plan", target="near_zero", nev=3, maxrestarts=200, return_info=True)
+    assert calls[-1] == ("harmonic", 3, 20, None, 200)
+    assert isinstance(near, picuda.SpectrumResult) and near.vectors is None
+    assert near.info["selected_algorithm"] == "harmonic" and near.info["requested_algorithm"] == "auto"
+    nearest = dense[np.argsort(np.abs(dense), kind="stable")][:3]
+    assert np.allclose(np.sort_complex(near.values), np.sort_complex(nearest), atol=1e-7, rtol=0)
+
+    lr = picuda.liouvillian_spectrum("plan", nev=2, krylovdim=n)
+    assert calls[-1] == ("arnoldi", "LR", 2, n)
+    assert np.allclose(lr, dense[np.argsort(-dense.real, kind="stable")][:2], atol=1e-9, rtol=0)
+    lm = picuda.liouvillian_spectrum("plan", target="largest_magnitude", nev=2, krylovdim=n, vectors=True)
+    assert calls[-1] == ("arnoldi", "LM", 2, n)
+    assert set(lm) == {"values", "vectors"} and lm["vectors"].shape == (n, 2)
+    picuda.liouvillian_spectrum("plan", target="near_zero", algorithm="arnoldi", nev=2, krylovdim=n)
+    assert calls[-1] == ("arnoldi", "SM", 2, n)
+    alg = picuda.HarmonicArnoldiAlgorithm(nev=2, krylovdim=12, maxrestarts=300)
+    out = picuda.liouvillian_spectrum("plan", nev=5, algorithm=alg)
+    assert calls[-1] == ("harmonic", 2, 12, 4, 300) and out.shape == (2,)
+
+    with pytest.raises(picuda.PiArgumentError, match="target must be"):
+        picuda.liouvillian_spectrum("plan", target="smallest")
+    with pytest.raises(picuda.PiArgumentError, match="unsupported spectrum algorithm"):
+        picuda.liouvillian_spectrum("plan", algorithm="dense")
+    with pytest.raises(picuda.PiArgumentError, match="Bool"):
+        picuda.liouvillian_spectrum("plan", nev=True)
+    with pytest.raises(picuda.PiArgumentError, match="positive"):
+        picuda.liouvillian_spectrum("plan", nev=0)
+    with pytest.raises(picuda.PiArgumentError, match="exceeds the source dimension"):
+        picuda.liouvillian_spectrum("plan", algorithm=picuda.HarmonicArnoldiAlgorithm(nev=n + 1))
