@@ -172,6 +172,26 @@ def test_cooperative_fluorescence_exact_state():
     assert np.allclose(x, R.reshape(-1, order="F"), atol=3e-10)
 
 
+def test_collective_decay_initial_derivative():
+    """benchmark/comparison/README.md:26-45 (the matched_collective track): on the symmetric
+    irrep, L = gamma D[J-] with gamma = 0.37 acting on |N/2,N/2><N/2,N/2| for N = 4..64 gives
+    a trace-zero Hermitian derivative with |L rho|_F = sqrt(2) gamma N whose only nonzero
+    eigenvalues are +gamma N and -gamma N."""
+    sm = np.array([[0, 1], [0, 0]], dtype=np.complex128)
+    gamma = 0.37
+    for N in (4, 8, 16, 32, 64):
+        b = O.PIBasis(N, 2, sectors=[(N, 0)])
+        plan = O.Plan(O.PIModel(b, [O.CollectiveJump(sm, rate=gamma)]))
+        y = O.apply(plan, O.computational_product_state(b, 2))
+        assert abs(O.trace(plan, y)) <= 1e-12
+        assert abs(np.linalg.norm(y) - math.sqrt(2) * gamma * N) <= 1e-12 * N
+        Y = y.reshape(N + 1, N + 1, order="F")
+        assert np.abs(Y - Y.conj().T).max() <= 1e-14 * N
+        ev = np.linalg.eigvalsh((Y + Y.conj().T) / 2)
+        nonzero = np.sort(ev[np.abs(ev) > 1e-10])
+        assert np.allclose(nonzero, [-gamma * N, gamma * N], atol=1e-12 * N, rtol=0)
+
+
 def test_collective_local_radiation_expectations():
     """test/test_published_models.jl:446-457 (Zhang-Zhang-Molmer fluxes of Dicke states)."""
     b = O.PIBasis(4, 2)
