@@ -627,7 +627,11 @@ def harmonic_arnoldi_spectrum(L, nev=6, krylovdim=None, thickdim=None, maxrestar
     (Z^H Z, Z^H V) with Z = L V - sigma V, its eigenproblem, the ordering by distance to the
     target and the restart selection run on the host, as the reference hands them to LAPACK.
     Symmetry projectors are not provided (projector must be None).  Returns a dict with the
-    reference's result fields; `vectors` adds the (dim, nev) Ritz vectors."""
+    reference's result fields; `vectors` adds the (dim, nev) Ritz vectors.
+
+    The projections use pi_mdot_f64_noalloc, whose partial sums live in one array of the
+    library per device: two solves running at once on different streams of one device
+    (or a solve beside another caller of that function) must not overlap."""
     compiled = _as_compiled(L)
     n = len(compiled.basis)
     krylovdim, thickdim, t, v0, s0 = _check_harmonic_arguments(n, nev, krylovdim, thickdim, maxrestarts, target,
