@@ -9,6 +9,7 @@ is no CPU fallback: without the library or a GPU these functions raise.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -331,6 +332,9 @@ def krylov_liouvillian_spectrum(L, nev=6, krylovdim=None, which="LR", initial_ve
 # basis pi_combine_f64 combines.
 _MDOT_VECTORS = 32
 _COMBINE_VECTORS = 128
+# Serialises the solves of this process that use pi_mdot_f64_noalloc's shared scratch; each
+# solve has synchronised its last multi-dot before it releases the lock.
+_NOALLOC_LOCK = threading.Lock()
 
 
 class _DeviceKrylovSpace:
@@ -630,17 +634,18 @@ def harmonic_arnoldi_spectrum(L, nev=6, krylovdim=None, thickdim=None, maxrestar
     reference's result fields; `vectors` adds the (dim, nev) Ritz vectors.
 
     The projections use pi_mdot_f64_noalloc, whose partial sums live in one array of the
-    library per device: two solves running at once on different streams of one device
-    (or a solve beside another caller of that function) must not overlap."""
+    library per device, so the solves of one process run one at a time (a module lock); a
+    caller of that function outside this module must not overlap a solve."""
     compiled = _as_compiled(L)
     n = len(compiled.basis)
     krylovdim, thickdim, t, v0, s0 = _check_harmonic_arguments(n, nev, krylovdim, thickdim, maxrestarts, target,
                                                                initial_vector, initial_subspace, projector)
     rng = rng if rng is not None else np.random.default_rng()
     m = min(n, max(krylovdim, nev + 2))
-    space = _DeviceKrylovSpace(compiled, m)
-    return _harmonic_arnoldi(space, n, int(nev), krylovdim, thickdim, int(maxrestarts), t, v0, s0, float(atol),
-                             float(rtol), bool(vectors), rng, bool(require_convergence))
+    with _NOALLOC_LOCK:
+        space = _DeviceKrylovSpace(compiled, m)
+        return _harmonic_arnoldi(space, n, int(nev), krylovdim, thickdim, int(maxrestarts), t, v0, s0, float(atol),
+                                 float(rtol), bool(vectors), rng, bool(require_convergence))
 
 
 @dataclass
