@@ -16,7 +16,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import PiArgumentError, PiDimensionMismatch
-from .core import PIBasis, PIModel, PIOperator, PIState, collective_operator, spin_matrices
+from .core import PIModel, PIOperator, PIState, collective_operator
 
 _DEFAULT_MEMORY_BUDGET = 512 * 1024 ** 2
 

@@ -25,7 +25,7 @@ from numbers import Integral, Real
 import numpy as np
 
 from ._lib import PiArgumentError, PiDimensionMismatch, PiError, PiNotConverged
-from .core import PIModel, PIState, Term
+from .core import PIModel, Term
 
 _SCAN_TASKS = ("steady_state", "spectrum")
 _SCAN_EXECUTIONS = ("serial", "threads", "batched")

@@ -7,7 +7,6 @@ import numpy as np
 import pytest
 
 import picuda
-from picuda import _lib
 from tests import models as M
 
 pytestmark = pytest.mark.gpu
