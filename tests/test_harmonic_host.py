@@ -407,3 +407,41 @@ def test_liouvillian_spectrum_dispatch(monkeypatch):
         picuda.liouvillian_spectrum("plan", nev=0)
     with pytest.raises(picuda.PiArgumentError, match="exceeds the source dimension"):
         picuda.liouvillian_spectrum("plan", algorithm=picuda.HarmonicArnoldiAlgorithm(nev=n + 1))
+
+
+def test_arnoldi_spectral_scan_continuation_host_logic(monkeypatch):
+    """The spectral scan's Arnoldi branch (scans.jl:983-1041) with the device process
+    replaced by the oracle's restatement: the second point starts from v_1 + sum_c v_c / c
+    of the first point's Ritz vectors, normalised, and the restart seed is that vector."""
+    import types
+    from picuda import scans as S
+    from tests import models as M
+    spin = picuda.spin_matrices()
+    fam = picuda.compile_family(picuda.PIModel(picuda.PIBasis(3, 2), [picuda.LocalJump(spin["jm"], rate=1.0),
+                                                                      picuda.LocalJump(spin["jp"], rate=0.2)]))
+    seeds = []
+
+    def compile_point(plan, parameter, index):
+        made = plan.model_builder(parameter, index)
+        model = S._family_model(made.family, S._family_rates(made.family, made.rates))
+        return types.SimpleNamespace(basis=model.basis, matrix=O.materialize(O.Plan(M.to_oracle(model))))
+
+    def arnoldi(compiled, nev=6, krylovdim=None, which="LR", initial_vector=None, atol=1e-10, rtol=1e-8,
+                vectors=False, rng=None, require_convergence=True):
+        seeds.append(None if initial_vector is None else np.array(initial_vector))
+        n = len(compiled.basis)
+        return O.krylov_liouvillian_spectrum(lambda v: compiled.matrix @ v, n, nev=nev, krylovdim=krylovdim,
+                                             which=which, initial_vector=initial_vector, atol=atol, rtol=rtol,
+                                             vectors=vectors, rng=rng, require_convergence=require_convergence)
+
+    monkeypatch.setattr(S, "_compile_point", compile_point)
+    monkeypatch.setattr(B, "krylov_liouvillian_spectrum", arnoldi)
+    plan = picuda.ParameterScanPlan([0.2, 0.3], fam, rate_builder=lambda p: (1.0, p), task="spectrum", nev=3,
+                                    save_vectors=True, solver_options={"krylovdim": 20})
+    res = picuda.parameter_scan(plan, on_error="throw")
+    assert [p.warm_started for p in res] == [False, True]
+    assert seeds[0] is None
+    expected = S._arnoldi_continuation(res.points[0].output["vectors"])
+    assert np.array_equal(seeds[1], expected)
+    assert np.array_equal(res.restart_seed, S._arnoldi_continuation(res.points[1].output["vectors"]))
+    assert res.points[1].diagnostics["method"] == "arnoldi"
