@@ -1289,3 +1289,104 @@ def harmonic_arnoldi_spectrum(A, n, nev=6, krylovdim=None, thickdim=None, maxres
     if require_convergence:
         raise ValueError("thick-restarted harmonic Arnoldi did not converge")
     return best
+
+
+def _arnoldi_expand(A, V, H, first, last):
+    """_arnoldi_expand! (krylov.jl:1000-1015), 0-based columns first..last-1: two modified
+    Gram-Schmidt passes per step, breakdown at |h| <= eps * max(|L v_j|, tiny); returns the
+    number of basis columns with images."""
+    eps = np.finfo(float).eps
+    k = first
+    for j in range(first, last):
+        w = A(V[:, j])
+        image_norm = np.linalg.norm(w)
+        H[:j + 1, j] = 0
+        for _ in range(2):
+            for i in range(j + 1):
+                hij = np.vdot(V[:, i], w)
+                H[i, j] += hij
+                w = w - hij * V[:, i]
+        H[j + 1, j] = np.linalg.norm(w)
+        k = j + 1
+        if abs(H[j + 1, j]) <= eps * max(image_norm, np.finfo(float).tiny):
+            break
+        V[:, j + 1] = w / H[j + 1, j]
+    return k
+
+
+def _selected_ritz_order(values, which, target):
+    """_selected_ritz_order (krylov.jl:996-998)."""
+    if target is None:
+        return ritz_order(values, which)
+    return np.argsort(np.abs(values - target), kind="stable")
+
+
+def implicitly_restarted_arnoldi_spectrum(A, n, nev=6, krylovdim=None, retained_dimension=None, maxrestarts=20,
+                                          which="LR", target=None, initial_vector=None, atol=1e-10, rtol=1e-8,
+                                          vectors=False, rng=None, require_convergence=True):
+    """implicitly_restarted_arnoldi_spectrum (krylov.jl:1035-1110): m-step Arnoldi, then per
+    restart exact shifts at the unwanted Ritz values applied by implicit QR steps on the
+    Hessenberg matrix, truncation to the retained columns and re-expansion."""
+    if not (0 < nev <= n):
+        raise ValueError("nev must lie between 1 and the operator dimension")
+    krylovdim = max(30, 3 * nev + 6) if krylovdim is None else krylovdim
+    retained_dimension = max(nev, min(2 * nev, krylovdim - 1)) if retained_dimension is None else retained_dimension
+    m = min(n, max(krylovdim, nev + 1))
+    keep = min(m - 1, max(retained_dimension, nev))
+    eps = np.finfo(float).eps
+    V = np.zeros((n, m + 1), dtype=np.complex128)
+    H = np.zeros((m + 1, m), dtype=np.complex128)
+    if initial_vector is None:
+        rng = rng if rng is not None else np.random.default_rng(0)
+        q = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+    else:
+        q = np.array(initial_vector, dtype=np.complex128)
+    nq = np.linalg.norm(q)
+    if not nq > 0:
+        raise ValueError("initial_vector must be nonzero")
+    V[:, 0] = q / nq
+    t = None if target is None else complex(target)
+    k = _arnoldi_expand(A, V, H, 0, m)
+    applications = k
+    best = None
+    for cycle in range(maxrestarts + 1):
+        vals_all, Y_all = np.linalg.eig(H[:k, :k])
+        order = _selected_ritz_order(vals_all, which, t)
+        sel = order[:min(nev, k)]
+        vals, Y = vals_all[sel], Y_all[:, sel]
+        residuals = np.abs(H[k, k - 1] * Y[-1, :])
+        scale = max(max(np.linalg.norm(H[:k + 1, j]) for j in range(k)), np.finfo(float).tiny)
+        tol = atol + rtol * scale
+        converged = residuals <= tol
+        best = dict(values=vals, residuals=residuals, converged=converged, iterations=applications, restarts=cycle,
+                    krylov_dimension=m, retained_dimension=keep, dimension=n, which=which, target=t,
+                    algorithm="implicit_qr_arnoldi", residual_scale=scale, residual_tolerance=tol)
+        if vectors:
+            best["vectors"] = V[:, :k] @ Y
+        if vals.size >= nev and converged.all():
+            return best
+        if cycle == maxrestarts or k <= keep:
+            break
+        Hs = H[:k, :k].copy()
+        Qt = np.eye(k, dtype=np.complex128)
+        for shift in vals_all[order[keep:]]:
+            Q, _ = np.linalg.qr(Hs - shift * np.eye(k))
+            Hs = Q.conj().T @ Hs @ Q
+            Qt = Qt @ Q
+        Vp = V[:, :k] @ Qt
+        q = Vp[:, keep] * Hs[keep, keep - 1]
+        if H[k, k - 1] != 0:
+            q = q + (H[k, k - 1] * Qt[k - 1, keep - 1]) * V[:, k]
+        beta = _mgs2(q, Vp, keep)
+        if not beta > np.sqrt(eps) * max(scale, np.finfo(float).tiny):
+            break
+        V[:, :keep] = Vp[:, :keep]
+        V[:, keep] = q / beta
+        H[:] = 0
+        H[:keep, :keep] = Hs[:keep, :keep]
+        H[keep, keep - 1] = beta
+        k = _arnoldi_expand(A, V, H, keep, m)
+        applications += k - keep
+    if require_convergence:
+        raise ValueError("implicitly restarted Arnoldi did not converge")
+    return best

@@ -648,6 +648,163 @@ def harmonic_arnoldi_spectrum(L, nev=6, krylovdim=None, thickdim=None, maxrestar
                                  float(rtol), bool(vectors), rng, bool(require_convergence))
 
 
+def _ritz_order(values, which):
+    """_ritz_order (krylov.jl:893-898): stable order by largest real part, largest modulus or
+    smallest modulus."""
+    key = {"LR": -values.real, "LM": -np.abs(values), "SM": np.abs(values)}[which]
+    return np.argsort(key, kind="stable")
+
+
+def _arnoldi_expand(space, V, H, first, last):
+    """_arnoldi_expand! (krylov.jl:1000-1015) over the vector operations of `space`, 0-based
+    columns first..last-1 of the (m+1)-vector block V and the host Hessenberg matrix H: two
+    Gram-Schmidt passes per step (classical, as in _orthogonalize), breakdown at
+    |h| <= eps * max(|L v_j|, tiny).  Returns the number of basis vectors with images."""
+    eps = np.finfo(float).eps
+    k = first
+    w = space.copy(V[0])
+    for j in range(first, last):
+        space.apply(w, V[j])
+        image_norm = space.norm(w)
+        H[:j + 1, j] = 0
+        for _ in range(2):
+            h = space.dots(V, j + 1, w)
+            H[:j + 1, j] += h
+            space.subtract(w, V, j + 1, h)
+        H[j + 1, j] = space.norm(w)
+        k = j + 1
+        if abs(H[j + 1, j]) <= eps * max(image_norm, np.finfo(float).tiny):
+            break
+        V[j + 1] = w / float(H[j + 1, j].real)
+    return k
+
+
+def _iram(space, n, nev, krylovdim, retained_dimension, maxrestarts, which, target, initial_vector, atol, rtol,
+          vectors, rng, require_convergence):
+    """Implicitly restarted Arnoldi (krylov.jl:1035-1110) over the vector operations of
+    `space`: m-step Arnoldi, then per restart exact shifts at the unwanted Ritz values by
+    implicit QR steps on the host Hessenberg matrix, the basis rotated and truncated to the
+    retained vectors on the device (one combination), and re-expansion."""
+    eps = np.finfo(float).eps
+    tiny = np.finfo(float).tiny
+    m = min(n, max(krylovdim, nev + 1))
+    keep = min(m - 1, max(retained_dimension, nev))
+    V = space.block(m + 1)
+    H = np.zeros((m + 1, m), dtype=np.complex128)
+    if initial_vector is None:
+        initial_vector = (rng.standard_normal(n) + 1j * rng.standard_normal(n)) / np.sqrt(2)
+    q = space.upload(initial_vector)
+    nq = space.norm(q)
+    if not nq > 0:
+        raise PiArgumentError("initial_vector must be nonzero")
+    V[0] = q / nq
+    k = _arnoldi_expand(space, V, H, 0, m)
+    applications = k
+    history = []
+    best = None
+    order = sel = Y_all = None
+    for cycle in range(maxrestarts + 1):
+        vals_all, Y_all = np.linalg.eig(H[:k, :k])
+        order = np.argsort(np.abs(vals_all - target), kind="stable") if target is not None else \
+            _ritz_order(vals_all, which)
+        sel = order[:min(nev, k)]
+        vals = vals_all[sel]
+        residuals = np.abs(H[k, k - 1] * Y_all[-1, sel])
+        scale = max(max(np.linalg.norm(H[:k + 1, j]) for j in range(k)), tiny)
+        tolerance = atol + rtol * scale
+        converged = residuals <= tolerance
+        history.append(dict(cycle=cycle, subspace_dimension=k, converged=int(converged.sum()),
+                            maximum_residual=float(residuals.max()), residual_scale=scale))
+        best = dict(values=vals, residuals=residuals, converged=converged, iterations=applications, restarts=cycle,
+                    krylov_dimension=m, retained_dimension=keep, dimension=n, which=which, target=target,
+                    algorithm="implicit_qr_arnoldi", residual_scale=scale, residual_tolerance=tolerance,
+                    restart_history=list(history), workspace_reused=False, operator_applications=applications)
+        if vals.size >= nev and converged.all():
+            break
+        failure = (f"implicitly restarted Arnoldi did not converge in {maxrestarts} restarts; maximum requested "
+                   f"Ritz residual={residuals.max()}")
+        if cycle == maxrestarts or k <= keep:
+            if require_convergence:
+                raise PiArgumentError(failure)
+            break
+        # Exact unwanted Ritz shifts: by the implicit-Q theorem the first `keep` rotated
+        # vectors keep an Arnoldi factorisation.
+        Hs = H[:k, :k].copy()
+        Qt = np.eye(k, dtype=np.complex128)
+        for shift in vals_all[order[keep:]]:
+            Q, _ = np.linalg.qr(Hs - shift * np.eye(k))
+            Hs = Q.conj().T @ Hs @ Q
+            Qt = Qt @ Q
+        Vp = space.combine(V, k, Qt[:, :keep + 1])
+        # The new residual joins the retained Hessenberg coupling and the old residual.
+        q = Vp[keep] * complex(Hs[keep, keep - 1])
+        if H[k, k - 1] != 0:
+            q = q + complex(H[k, k - 1] * Qt[k - 1, keep - 1]) * V[k]
+        beta = _orthogonalize(space, q, Vp, keep)
+        if not beta > np.sqrt(eps) * max(scale, tiny):
+            if require_convergence:
+                raise PiArgumentError(failure)
+            break
+        V[:keep] = Vp[:keep]
+        V[keep] = q / beta
+        del Vp
+        H[:] = 0
+        H[:keep, :keep] = Hs[:keep, :keep]
+        H[keep, keep - 1] = beta
+        k = _arnoldi_expand(space, V, H, keep, m)
+        applications += k - keep
+    if vectors:
+        best["vectors"] = space.download(space.combine(V, k, Y_all[:, sel]))
+    return best
+
+
+def implicitly_restarted_arnoldi_spectrum(L, nev=6, krylovdim=None, retained_dimension=None, maxrestarts=20,
+                                          which="LR", target=None, initial_vector=None, atol=1e-10, rtol=1e-8,
+                                          vectors=False, rng=None, require_convergence=True):
+    """implicitly_restarted_arnoldi_spectrum(L; nev=6, krylovdim=max(30, 3nev+6),
+    retained_dimension=max(nev, min(2nev, krylovdim-1)), maxrestarts=20, which=:LR,
+    target=nothing, initial_vector, atol, rtol, vectors, rng, require_convergence)
+    (krylov.jl:1035-1110): eigenpairs at the spectral edge (:LR, :LM, :SM) or nearest
+    `target`, by Arnoldi with exact-shift implicit QR restarts.
+
+    The basis stays on the GPU (applies through pi_apply_f64, projections through
+    pi_mdot_f64_noalloc, the restart rotation and Ritz vectors through pi_combine_f64); the
+    Hessenberg matrix, its eigenproblem and the QR shift steps run on the host.  One solve
+    at a time per process, as for harmonic_arnoldi_spectrum."""
+    compiled = _as_compiled(L)
+    n = len(compiled.basis)
+    for name, value in (("nev", nev), ("maxrestarts", maxrestarts)):
+        if isinstance(value, bool) or not isinstance(value, (int, np.integer)):
+            raise PiArgumentError(f"{name} must be an integer")
+    if not (0 < nev <= n):
+        raise PiArgumentError("nev must lie between 1 and the operator dimension")
+    if which not in ("LR", "LM", "SM"):
+        raise PiArgumentError("which must be :LR, :LM, or :SM")
+    if maxrestarts < 0:
+        raise PiArgumentError("maxrestarts must be nonnegative")
+    if target is not None:
+        t = complex(target)
+        if not (np.isfinite(t.real) and np.isfinite(t.imag)):
+            raise PiArgumentError("Krylov target must be a finite number")
+        target = t
+    krylovdim = max(30, 3 * nev + 6) if krylovdim is None else int(krylovdim)
+    retained_dimension = (max(nev, min(2 * nev, krylovdim - 1)) if retained_dimension is None
+                          else int(retained_dimension))
+    m = min(n, max(krylovdim, nev + 1))
+    if m + 1 > _COMBINE_VECTORS:
+        raise PiArgumentError(f"the CUDA implicitly restarted Arnoldi process supports krylov dimensions up to "
+                              f"{_COMBINE_VECTORS - 1}")
+    if initial_vector is not None:
+        initial_vector = np.asarray(initial_vector, dtype=np.complex128)
+        if initial_vector.shape != (n,):
+            raise PiDimensionMismatch("initial_vector has wrong length")
+    rng = rng if rng is not None else np.random.default_rng()
+    with _NOALLOC_LOCK:
+        space = _DeviceKrylovSpace(compiled, m + 1)
+        return _iram(space, n, int(nev), krylovdim, retained_dimension, int(maxrestarts), which, target,
+                     initial_vector, float(atol), float(rtol), bool(vectors), rng, bool(require_convergence))
+
+
 @dataclass
 class SpectrumResult:
     """Typed high-level spectral result (highlevel.jl:215-219)."""
@@ -666,16 +823,16 @@ def liouvillian_spectrum(x, target="largest_real", nev=6, algorithm="auto", vect
 
     Automatic selection runs harmonic Arnoldi for target=:near_zero and Arnoldi otherwise
     (the reference's dense branch for dim <= 256 materialises the matrix; the CUDA path has
-    none).  An explicit Arnoldi request orders by largest real part, largest modulus or, for
-    :near_zero, smallest modulus; HarmonicArnoldiAlgorithm fixes nev, krylovdim, thickdim
-    and maxrestarts.  Remaining keywords (krylovdim, atol, rtol, initial_vector, rng,
+    none).  An explicit Arnoldi or implicitly restarted Arnoldi (:iram) request orders by
+    largest real part, largest modulus or, for :near_zero, smallest modulus;
+    HarmonicArnoldiAlgorithm fixes nev, krylovdim, thickdim and maxrestarts.  Remaining keywords (krylovdim, atol, rtol, initial_vector, rng,
     require_convergence, and for harmonic Arnoldi thickdim, maxrestarts, initial_subspace)
     go to the solver.  Returns the values, a dict of values and vectors, or with
     return_info=True a SpectrumResult whose info holds the solver's fields."""
     if target not in _SPECTRUM_TARGETS:
         raise PiArgumentError("target must be :largest_real, :near_zero, or :largest_magnitude")
     explicit = isinstance(algorithm, HarmonicArnoldiAlgorithm)
-    if not explicit and algorithm not in ("auto", "krylov", "arnoldi", "harmonic"):
+    if not explicit and algorithm not in ("auto", "krylov", "arnoldi", "harmonic", "iram", "implicit_qr"):
         raise PiArgumentError(f"unsupported spectrum algorithm {algorithm!r}; the CUDA path runs Arnoldi and "
                               "harmonic Arnoldi")
     if isinstance(nev, bool):
@@ -699,11 +856,12 @@ def liouvillian_spectrum(x, target="largest_real", nev=6, algorithm="auto", vect
         opts.update(kwargs)
         res = harmonic_arnoldi_spectrum(compiled, vectors=vectors, **opts)
     else:
-        method = "arnoldi"
+        method = "iram" if algorithm in ("iram", "implicit_qr") else "arnoldi"
         which = {"largest_real": "LR", "largest_magnitude": "LM", "near_zero": "SM"}[target]
         opts.setdefault("rng", np.random.default_rng(0))
         opts.update(kwargs)
-        res = krylov_liouvillian_spectrum(compiled, which=which, vectors=vectors, **opts)
+        solve = implicitly_restarted_arnoldi_spectrum if method == "iram" else krylov_liouvillian_spectrum
+        res = solve(compiled, which=which, vectors=vectors, **opts)
     take = min(requested, len(res["values"]))
     values = res["values"][:take]
     if not vectors and not return_info:
@@ -744,20 +902,22 @@ def _liouvillian_gap_info(values, atol, rtol, check_stability):
                 dimension=values.size)
 
 
-_GAP_METHODS = {"krylov": "arnoldi", "ordinary_arnoldi": "arnoldi", "arnoldi": "arnoldi"}
+_GAP_METHODS = {"krylov": "arnoldi", "ordinary_arnoldi": "arnoldi", "arnoldi": "arnoldi", "iram": "iram",
+                "implicit_qr": "iram"}
 
 
 def pi_liouvillian_gap(x, atol=1e-12, rtol=1e-10, check_stability=True, return_info=False, symmetry=None,
                        method="krylov", nev=6, krylovdim=None, require_convergence=True, initial_vector=None,
-                       rng=None):
+                       rng=None, retained_dimension=None, maxrestarts=20):
     """pi_liouvillian_gap(x; method=:krylov, nev, krylovdim=max(20, 2nev+4), atol, rtol,
     check_stability, return_info, initial_vector, rng) (spectra.jl:262-470, the Arnoldi
     branch :441-466): the asymptotic decay gap -max Re(lambda) outside the stationary
-    cluster, from the nev largest-real Ritz values of the device Arnoldi process.  The count
-    of stationary modes is certified when fewer than nev of the returned values are
+    cluster, from the nev largest-real Ritz values of the device Arnoldi process, or with
+    method=:iram of implicitly restarted Arnoldi (retained_dimension, maxrestarts).  The
+    count of stationary modes is certified when fewer than nev of the returned values are
     stationary.
 
-    The CUDA path provides the Arnoldi method only: the reference's default method=:dense
+    The CUDA path provides these two methods: the reference's default method=:dense
     materialises the matrix, and harmonic selection cannot certify a global gap without a
     symmetry projector (spectra.jl:414-422), which the CUDA path does not provide."""
     if not isinstance(method, str):
@@ -766,14 +926,21 @@ def pi_liouvillian_gap(x, atol=1e-12, rtol=1e-10, check_stability=True, return_i
         raise PiArgumentError("method=:harmonic selects modes nearest zero in modulus and cannot certify the global "
                               "largest-real Liouvillian gap; use method=:krylov")
     if method not in _GAP_METHODS:
-        raise PiArgumentError(f"the CUDA path computes Liouvillian gaps with method=:krylov, not :{method}")
+        raise PiArgumentError(f"the CUDA path computes Liouvillian gaps with method=:krylov or :iram, not :{method}")
     if symmetry is not None:
         raise PiArgumentError("use method=:harmonic for matrix-free symmetry projection")
     if isinstance(nev, bool) or not isinstance(nev, (int, np.integer)):
         raise PiArgumentError("nev must be an integer")
     krylovdim = max(20, 2 * nev + 4) if krylovdim is None else krylovdim
-    arn = krylov_liouvillian_spectrum(x, nev=nev, krylovdim=krylovdim, which="LR", initial_vector=initial_vector,
-                                      atol=atol, rtol=rtol, rng=rng, require_convergence=require_convergence)
+    if _GAP_METHODS[method] == "iram":
+        retained = max(nev, min(2 * nev, krylovdim - 1)) if retained_dimension is None else retained_dimension
+        arn = implicitly_restarted_arnoldi_spectrum(x, nev=nev, krylovdim=krylovdim, retained_dimension=retained,
+                                                    maxrestarts=maxrestarts, which="LR",
+                                                    initial_vector=initial_vector, atol=atol, rtol=rtol, rng=rng,
+                                                    require_convergence=require_convergence)
+    else:
+        arn = krylov_liouvillian_spectrum(x, nev=nev, krylovdim=krylovdim, which="LR", initial_vector=initial_vector,
+                                          atol=atol, rtol=rtol, rng=rng, require_convergence=require_convergence)
     info = _liouvillian_gap_info(arn["values"], atol, rtol, check_stability)
     # A partial spectrum certifies the returned slow mode, but not that every stationary
     # mode was counted when all nev returned values are stationary.

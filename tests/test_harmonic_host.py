@@ -445,3 +445,162 @@ def test_arnoldi_spectral_scan_continuation_host_logic(monkeypatch):
     assert np.array_equal(seeds[1], expected)
     assert np.array_equal(res.restart_seed, S._arnoldi_continuation(res.points[1].output["vectors"]))
     assert res.points[1].diagnostics["method"] == "arnoldi"
+
+
+# ---- implicitly restarted Arnoldi (krylov.jl:996-1110) -------------------------------------
+
+class TorchCpuSpace(NumpySpace):
+    """The device space's tensor semantics on CPU torch tensors: rows of complex128 tensors,
+    in-place row updates and Python-scalar arithmetic as on the GPU; the reductions and
+    combinations follow the C-ABI layouts (coefficients k x c column-major)."""
+
+    def __init__(self, A):
+        super().__init__(A)
+        self.torch = pytest.importorskip("torch")
+        self.At = self.torch.from_numpy(A)
+
+    def block(self, m):
+        return self.torch.zeros((m, self.n), dtype=self.torch.complex128)
+
+    def upload(self, v):
+        return self.torch.from_numpy(np.ascontiguousarray(v, dtype=np.complex128)).clone()
+
+    def copy(self, v):
+        return v.clone()
+
+    def download(self, rows):
+        return rows.numpy().T.copy()
+
+    def apply(self, dst, src):
+        assert dst.is_contiguous() and src.is_contiguous() and dst.shape == src.shape == (self.n,)
+        dst.copy_(self.At @ src)
+
+    def dots(self, M, k, q):
+        assert q.is_contiguous() and M[0].is_contiguous()
+        return (M[:k].conj() @ q).numpy()
+
+    def norm(self, q):
+        return float(self.torch.linalg.vector_norm(q))
+
+    def combine(self, M, k, Y):
+        Yc = np.ascontiguousarray(np.asarray(Y, dtype=np.complex128).T)  # the layout the C-ABI receives
+        coef = self.torch.from_numpy(Yc.reshape(-1)).reshape(Yc.shape[0], k)
+        return (coef @ M[:k]).contiguous()
+
+    def subtract(self, q, M, k, coef):
+        q.sub_(self.torch.from_numpy(np.ascontiguousarray(coef, dtype=np.complex128)) @ M[:k])
+
+
+def _host_iram(space, n, nev=6, krylovdim=None, retained_dimension=None, maxrestarts=20, which="LR", target=None,
+               initial_vector=None, atol=1e-10, rtol=1e-8, vectors=False, require_convergence=True):
+    kd = max(30, 3 * nev + 6) if krylovdim is None else krylovdim
+    rd = max(nev, min(2 * nev, kd - 1)) if retained_dimension is None else retained_dimension
+    return B._iram(space, n, nev, kd, rd, maxrestarts, which, None if target is None else complex(target),
+                   initial_vector, atol, rtol, vectors, np.random.default_rng(0), require_convergence)
+
+
+def test_oracle_iram_known_answers():
+    """test/test_krylov.jl:219-234: nev=2, krylovdim=10, retained_dimension=5,
+    maxrestarts=30, atol=1e-9, rtol=1e-7 reaches the two largest-real values within 2e-7
+    after at least one restart with |L X - X diag(values)| < 3e-7, and the gap from them
+    equals the dense gap within 2e-7."""
+    L = _pi_matrix()
+    n = L.shape[0]
+    dense = np.linalg.eigvals(L)
+    dense = dense[O.ritz_order(dense, "LR")]
+    r = O.implicitly_restarted_arnoldi_spectrum(lambda v: L @ v, n, nev=2, krylovdim=10, retained_dimension=5,
+                                                maxrestarts=30, initial_vector=_seed(n, 112), vectors=True,
+                                                atol=1e-9, rtol=1e-7)
+    assert r["algorithm"] == "implicit_qr_arnoldi" and r["restarts"] > 0
+    assert np.allclose(r["values"], dense[:2], atol=2e-7, rtol=0)
+    X = r["vectors"]
+    assert np.linalg.norm(L @ X - X * r["values"][None, :]) < 3e-7
+    gap = B._liouvillian_gap_info(r["values"], 1e-9, 1e-7, True)["gap"]
+    assert abs(gap - _dense_gap(L)) <= 2e-7
+
+
+@pytest.mark.parametrize("space_kind", ["numpy", "torch"])
+@pytest.mark.parametrize("case", ["pi", "nonnormal_LR", "nonnormal_LM", "target"])
+def test_library_iram_matches_oracle(space_kind, case):
+    if case == "pi":
+        A, kw = _pi_matrix(), dict(nev=2, krylovdim=10, retained_dimension=5, maxrestarts=30, atol=1e-9, rtol=1e-7)
+    elif case == "nonnormal_LR":
+        A, kw = _nonnormal(60, 3), dict(nev=3, krylovdim=20, maxrestarts=200)
+    elif case == "nonnormal_LM":
+        A, kw = _nonnormal(60, 4), dict(nev=3, krylovdim=20, maxrestarts=200, which="LM")
+    else:
+        A, kw = _nonnormal(50, 5), dict(nev=3, krylovdim=20, maxrestarts=300, target=-2.0 + 0.5j)
+    n = A.shape[0]
+    v0 = _seed(n, 9)
+    ref = O.implicitly_restarted_arnoldi_spectrum(lambda v: A @ v, n, initial_vector=v0, vectors=True, **kw)
+    space = NumpySpace(A) if space_kind == "numpy" else TorchCpuSpace(A)
+    got = _host_iram(space, n, initial_vector=v0, vectors=True, **kw)
+    assert got["converged"].all() and got["restarts"] == ref["restarts"]
+    assert got["iterations"] == ref["iterations"]
+    tol = got["residual_tolerance"]
+    assert np.allclose(got["values"], ref["values"], atol=max(1e-8, 10 * tol), rtol=0)
+    X = got["vectors"]
+    resid = np.linalg.norm(A @ X - X * got["values"][None, :], axis=0)
+    assert (resid <= 10 * tol).all(), (resid, tol)
+
+
+@pytest.mark.parametrize("space_kind", ["numpy", "torch"])
+def test_library_harmonic_over_torch_semantics(space_kind):
+    """The harmonic algorithm over the torch-tensor stand-in gives the numpy space's values."""
+    A = _nonnormal(60, 3)
+    v0 = _seed(60, 1)
+    n = 60
+    kd, td, t, vv, s0 = B._check_harmonic_arguments(n, 3, 20, None, 200, 0, v0, None, None)
+    space = NumpySpace(A) if space_kind == "numpy" else TorchCpuSpace(A)
+    got = B._harmonic_arnoldi(space, n, 3, kd, td, 200, t, vv, s0, 1e-10, 1e-8, True, np.random.default_rng(0), True)
+    ref = O.harmonic_arnoldi_spectrum(lambda v: A @ v, n, nev=3, krylovdim=20, maxrestarts=200, initial_vector=v0)
+    assert np.allclose(got["values"], ref["values"], atol=1e-8, rtol=0)
+    assert got["vectors"].shape == (60, 3)
+
+
+def test_library_iram_not_converged_and_checks():
+    A = _nonnormal(60, 3)
+    with pytest.raises(picuda.PiArgumentError, match="did not converge in 1 restarts"):
+        _host_iram(NumpySpace(A), 60, nev=3, krylovdim=8, maxrestarts=1, initial_vector=_seed(60, 1), atol=0, rtol=0)
+    out = _host_iram(NumpySpace(A), 60, nev=3, krylovdim=8, maxrestarts=1, initial_vector=_seed(60, 1), atol=0,
+                     rtol=0, vectors=True, require_convergence=False)
+    assert out["restarts"] == 1 and out["vectors"].shape == (60, 3)
+    with pytest.raises(picuda.PiArgumentError, match="nonzero"):
+        _host_iram(NumpySpace(A), 60, nev=3, initial_vector=np.zeros(60))
+
+
+def test_iram_gap_and_spectrum_dispatch(monkeypatch):
+    """test/test_krylov.jl:219-234 through pi_liouvillian_gap(method=:iram) and
+    liouvillian_spectrum(algorithm=:iram), with the device process replaced by the library's
+    algorithm over numpy: the gap equals the dense gap within 2e-7 and the values are the
+    two largest-real eigenvalues."""
+    import types
+    L = _pi_matrix()
+    n = L.shape[0]
+    calls = []
+
+    def iram(compiled, nev=6, krylovdim=None, retained_dimension=None, maxrestarts=20, which="LR", target=None,
+             initial_vector=None, atol=1e-10, rtol=1e-8, vectors=False, rng=None, require_convergence=True):
+        calls.append((nev, krylovdim, retained_dimension, maxrestarts, which))
+        return _host_iram(NumpySpace(L), n, nev=nev, krylovdim=krylovdim, retained_dimension=retained_dimension,
+                          maxrestarts=maxrestarts, which=which, target=target, initial_vector=initial_vector,
+                          atol=atol, rtol=rtol, vectors=vectors, require_convergence=require_convergence)
+
+    monkeypatch.setattr(B, "implicitly_restarted_arnoldi_spectrum", iram)
+    monkeypatch.setattr(B, "_as_compiled", lambda x: types.SimpleNamespace(basis=range(n)))
+    info = picuda.pi_liouvillian_gap("model", method="iram", nev=2, krylovdim=10, retained_dimension=5,
+                                     maxrestarts=30, return_info=True, initial_vector=_seed(n, 112), atol=1e-9,
+                                     rtol=1e-7)
+    assert calls[-1] == (2, 10, 5, 30, "LR")
+    assert abs(info["gap"] - _dense_gap(L)) <= 2e-7
+    assert info["method"] == "iram" and info["selection"] == "largest_real"
+    picuda.pi_liouvillian_gap("model", method="implicit_qr", nev=2, krylovdim=10, initial_vector=_seed(n, 112),
+                              atol=1e-9, rtol=1e-7)
+    assert calls[-1] == (2, 10, 4, 20, "LR")
+    res = picuda.liouvillian_spectrum("model", nev=2, algorithm="iram", krylovdim=10, retained_dimension=5,
+                                      maxrestarts=30, initial_vector=_seed(n, 112), atol=1e-9, rtol=1e-7,
+                                      return_info=True)
+    assert calls[-1] == (2, 10, 5, 30, "LR")
+    dense = np.linalg.eigvals(L)
+    assert np.allclose(res.values, dense[O.ritz_order(dense, "LR")][:2], atol=2e-7, rtol=0)
+    assert res.info["selected_algorithm"] == "iram"
