@@ -203,15 +203,15 @@ class ParameterScanPlan:
             # modulus.
             algorithm = algorithm or "auto"
             if not isinstance(algorithm, HarmonicArnoldiAlgorithm):
-                if algorithm not in ("auto", "krylov", "arnoldi", "harmonic"):
+                if algorithm not in ("auto", "krylov", "arnoldi", "harmonic", "iram", "implicit_qr"):
                     raise PiArgumentError(f"unsupported spectral scan algorithm {algorithm}; the CUDA path runs "
-                                          "Arnoldi and harmonic Arnoldi")
+                                          "Arnoldi, implicitly restarted Arnoldi and harmonic Arnoldi")
                 if algorithm == "harmonic" or (algorithm == "auto" and spectrum_target == "near_zero"):
                     algorithm = HarmonicArnoldiAlgorithm(nev=int(nev), krylovdim=soptions.pop("krylovdim", None),
                                                          thickdim=soptions.pop("thickdim", None),
                                                          maxrestarts=soptions.pop("maxrestarts", 20))
                 else:
-                    algorithm = "arnoldi"
+                    algorithm = "iram" if algorithm in ("iram", "implicit_qr") else "arnoldi"
             managed = ("return_info", "initial_vector", "workspace", "rng", "vectors", "nev", "subspace_dim",
                        "target", "memory_budget")
         forbidden = [k for k in managed if k in soptions]
@@ -351,12 +351,14 @@ def _point_rng(seed, index):
 
 
 def _spectrum_points(plan, selected, callback, on_error, kw):
-    """Spectral task (scans.jl:974-1053): one device Arnoldi or harmonic Arnoldi process per
-    point.  With continuation=True, harmonic Arnoldi starts from the previous point's Ritz
-    vectors as an initial subspace; Arnoldi starts from their combination v_1 + sum_c v_c / c,
-    normalised (scans.jl:1020-1041)."""
-    from .backend import HarmonicArnoldiAlgorithm, harmonic_arnoldi_spectrum, krylov_liouvillian_spectrum
+    """Spectral task (scans.jl:974-1053): one device Arnoldi, implicitly restarted Arnoldi or
+    harmonic Arnoldi process per point.  With continuation=True, harmonic Arnoldi starts
+    from the previous point's Ritz vectors as an initial subspace; the Arnoldi methods start
+    from their combination v_1 + sum_c v_c / c, normalised (scans.jl:1020-1041)."""
+    from .backend import (HarmonicArnoldiAlgorithm, harmonic_arnoldi_spectrum, implicitly_restarted_arnoldi_spectrum,
+                          krylov_liouvillian_spectrum)
     harmonic = isinstance(plan.algorithm, HarmonicArnoldiAlgorithm)
+    ordinary = implicitly_restarted_arnoldi_spectrum if plan.algorithm == "iram" else krylov_liouvillian_spectrum
     which = {"largest_real": "LR", "largest_magnitude": "LM", "near_zero": "SM"}[plan.spectrum_target]
     points, seed, stopped = [], None, False
     for index in selected:
@@ -375,9 +377,8 @@ def _spectrum_points(plan, selected, callback, on_error, kw):
                 res = harmonic_arnoldi_spectrum(compiled, initial_subspace=seed if warm else None,
                                                 vectors=want_vectors, rng=_point_rng(plan.seed, index), **opts)
             else:
-                res = krylov_liouvillian_spectrum(compiled, nev=plan.nev, which=which,
-                                                  initial_vector=seed if warm else None, vectors=want_vectors,
-                                                  rng=_point_rng(plan.seed, index), **kw)
+                res = ordinary(compiled, nev=plan.nev, which=which, initial_vector=seed if warm else None,
+                               vectors=want_vectors, rng=_point_rng(plan.seed, index), **kw)
             t2 = time.perf_counter()
             vecs = res.pop("vectors", None)
             if plan.continuation and vecs is not None and vecs.shape[1] > 0:
@@ -388,7 +389,7 @@ def _spectrum_points(plan, selected, callback, on_error, kw):
                                        float(res["residuals"].max()), None, bool(res["converged"].all()),
                                        res["iterations"], t1 - t0, t2 - t1, t2 - t0, warm, False,
                                        dict(solver=res, user=user, backend="cuda", dimension=n,
-                                            method="harmonic" if harmonic else "arnoldi"), None, None)
+                                            method="harmonic" if harmonic else plan.algorithm), None, None)
         except (PiError, ValueError) as err:
             _handle_failure(on_error, err)
             point = _failed(index, parameter, err, time.perf_counter() - t0)

@@ -604,3 +604,44 @@ def test_iram_gap_and_spectrum_dispatch(monkeypatch):
     dense = np.linalg.eigvals(L)
     assert np.allclose(res.values, dense[O.ritz_order(dense, "LR")][:2], atol=2e-7, rtol=0)
     assert res.info["selected_algorithm"] == "iram"
+
+
+def test_iram_spectral_scan_host_logic(monkeypatch):
+    """A spectral scan with algorithm=:iram runs implicitly restarted Arnoldi per point and
+    continues like Arnoldi, from the weighted combination of the previous Ritz vectors."""
+    import types
+    from picuda import scans as S
+    from tests import models as M
+    spin = picuda.spin_matrices()
+    fam = picuda.compile_family(picuda.PIModel(picuda.PIBasis(3, 2), [picuda.LocalJump(spin["jm"], rate=1.0),
+                                                                      picuda.LocalJump(spin["jp"], rate=0.2)]))
+    seeds = []
+
+    def compile_point(plan, parameter, index):
+        made = plan.model_builder(parameter, index)
+        model = S._family_model(made.family, S._family_rates(made.family, made.rates))
+        return types.SimpleNamespace(basis=model.basis, matrix=O.materialize(O.Plan(M.to_oracle(model))))
+
+    def iram(compiled, nev=6, krylovdim=None, retained_dimension=None, maxrestarts=20, which="LR", target=None,
+             initial_vector=None, atol=1e-10, rtol=1e-8, vectors=False, rng=None, require_convergence=True):
+        seeds.append(None if initial_vector is None else np.array(initial_vector))
+        n = len(compiled.basis)
+        v0 = initial_vector if initial_vector is not None else _seed(n, 5)
+        return _host_iram(NumpySpace(compiled.matrix), n, nev=nev, krylovdim=krylovdim, maxrestarts=maxrestarts,
+                          which=which, initial_vector=v0, atol=atol, rtol=rtol, vectors=vectors,
+                          require_convergence=require_convergence)
+
+    monkeypatch.setattr(S, "_compile_point", compile_point)
+    monkeypatch.setattr(B, "implicitly_restarted_arnoldi_spectrum", iram)
+    plan = picuda.ParameterScanPlan([0.2, 0.3], fam, rate_builder=lambda p: (1.0, p), task="spectrum", nev=2,
+                                    algorithm="iram", save_vectors=True,
+                                    solver_options={"krylovdim": 12, "maxrestarts": 50})
+    res = picuda.parameter_scan(plan, on_error="throw")
+    assert [p.status for p in res] == ["success", "success"]
+    assert [p.warm_started for p in res] == [False, True]
+    assert np.array_equal(seeds[1], S._arnoldi_continuation(res.points[0].output["vectors"]))
+    assert res.points[1].diagnostics["method"] == "iram"
+    for p, pt in zip([0.2, 0.3], res.points):
+        L = compile_point(plan, p, 0).matrix
+        dense = np.linalg.eigvals(L)
+        assert np.allclose(pt.output["values"], dense[O.ritz_order(dense, "LR")][:2], atol=1e-6, rtol=0)

@@ -110,6 +110,7 @@ def test_spectral_scan_plan_validation():
     assert picuda.ParameterScanPlan([1.0], build, task="spectrum", spectrum_target="near_zero",
                                     algorithm="arnoldi").algorithm == "arnoldi"
     assert picuda.ParameterScanPlan([1.0], build, task="spectrum").algorithm == "arnoldi"
+    assert picuda.ParameterScanPlan([1.0], build, task="spectrum", algorithm="implicit_qr").algorithm == "iram"
     with pytest.raises(picuda.PiArgumentError):
         picuda.ParameterScanPlan([1.0], build, task="spectrum", solver_options={"vectors": True})
     with pytest.raises(picuda.PiArgumentError):
