@@ -9,6 +9,8 @@ Three layers, no GPU:
     pi_mdot_f64_noalloc and pi_combine_f64;
   * argument checks and the algorithm record (HarmonicArnoldiAlgorithm, highlevel.jl:126-150).
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -645,3 +647,96 @@ def test_iram_spectral_scan_host_logic(monkeypatch):
         L = compile_point(plan, p, 0).matrix
         dense = np.linalg.eigvals(L)
         assert np.allclose(pt.output["values"], dense[O.ritz_order(dense, "LR")][:2], atol=1e-6, rtol=0)
+
+
+# ---- the device vector space's C-ABI marshalling, against a host model of the two calls ----
+
+class _HostLib:
+    """pi_mdot_f64_noalloc and pi_combine_f64 as include/picuda.h specifies them, computed
+    on host memory: V holds nv (or k) vectors of n complex at leading dimension ldv, h and
+    out receive the results, coef is k x ncols complex column-major."""
+
+    @staticmethod
+    def _view(ptr, count):
+        address = ptr.value if isinstance(ptr, C.c_void_p) else C.cast(ptr, C.c_void_p).value
+        return np.ctypeslib.as_array((C.c_double * (2 * count)).from_address(address)).view(np.complex128)
+
+    def __init__(self):
+        self.mdot_sizes = []
+
+    def pi_mdot_f64_noalloc(self, V, ldv, nv, w, n, h, stream):
+        assert 1 <= nv <= 32 and ldv >= n
+        self.mdot_sizes.append(nv)
+        Vm = self._view(V, ldv * nv).reshape(nv, ldv)[:, :n]
+        self._view(h, nv)[:] = Vm.conj() @ self._view(w, n)
+        return 0
+
+    def pi_combine_f64(self, plan, V, ldv, k, coef, ncols, out, ldo):
+        assert 1 <= k <= 128
+        n = ldv
+        Vm = self._view(V, ldv * k).reshape(k, ldv)[:, :n]
+        cm = self._view(coef, k * ncols).reshape(ncols, k)  # column c holds coef[0..k) of output c
+        self._view(out, ldo * ncols).reshape(ncols, ldo)[:, :n] = cm @ Vm
+        return 0
+
+
+def _host_device_space(A, m, monkeypatch):
+    """A _DeviceKrylovSpace whose tensors live on the host and whose library is _HostLib."""
+    import types
+    torch = pytest.importorskip("torch")
+
+    class TorchHost:
+        cuda = types.SimpleNamespace(synchronize=lambda: None,
+                                     current_stream=lambda: types.SimpleNamespace(cuda_stream=0))
+
+        def __getattr__(self, name):
+            return getattr(torch, name)
+
+        @staticmethod
+        def empty(*shape, dtype=None, device=None):
+            return torch.empty(*shape, dtype=dtype)
+
+        @staticmethod
+        def zeros(*shape, dtype=None, device=None):
+            return torch.zeros(*shape, dtype=dtype)
+
+    n = A.shape[0]
+    At = torch.from_numpy(A)
+
+    def apply(y, compiled, x):
+        y.copy_(At @ x)
+
+    monkeypatch.setattr(B, "apply_", apply)
+    monkeypatch.setattr(B, "_torch", lambda: TorchHost())
+    lib = _HostLib()
+    monkeypatch.setattr(B._lib, "load", lambda: lib)
+    space = B._DeviceKrylovSpace(types.SimpleNamespace(basis=range(n), handle=None), m)
+    space.upload = lambda v: torch.from_numpy(np.ascontiguousarray(v, dtype=np.complex128)).clone()
+    space.download = lambda rows: rows.numpy().T.copy()
+    return space, lib
+
+
+def test_device_space_marshalling_harmonic_and_iram(monkeypatch):
+    """The device space's pointers, leading dimensions, 32-vector multi-dot groups and
+    column-major coefficients, checked by running harmonic Arnoldi and implicitly restarted
+    Arnoldi with krylovdim 40 (projections over more than 32 vectors) against the oracle."""
+    A = _nonnormal(80, 6)
+    n = 80
+    v0 = _seed(n, 21)
+    space, lib = _host_device_space(A, 41, monkeypatch)
+    kd, td, t, vv, s0 = B._check_harmonic_arguments(n, 3, 40, None, 100, 0, v0, None, None)
+    got = B._harmonic_arnoldi(space, n, 3, kd, td, 100, t, vv, s0, 1e-10, 1e-8, True, np.random.default_rng(0),
+                              True)
+    ref = O.harmonic_arnoldi_spectrum(lambda v: A @ v, n, nev=3, krylovdim=40, maxrestarts=100, initial_vector=v0)
+    assert max(lib.mdot_sizes) == 32 and 8 in lib.mdot_sizes  # 40 = 32 + 8
+    assert got["restarts"] == ref["restarts"]
+    assert np.allclose(got["values"], ref["values"], atol=1e-8, rtol=0)
+    X = got["vectors"]
+    assert (np.linalg.norm(A @ X - X * got["values"][None, :], axis=0) <= 1.01 * got["residual_tolerance"]).all()
+    space, lib = _host_device_space(A, 41, monkeypatch)
+    got = B._iram(space, n, 3, 40, 6, 100, "LR", None, v0, 1e-10, 1e-8, True, np.random.default_rng(0), True)
+    ref = O.implicitly_restarted_arnoldi_spectrum(lambda v: A @ v, n, nev=3, krylovdim=40, retained_dimension=6,
+                                                  maxrestarts=100, initial_vector=v0)
+    assert max(lib.mdot_sizes) == 32 and 9 in lib.mdot_sizes  # the 41-vector block
+    assert got["restarts"] == ref["restarts"]
+    assert np.allclose(got["values"], ref["values"], atol=1e-8, rtol=0)
