@@ -199,7 +199,9 @@ int pi_dot_f64(pi_plan* plan, const double* a_dev, const double* b_dev, double* 
  * loads the library until exit), so it allocates nothing.  nv is limited to 32 (larger nv
  * is rejected).  The first call on a device looks up the array's device address and should
  * come before any stream capture.  Calls share the array: two calls that overlap on the GPU
- * race.  Asynchronous on `stream` (NULL = default stream). */
+ * race.  Asynchronous on `stream` (NULL = default stream).  The harmonic and implicitly
+ * restarted Arnoldi drivers (krylov.jl:996-1110, 1378-1551) project through it, in groups of
+ * at most 32 basis vectors. */
 int pi_mdot_f64_noalloc(const double* V_dev, long long ldv, int nv, const double* w_dev, long long n,
                         double* h_dev, void* stream);
 
