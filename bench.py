@@ -2,12 +2,16 @@
 
 Workload (one step): the fused L x of the N=120 qubit-ensemble model (H = 0.3 Jz + 1.2 Jx,
 local decay 0.2, local dephasing 0.1, collective decay 0.05/N; PI dimension 302,621) applied
-to a batch of 128 resident state vectors (inputs larger than L2, no flush needed), stored
-element-major by default (a (dim, 128) array; --layout columns for (128, dim)).  The
-headline is the FP32 apply (the mixed-precision path's inner operator) in population
-coordinates: value = algorithmic bytes (read x once, write y once) / device time.
-The FP64 apply, the end-to-end host-buffer call, the steady-state solve rate and the CPU
-baseline (C restatement of the reference's threaded apply) are reported beside it.
+to a batch of 128 resident state vectors (inputs larger than L2, no flush needed).  The
+headline is the plain complex FP64 apply on that batch in the reference's matrix layout
+(128 columns of the PI dimension, the layout of apply!(Y, compiled, X) on Julia matrices):
+value = algorithmic bytes (read x once, write y once) / device time; e2e is the same apply
+through the host-buffer C-ABI call pi_apply_host_f64 with the copies inside the timed
+region.  The FP32 apply of the mixed-precision path (element-major batch, population
+coordinates) is reported with its own roofline under "fp32"; steady-state, expv, RK4, scan
+and serving rates and the CPU baseline (C restatement of the reference's threaded apply)
+are reported beside them.  --impl reference times that CPU restatement on the same FP64
+workload.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -512,8 +516,21 @@ def cpu_baseline_apply(model_oracle_plan, n, budget_s=10.0, max_vectors=2000):
     return gbs, threads, count, dt
 
 
+WORKLOAD = ("fused L x, N=120 qubit ensemble (dim 302,621), batch of 128 state vectors as 128 columns "
+            "(the layout of apply!(Y, compiled, X)), complex FP64")
+
+
+def config_of(n):
+    """The workload's config, identical on both arms."""
+    return {"workload": WORKLOAD, "batch": BATCH, "pi_dim": n,
+            "model": "H=0.3Jz+1.2Jx, local decay 0.2, local dephasing 0.1, collective decay 0.05/N",
+            "l2": "inputs larger than L2 (620 MB read per step), no flush needed"}
+
+
 def run_reference(args, world, rank):
-    """--impl reference: the reference's CPU matrix-free apply (restated in C, threaded)."""
+    """--impl reference: the reference's CPU matrix-free apply (restated in C, threaded over
+    all host cores) on the headline workload: every step applies L to the same 128 FP64
+    columns."""
     if rank != 0:
         return 0
     import picuda
@@ -525,31 +542,52 @@ def run_reference(args, world, rank):
     n = len(plan)
     threads = os.cpu_count() or 1
     rng = np.random.default_rng(1)
-    per_step = 8
-    xs = [(rng.standard_normal(n) + 1j * rng.standard_normal(n)).astype(np.complex128) for _ in range(per_step)]
-    y = np.empty_like(xs[0])
+    X = (rng.standard_normal((BATCH, n)) + 1j * rng.standard_normal((BATCH, n))).astype(np.complex128)
+    Y = np.empty_like(X)
+
+    def step():
+        for c in range(BATCH):
+            ta(X[c], Y[c], threads)
+
     for _ in range(args.warmup):
-        for x in xs:
-            ta(x, y, threads)
+        step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for x in xs:
-            ta(x, y, threads)
+        step()
     dt = time.perf_counter() - t0
-    bytes_step = 2 * 16 * n * per_step
+    bytes_step = 2 * 16 * n * BATCH
     value = bytes_step * args.steps / dt / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": "L x, N=120 qubit ensemble (dim 302,621), FP64",
-                   "vectors_per_step": per_step, "l2": "inputs > L2 not applicable (CPU)"},
+        "config": config_of(n),
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} applies per step x {args.steps} steps, N=120, FP64"},
+                         "sample": f"{BATCH} FP64 applies per step x {args.steps} steps, N=120 (C restatement of "
+                                   "the reference's output-sector-owned threaded apply, all host threads)"},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def fp64_gemm_tflops(torch, size=4096, reps=5):
+    """FP64 throughput of a cuBLAS DGEMM (torch.matmul) on this GPU, measured in this run: the
+    denominator of the FP64-pipe fraction of the plain apply."""
+    a = torch.randn((size, size), dtype=torch.float64, device="cuda")
+    b = torch.randn((size, size), dtype=torch.float64, device="cuda")
+    c = a @ b
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(reps):
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2.0 * size ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b, c
+    return best
 
 
 def main():
@@ -629,11 +667,38 @@ def main():
     compiled = picuda.compile(model)
     n = len(model.basis)
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    peak, peak_kind = measured_peaks()
+
+    # Headline: the plain FP64 apply of 128 columns (pi_apply_f64 on torch's current stream,
+    # so the CUDA events on that stream bracket exactly the launches).
+    X64 = torch.randn((BATCH, n), dtype=torch.complex128, device="cuda", generator=g)
+    Y64 = torch.empty_like(X64)
+    for _ in range(args.warmup):
+        picuda.apply_(Y64, compiled, X64)
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            picuda.apply_(Y64, compiled, X64)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms64_rank = e0.elapsed_time(e1) / args.steps
+    bytes64 = 2 * 16 * n * BATCH
+    value, ms64 = replica_throughput(bytes64, ms64_rank, world)
+    achieved64 = bytes64 / (ms64_rank * 1e-3) / 1e9
+    flops64 = stencil_flops(picuda, model) * BATCH
+
+    # FP32 apply of the mixed-precision path (population coordinates), element-major batch
+    # by default; its own roofline.
     em = args.layout == "element-major"
     shape = (n, BATCH) if em else (BATCH, n)
     X32 = torch.randn(shape, dtype=torch.complex64, device="cuda", generator=g)
     Y32 = torch.empty_like(X32)
-    stream = torch.cuda.current_stream()
 
     def step32():
         if em:
@@ -641,65 +706,63 @@ def main():
         else:
             picuda.apply_(Y32, compiled, X32, precision="fp32", coords="population")
 
-    for _ in range(args.warmup):
+    for _ in range(max(args.warmup, 3)):
         step32()  # the first element-major call autotunes the kernel choice for this width
     torch.cuda.synchronize()
     em_choice = picuda.element_major_tuning(compiled, BATCH) if em else None
     barrier(world)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(args.steps):
-            step32()
-        e1.record(stream)
-        torch.cuda.synchronize()
-    barrier(world)
-    ms = e0.elapsed_time(e1) / args.steps
-    bytes32 = 2 * 8 * n * BATCH
-    value, ms = replica_throughput(bytes32, ms, world)
-    peak, peak_kind = measured_peaks()
-    achieved = bytes32 / (ms * 1e-3) / 1e9
-
-    # FP64 apply on the same batch (plain path), timed the same way
-    X64 = (X32.t().contiguous() if em else X32).to(torch.complex128)
-    Y64 = torch.empty_like(X64)
-    for _ in range(3):
-        picuda.apply_(Y64, compiled, X64)
+    k32 = max(args.steps, 20)
     torch.cuda.synchronize()
     e0.record(stream)
-    k64 = max(3, args.steps // 5)
-    for _ in range(k64):
-        picuda.apply_(Y64, compiled, X64)
+    for _ in range(k32):
+        step32()
     e1.record(stream)
     torch.cuda.synchronize()
-    ms64 = e0.elapsed_time(e1) / k64
-    bytes64 = 2 * 16 * n * BATCH
-    flops64 = stencil_flops(picuda, model) * BATCH
-    del X64, Y64
+    barrier(world)
+    ms32 = e0.elapsed_time(e1) / k32
+    bytes32 = 2 * 8 * n * BATCH
+    value32, ms32 = replica_throughput(bytes32, ms32, world)
+    achieved32 = bytes32 / (ms32 * 1e-3) / 1e9
 
     if args.only_apply:
         if rank == 0:
-            print(json.dumps({"only_apply": True, "ms_fp32": ms, "ms_fp64": ms64, "gbs_fp32": achieved,
-                              "kernel": em_choice}))
+            print(json.dumps({"only_apply": True, "ms_fp64": ms64, "gbs_fp64": achieved64, "ms_fp32": ms32,
+                              "gbs_fp32": achieved32, "kernel": em_choice}))
         return 0
 
-    # End to end through the host-buffer C-ABI call (pinned host memory, H2D + apply + D2H)
-    xh = (X32.t().contiguous() if em else X32).cpu().pin_memory()
-    yh = torch.empty_like(xh).pin_memory()
+    dgemm = fp64_gemm_tflops(torch) if rank == 0 else None
     lib = picuda.load_library()
     import ctypes as C
+    # End to end through the host-buffer C-ABI call, FP64: pinned host columns, H2D + apply +
+    # D2H inside the timed region, every step.
+    xh64 = X64.cpu().pin_memory()
+    yh64 = torch.empty_like(xh64).pin_memory()
+    del X64, Y64
+    for _ in range(2):
+        lib.pi_apply_host_f64(compiled.handle, C.c_void_p(yh64.data_ptr()), C.c_void_p(xh64.data_ptr()), BATCH)
+    k_e2e = max(3, args.steps // 5)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        rc = lib.pi_apply_host_f64(compiled.handle, C.c_void_p(yh64.data_ptr()), C.c_void_p(xh64.data_ptr()),
+                                   BATCH)
+        if rc != 0:
+            raise RuntimeError(picuda._lib.last_error())
+    e2e_s = (time.perf_counter() - t0) / k_e2e
+    e2e_s = max_over_ranks(e2e_s, world)
+    e2e_value = world * bytes64 / e2e_s / 1e9
+    del xh64, yh64
+    # The same for the FP32 apply (pi_apply_host_f32, columns, population coordinates).
+    xh = (X32.t().contiguous() if em else X32).cpu().pin_memory()
+    yh = torch.empty_like(xh).pin_memory()
     for _ in range(2):
         lib.pi_apply_host_f32(compiled.handle, C.c_void_p(yh.data_ptr()), C.c_void_p(xh.data_ptr()), BATCH, 1)
-    k_e2e = max(3, args.steps // 10)
     t0 = time.perf_counter()
     for _ in range(k_e2e):
         rc = lib.pi_apply_host_f32(compiled.handle, C.c_void_p(yh.data_ptr()), C.c_void_p(xh.data_ptr()), BATCH, 1)
         if rc != 0:
             raise RuntimeError(picuda._lib.last_error())
-    e2e_s = (time.perf_counter() - t0) / k_e2e
-    e2e_s = max_over_ranks(e2e_s, world)
-    e2e_value = world * bytes32 / e2e_s / 1e9
+    e2e32_s = max_over_ranks((time.perf_counter() - t0) / k_e2e, world)
+    del xh, yh, X32, Y32
 
     solves = solve_rates(picuda, torch) if rank == 0 else None
     scan = scan_rates(picuda, torch, args.scan_instances, args.scan_intervals) if rank == 0 else None
@@ -720,28 +783,37 @@ def main():
         cl = clocks.summary()
         line = {
             "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64", "data": "synthetic",
-            "config": {"workload": "fused L x, N=120 qubit ensemble (dim 302,621), batch of 128 resident "
-                                   "state vectors, FP32 population coordinates",
-                       "layout": ("element-major (dim, 128): pi_apply_f32_em" if em else
-                                  "columns (128, dim): pi_apply_f32"),
-                       "kernel": em_choice,
-                       "model": "H=0.3Jz+1.2Jx, local decay 0.2, local dephasing 0.1, collective decay 0.05/N",
-                       "batch": BATCH, "pi_dim": n, "l2": "inputs larger than L2 (310 MB per step read)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "peak_kind": peak_kind,
-                         "traffic": profile_traffic("apply_em_f32_batch128_N120" if em else
-                                                    "apply_f32_batch128_N120"),
-                         "algorithmic_bytes_per_launch": bytes32},
-            "fp64": {"value": bytes64 / (ms64 * 1e-3) / 1e9, "unit": "GB/s", "ms_per_step": ms64,
-                     "frac_hbm": bytes64 / (ms64 * 1e-3) / 1e9 / peak,
-                     "tflops": flops64 / (ms64 * 1e-3) / 1e12,
-                     "note": "plain FP64 apply on the same batch; FP64-ALU bound on GB300"},
-            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 8 * n * BATCH,
-                    "d2h_bytes_per_step": 8 * n * BATCH, "ms_per_step": e2e_s * 1e3,
-                    "call": "pi_apply_host_f32 (pinned host buffers)"},
+            "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": config_of(n),
+            "call": "pi_apply_f64 (k_apply_canon<double>: canonical-position register kernel)",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "roofline": {"bound": "hbm", "achieved": achieved64, "peak": peak, "unit": "GB/s",
+                         "frac": achieved64 / peak, "peak_kind": peak_kind,
+                         "traffic": profile_traffic("apply_f64_batch128_N120"),
+                         "algorithmic_bytes_per_launch": bytes64,
+                         "fp64_pipe": {"achieved_tflops": flops64 / (ms64_rank * 1e-3) / 1e12,
+                                       "peak_tflops": dgemm,
+                                       "frac": (flops64 / (ms64_rank * 1e-3) / 1e12 / dgemm) if dgemm else None,
+                                       "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
+                                       "algorithmic_flops_per_launch": flops64,
+                                       "note": "the FP64 apply is bound by GB300's FP64 pipe, not by HBM"}},
+            "e2e": {"value": e2e_value, "unit": "GB/s", "h2d_bytes_per_step": 16 * n * BATCH,
+                    "d2h_bytes_per_step": 16 * n * BATCH, "ms_per_step": e2e_s * 1e3,
+                    "call": "pi_apply_host_f64 (pinned host columns; copies and apply pipelined over three streams)"},
+            "fp32": {"value": value32, "unit": "GB/s", "ms_per_step": ms32, "steps": k32,
+                     "workload": "the same L x and batch in complex FP32, population coordinates (the operator of "
+                                 "the mixed-precision solvers)",
+                     "layout": ("element-major (dim, 128): pi_apply_f32_em" if em else "columns (128, dim): pi_apply_f32"),
+                     "kernel": em_choice,
+                     "roofline": {"bound": "hbm", "achieved": achieved32, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved32 / peak, "peak_kind": peak_kind,
+                                  "traffic": profile_traffic("apply_em_f32_batch128_N120" if em else
+                                                             "apply_f32_batch128_N120"),
+                                  "algorithmic_bytes_per_launch": bytes32},
+                     "e2e": {"value": world * bytes32 / e2e32_s / 1e9, "unit": "GB/s",
+                             "h2d_bytes_per_step": 8 * n * BATCH, "d2h_bytes_per_step": 8 * n * BATCH,
+                             "ms_per_step": e2e32_s * 1e3, "call": "pi_apply_host_f32 (pinned host buffers)"}},
             "solves": solves,
             "scan": scan,
             "serve": serve,

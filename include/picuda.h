@@ -36,7 +36,7 @@ extern "C" {
 #define PI_ERR_CUDA (-5)
 #define PI_ERR_UNSUPPORTED (-6)        /* model outside the CUDA backend (d != 2, p-body, ...) */
 #define PI_ERR_NO_DEVICE (-7)
-#define PI_ERR_BUSY (-8)               /* a handle used concurrently */
+#define PI_ERR_BUSY (-8)               /* a plan in use (PI_CONCURRENCY_REJECT) */
 
 /* Term kinds (terms.jl:118-149). Operators are 2x2 complex, column-major interleaved. */
 #define PI_TERM_HAMILTONIAN 0      /* CollectiveHamiltonian / LocalHamiltonian: rate/hbar */
@@ -89,6 +89,18 @@ int pi_plan_destroy(pi_plan* plan);
  * sectors swapped, offsets negated, coefficients conjugated and shifted), so every apply
  * and solver entry point runs it; destroy it with pi_plan_destroy. */
 int pi_plan_adjoint(const pi_plan* plan, pi_plan** out);
+
+/* Concurrent calls on one plan (solves, Arnoldi, RK4, host-buffer applies: every call that
+ * uses the plan's own stream, staging buffers or engine).  PI_CONCURRENCY_WAIT (the default)
+ * serializes them: a second host thread waits for the first, as the reference's locked
+ * MatrixFreeLiouvillian does for shared tasks (liouvillian.jl:35-60).  PI_CONCURRENCY_REJECT
+ * makes a call that finds the plan in use return PI_ERR_BUSY at once, the rule of the
+ * reference's per-task workspaces (threaded_apply.jl:575).  The device-pointer applies
+ * (pi_apply_f64, pi_apply_f32, pi_apply_f32_em) only read the plan and run on the caller's
+ * stream, so they never wait. */
+#define PI_CONCURRENCY_WAIT 0
+#define PI_CONCURRENCY_REJECT 1
+int pi_plan_set_concurrency(pi_plan* plan, int mode);
 
 typedef struct {
   int N;
@@ -197,8 +209,9 @@ int pi_dot_f64(pi_plan* plan, const double* a_dev, const double* b_dev, double* 
  * that fix their memory at start-up, enqueueing while a stream is captured -- its partial
  * sums live in a static device array inside this library (128 KiB, kept on every GPU that
  * loads the library until exit), so it allocates nothing.  nv is limited to 32 (larger nv
- * is rejected).  The first call on a device looks up the array's device address and should
- * come before any stream capture.  Calls share the array: two calls that overlap on the GPU
+ * is rejected).  Every call looks up the array's device address on the current device (a
+ * host-side lookup, valid again after a device reset); a CUDA error left pending by earlier
+ * work is reported, not cleared.  Calls share the array: two calls that overlap on the GPU
  * race.  Asynchronous on `stream` (NULL = default stream).  The harmonic and implicitly
  * restarted Arnoldi drivers (krylov.jl:996-1110, 1378-1551) project through it, in groups of
  * at most 32 basis vectors. */
@@ -232,6 +245,73 @@ int pi_combine_f64(pi_plan* plan, const double* V_dev, long long ldv, int k, con
 
 /* ---- steady state: krylov_steady_state (krylov.jl:797-891) -------------------------- */
 
+/* Level-sweep preconditioner: replaces schur_sector_preconditioner (krylov.jl:594-700),
+ * which LU-factors the dense n^2 x n^2 Schur blocks of L/s + v t^H (O(n^6) per sector).
+ * This one inverts, exactly and in O(dim) work, M = L0/s + v t^H, where L0 keeps every term
+ * of L that preserves the charge m - m' (all Jz-covariant dissipators, the diagonal of the
+ * Hamiltonian) and drops the terms that change it (a Jx or Jy drive).  L0 is block diagonal
+ * in the charge and, inside a charge block, block triangular over the levels m with
+ * tridiagonal blocks over the sectors, so one thread block per charge sweeps the levels
+ * with precomputed Thomas factors.  Used on the left in GMRES exactly like the reference's
+ * preconditioner argument (_gmres!, krylov.jl:732-787).  Models whose charge-keeping gains
+ * both raise and lower m (decay and pumping together) are rejected with
+ * PI_ERR_UNSUPPORTED; a singular level block without the single free dark-state entry
+ * needs regularization > 0 (added to the diagonal of L0/s, as in the reference).
+ * coords: PI_COORDS_POPULATION (FP32 sweeps; the coordinates whose norms weigh
+ * populations, the ones to use at large N) or PI_COORDS_REFERENCE (FP64 sweeps).
+ * operator_scale: 0 = estimate from 3 random probes in those coordinates.  The tables take
+ * about 64 bytes (population) or 120 bytes (reference) per PI coordinate. */
+typedef struct pi_precond pi_precond;
+typedef struct {
+  int coords;
+  int fp64;               /* sweep arithmetic: 1 FP64, 0 FP32 */
+  double operator_scale;  /* s */
+  double regularization;
+  int chains;             /* charge chains (thread blocks per apply) */
+  int levels;             /* (charge, level) blocks */
+  long long entries;      /* = dim */
+  int max_level;          /* sectors in the largest level block */
+  int direction;          /* -1: levels swept from high m to low m (decay-type gains) */
+  int singular;           /* 1: L0 singular, its free entry fixed by the trace */
+  size_t device_bytes;
+  double setup_seconds;
+} pi_precond_info_t;
+int pi_precond_create(pi_plan* plan, int coords, double regularization, double operator_scale,
+                      pi_precond** out);
+int pi_precond_destroy(pi_precond* precond);
+int pi_precond_info(const pi_precond* precond, pi_precond_info_t* out);
+/* z = M^-1 r (complex FP64 device vectors in the preconditioner's coordinates), enqueued on
+ * `stream`; the ldiv! of the reference's preconditioner object (krylov.jl:202-209). */
+int pi_precond_apply(const pi_precond* precond, double* z_dev, const double* r_dev, void* stream);
+
+/* Host-only inspection (no device): the tables pi_precond_create would upload for the model
+ * of pi_stencil_export's arguments, in FP64 (the sweep kernel reads them in FP32 for
+ * population coordinates).  Entries are ordered by charge chain, level (in sweep order) and
+ * sector.  Two-call pattern: with tables NULL only counts[0..3] = chains, levels, entries and
+ * d = 0 chain entries are written.  No counterpart in the reference. */
+typedef struct {
+  int* chain_lev;      /* chains + 1: first level record of every chain */
+  int* lev_ent;        /* levels + 1: first entry of every level record */
+  int* elem;           /* entries: element index in the PI vector */
+  double* W;           /* entries complex: 1/pivot (forward y_i = W_i r_i + A_i y_{i-1}) */
+  double* A;           /* entries complex */
+  double* C;           /* entries complex (backward u_i = y_i + C_i u_{i+1}) */
+  int* gsrc;           /* entries: three 10-bit sector positions in the previous level (1023 none) */
+  double* G;           /* 3 x entries complex: the gain coefficients */
+  double* t0;          /* d = 0 chain entries: trace weights */
+  double* v0;          /* d = 0 chain entries: the border vector v */
+  double* w0;          /* d = 0 chain entries complex: the sweep y_v of s v with the free equation
+                          dropped (mode 0) or s L0^-1 v (mode 1) */
+  int meta[8];         /* chain0, chain0_ent, mode (0 free entry, 1 Sherman-Morrison), free_ent,
+                          direction, max_level */
+  double sm_coef[2];   /* rho_v, the dropped equation's residual for s v (mode 0), or
+                          1 / (1 + t^H w0) (mode 1) */
+} pi_precond_tables_t;
+int pi_precond_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                      const double* ops, const double* rates, const double* hbar, int coords,
+                      double regularization, double operator_scale, long long* counts,
+                      pi_precond_tables_t* tables);
+
 typedef struct {
   int krylovdim;          /* GMRES restart length m (default 30) */
   int maxiter;            /* total Arnoldi steps (default 500) */
@@ -240,6 +320,12 @@ typedef struct {
   int precision;          /* PI_FP64, or PI_FP32 = FP32 inner applies with FP64 refinement */
   int use_initial;        /* 1: x_dev holds the initial state; 0: start from v = t/|t|^2 */
   int max_refinements;    /* PI_FP32 only: outer FP64 refinement cycles (default 200) */
+  int coords;             /* coordinates of the solve (PI_COORDS_*, default reference): in
+                             population coordinates the residual and trace tests weigh
+                             populations (the reference-coordinate norms of high-multiplicity
+                             sectors vanish at large N); x_dev stays in reference coordinates */
+  const pi_precond* preconditioner;  /* NULL (default) or a left preconditioner built for the
+                             same plan and coordinates; its operator scale is used */
 } pi_gmres_opts_t;
 
 typedef struct {
@@ -256,7 +342,11 @@ typedef struct {
 } pi_gmres_info_t;
 
 void pi_gmres_default_opts(pi_gmres_opts_t* opts);
-/* Solves for the trace-one stationary state into x_dev (complex FP64, device). */
+/* Solves for the trace-one stationary state into x_dev (complex FP64, device, reference
+ * coordinates).  The info residuals are those of the solve's coordinates.  With a
+ * preconditioner the convergence tests are the reference's preconditioned ones: the
+ * preconditioned residual against atol + rtol |P b| and the raw residual against
+ * atol + rtol |b| (krylov.jl:739-786). */
 int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts,
                     pi_gmres_info_t* info);
 

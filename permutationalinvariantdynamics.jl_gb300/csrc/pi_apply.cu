@@ -553,9 +553,10 @@ cudaError_t launch_apply_t(const DevicePlan& dp, const void* coef, const void* x
 
 cudaError_t launch_apply_f64(const DevicePlan& dp, const double* x, double* y, int ncols, long long ld,
                              const BorderArgs& border, cudaStream_t stream) {
+  const void* coef = border.coords ? dp.coef64z : dp.coef64;
   if (dp.fast_sr > 0 && ncols >= kFastMinCols)
-    return launch_apply_fast<double>(dp, dp.coef64, x, y, ncols, ld, border, stream);
-  return launch_apply_t<double>(dp, dp.coef64, x, y, ncols, ld, border, stream);
+    return launch_apply_fast<double>(dp, coef, x, y, ncols, ld, border, stream);
+  return launch_apply_t<double>(dp, coef, x, y, ncols, ld, border, stream);
 }
 
 cudaError_t launch_apply_f32(const DevicePlan& dp, const float* x, float* y, int ncols, long long ld,

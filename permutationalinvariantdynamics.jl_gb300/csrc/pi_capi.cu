@@ -14,6 +14,7 @@
 #include "../../include/picuda.h"
 #include "pi_batch.hpp"
 #include "pi_handle.hpp"
+#include "pi_precond.hpp"
 
 namespace picuda {
 
@@ -87,7 +88,7 @@ int upload_plan(pi_plan* plan) {
   const int S = (int)hp.sectors.size();
   std::vector<DevSector> sectors(S);
   std::vector<DevTerm> terms;
-  std::vector<double2> coef64;
+  std::vector<double2> coef64, coef64z;
   std::vector<float2> coef32x, coef32z;
   std::vector<DevTile> tiles;
   std::vector<int> diag_sector;
@@ -137,6 +138,7 @@ int upload_plan(pi_plan* plan) {
         auto pad4 = [&]() {
           while (coef64.size() % 4) {
             coef64.push_back(make_double2(0, 0));
+            coef64z.push_back(make_double2(0, 0));
             coef32x.push_back(make_float2(0, 0));
             coef32z.push_back(make_float2(0, 0));
           }
@@ -148,6 +150,7 @@ int upload_plan(pi_plan* plan) {
             coef64.push_back(make_double2(z.real(), z.imag()));
             coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
             coef32z.push_back(make_float2((float)(z.real() * ratio), (float)(z.imag() * ratio)));
+            coef64z.push_back(make_double2(z.real() * ratio, z.imag() * ratio));
           }
           pad4();
         }
@@ -159,6 +162,7 @@ int upload_plan(pi_plan* plan) {
             coef64.push_back(make_double2(z.real(), z.imag()));
             coef32x.push_back(make_float2((float)z.real(), (float)z.imag()));
             coef32z.push_back(make_float2((float)(z.real() * r), (float)(z.imag() * r)));
+            coef64z.push_back(make_double2(z.real() * r, z.imag() * r));
           }
           pad4();
         }
@@ -192,6 +196,7 @@ int upload_plan(pi_plan* plan) {
       fast_sr = max_sr <= 5 ? 5 : (max_sr <= 9 ? 9 : 13);
       while (coef64.size() % 4) {
         coef64.push_back(make_double2(0, 0));
+        coef64z.push_back(make_double2(0, 0));
         coef32x.push_back(make_float2(0, 0));
         coef32z.push_back(make_float2(0, 0));
       }
@@ -200,6 +205,7 @@ int upload_plan(pi_plan* plan) {
       const int zlen = ((hp.max_n + 3) / 4) * 4 + 4;
       for (int i = 0; i < zlen; ++i) {
         coef64.push_back(make_double2(0, 0));
+        coef64z.push_back(make_double2(0, 0));
         coef32x.push_back(make_float2(0, 0));
         coef32z.push_back(make_float2(0, 0));
       }
@@ -286,6 +292,7 @@ int upload_plan(pi_plan* plan) {
   if ((rc = upload(plan, terms, &plan->dev.terms))) return rc;
   if ((rc = upload(plan, tiles, &plan->dev.tiles))) return rc;
   if ((rc = upload(plan, coef64, &plan->dev.coef64))) return rc;
+  if ((rc = upload(plan, coef64z, &plan->dev.coef64z))) return rc;
   if ((rc = upload(plan, coef32x, &plan->dev.coef32x))) return rc;
   if ((rc = upload(plan, coef32z, &plan->dev.coef32z))) return rc;
   if ((rc = upload(plan, diag_sector, &plan->dev.diag_sector))) return rc;
@@ -450,6 +457,66 @@ int pi_stencil_export_adjoint(int N, int d, int nsectors, const int* sector_ks, 
   return export_plan(adjoint_host_plan(hp), counts, term_table, coef);
 }
 
+int pi_precond_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                      const double* ops, const double* rates, const double* hbar, int coords, double regularization,
+                      double operator_scale, long long* counts, pi_precond_tables_t* tables) {
+  if (!counts) return fail(PI_ERR_INVALID_ARGUMENT, "null counts");
+  if (coords != PI_COORDS_REFERENCE && coords != PI_COORDS_POPULATION)
+    return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
+  if (!(std::isfinite(regularization) && regularization >= 0))
+    return fail(PI_ERR_INVALID_ARGUMENT, "regularization must be finite and nonnegative");
+  if (!(std::isfinite(operator_scale) && operator_scale > 0))
+    return fail(PI_ERR_INVALID_ARGUMENT, "operator_scale must be finite and positive");
+  QubitPlan hp;
+  int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
+  if (rc) return rc;
+  LevelPrecondHost H;
+  std::string err;
+  rc = build_level_precond(hp, coords, regularization, operator_scale, &H, &err);
+  if (rc) return fail(rc, err);
+  const long long n0 = (long long)H.t0.size();
+  counts[0] = (long long)H.chain_lev.size() - 1;
+  counts[1] = (long long)H.lev_ent.size() - 1;
+  counts[2] = (long long)H.elem.size();
+  counts[3] = n0;
+  if (!tables) return PI_OK;
+  auto put = [](double* out, const std::vector<std::complex<double>>& v) {
+    if (!out) return;
+    for (size_t i = 0; i < v.size(); ++i) {
+      out[2 * i] = v[i].real();
+      out[2 * i + 1] = v[i].imag();
+    }
+  };
+  if (tables->chain_lev) std::copy(H.chain_lev.begin(), H.chain_lev.end(), tables->chain_lev);
+  if (tables->lev_ent) std::copy(H.lev_ent.begin(), H.lev_ent.end(), tables->lev_ent);
+  if (tables->elem) std::copy(H.elem.begin(), H.elem.end(), tables->elem);
+  if (tables->gsrc) std::copy(H.gsrc.begin(), H.gsrc.end(), tables->gsrc);
+  put(tables->W, H.W);
+  put(tables->A, H.A);
+  put(tables->C, H.C);
+  put(tables->G, H.G);
+  if (tables->t0) std::copy(H.t0.begin(), H.t0.end(), tables->t0);
+  if (tables->v0) std::copy(H.v0.begin(), H.v0.end(), tables->v0);
+  if (tables->w0) {
+    for (long long i = 0; i < n0; ++i) {
+      const std::complex<double> w = H.w0[i];
+      tables->w0[2 * i] = w.real();
+      tables->w0[2 * i + 1] = w.imag();
+    }
+  }
+  tables->meta[0] = H.chain0;
+  tables->meta[1] = H.chain0_ent;
+  tables->meta[2] = H.mode;
+  tables->meta[3] = H.free_ent;
+  tables->meta[4] = H.direction;
+  tables->meta[5] = H.max_level;
+  tables->meta[6] = 0;
+  tables->meta[7] = 0;
+  tables->sm_coef[0] = H.sm_coef.real();
+  tables->sm_coef[1] = H.sm_coef.imag();
+  return PI_OK;
+}
+
 int pi_collective_block(int N, int k, const double* op, double* out) {
   if (!op || !out) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
   if (N < 1 || k < 0 || 2 * k > N) return fail(PI_ERR_INVALID_ARGUMENT, "sector is not a two-row partition of N");
@@ -576,6 +643,14 @@ int pi_plan_adjoint(const pi_plan* plan, pi_plan** out) {
 
 int pi_plan_destroy(pi_plan* plan) {
   free_plan(plan);
+  return PI_OK;
+}
+
+int pi_plan_set_concurrency(pi_plan* plan, int mode) {
+  if (!plan) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  if (mode != PI_CONCURRENCY_WAIT && mode != PI_CONCURRENCY_REJECT)
+    return fail(PI_ERR_INVALID_ARGUMENT, "mode must be PI_CONCURRENCY_WAIT or PI_CONCURRENCY_REJECT");
+  plan->reject_concurrent.store(mode == PI_CONCURRENCY_REJECT ? 1 : 0);
   return PI_OK;
 }
 

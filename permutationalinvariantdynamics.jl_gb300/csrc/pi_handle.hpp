@@ -28,7 +28,12 @@ struct pi_plan {
   void* stage_y = nullptr;
   size_t stage_bytes = 0;
   cudaStream_t pipe[3] = {nullptr, nullptr, nullptr};
-  std::atomic<int> busy{0};
+  // Calls that use the plan's stream, staging buffers or engine hold call_mu.  By default a
+  // second caller waits (the locked MatrixFreeLiouvillian of liouvillian.jl:35-60); with
+  // reject_concurrent set it gets PI_ERR_BUSY instead (the workspace rule of
+  // threaded_apply.jl:575).  Recursive, like the reference's ReentrantLock.
+  std::recursive_mutex call_mu;
+  std::atomic<int> reject_concurrent{0};
   // Element-major batched apply (pi_apply_em.cu): tile list and merged coefficient planes,
   // built on first use (FP32 reference / population coordinates).
   std::mutex em_mu;
@@ -78,16 +83,22 @@ void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 
-// RAII guard that rejects concurrent use of one plan (threaded_apply.jl:575).
+// RAII guard around one call on a plan: waits for the plan's other callers (default), or,
+// when the plan was switched to rejection, fails at once (ok = false) while another thread
+// holds it.
 struct BusyGuard {
   pi_plan* p;
   bool ok;
   explicit BusyGuard(pi_plan* plan) : p(plan) {
-    int expected = 0;
-    ok = p->busy.compare_exchange_strong(expected, 1);
+    if (p->reject_concurrent.load()) {
+      ok = p->call_mu.try_lock();
+    } else {
+      p->call_mu.lock();
+      ok = true;
+    }
   }
   ~BusyGuard() {
-    if (ok) p->busy.store(0);
+    if (ok) p->call_mu.unlock();
   }
 };
 

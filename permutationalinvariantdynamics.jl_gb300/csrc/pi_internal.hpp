@@ -16,6 +16,7 @@ struct DevicePlan {
   const DevTerm* terms = nullptr;
   const DevTile* tiles = nullptr;
   const double2* coef64 = nullptr;   // coefficients in reference coordinates
+  const double2* coef64z = nullptr;  // FP64 coefficients in population coordinates
   const float2* coef32x = nullptr;   // FP32 coefficients in reference coordinates
   const float2* coef32z = nullptr;   // FP32 coefficients in population coordinates
   const int* diag_sector = nullptr;  // per diagonal entry: its sector
@@ -39,7 +40,8 @@ constexpr int kFastMinCols = 2;
 constexpr int kCanonPerPos = 3;
 constexpr int kCanonEntries = 5 + 9 * kCanonPerPos;  // 32
 
-// Apply kernels (pi_apply.cu).
+// Apply kernels (pi_apply.cu).  Both take border.coords: reference (0) or population (1)
+// coordinates.
 cudaError_t launch_apply_f64(const DevicePlan& dp, const double* x, double* y, int ncols, long long ld,
                              const BorderArgs& border, cudaStream_t stream);
 // FP32 action; border.coords selects reference (0) or population (1) coordinates.

@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(kReduceThreads)
 
 }  // namespace picuda
 
-#include <mutex>
+#include <string>
 
 #include "../../include/picuda.h"
 
@@ -617,25 +617,19 @@ extern "C" int pi_mdot_f64_noalloc(const double* V_dev, long long ldv, int nv, c
     return fail(PI_ERR_INVALID_ARGUMENT,
                 "nv must lie in 1:32, the capacity of the static scratch of pi_mdot_f64_noalloc");
   if (n < 1 || ldv < n) return fail(PI_ERR_DIMENSION, "need n >= 1 and ldv >= n");
-  // The address of the static array on the current device, looked up once per device with
-  // that device current (the host-side symbol is only a stand-in, not a device address).
-  static std::mutex mu;
-  static double2* addr[64] = {nullptr};
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if (dev < 0 || dev >= 64) return fail(PI_ERR_UNSUPPORTED, "device ordinal beyond 63");
-  double2* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-      if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the static scratch");
-      addr[dev] = (double2*)p;
-    }
-    scratch = addr[dev];
-  }
+  // An error left pending by earlier, unrelated work is reported as such (and left in place
+  // for its owner) rather than mistaken for a failure of the launches below.
+  cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess)
+    return fail(PI_ERR_CUDA, std::string("a CUDA error was pending before pi_mdot_f64_noalloc: ") +
+                                 cudaGetErrorString(e));
+  // The host-side symbol is only a stand-in: the array's device address on the current device
+  // is looked up on every call (a host-side table lookup once the module is loaded), so a
+  // device reset that loads the module again never leaves a stale address behind.
+  void* scratch_addr = nullptr;
+  e = cudaGetSymbolAddress(&scratch_addr, g_noalloc_partials);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the static scratch");
+  double2* scratch = (double2*)scratch_addr;
   const int gy = (nv + kDotGroup - 1) / kDotGroup;
   long long gx = (n + 4LL * kReduceThreads - 1) / (4LL * kReduceThreads);
   gx = std::max(1LL, std::min(gx, (long long)(kNoAllocBlocks / gy)));
@@ -644,8 +638,10 @@ extern "C" int pi_mdot_f64_noalloc(const double* V_dev, long long ldv, int nv, c
   // so nothing needs clearing; two calls that overlap on the GPU share the array and race.
   k_mdot_partial_noalloc<<<dim3((unsigned)gx, gy), kReduceThreads, 0, s>>>(
       (const double2*)V_dev, ldv, nv, (const double2*)w_dev, n, scratch);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "pi_mdot_f64_noalloc partial-sum launch");
   k_mdot_final_noalloc<<<nv, kReduceThreads, 0, s>>>(scratch, (int)gx, (double2*)h_dev);
   e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_fail(e, "pi_mdot_f64_noalloc launch");
+  if (e != cudaSuccess) return cuda_fail(e, "pi_mdot_f64_noalloc final-sum launch");
   return PI_OK;
 }

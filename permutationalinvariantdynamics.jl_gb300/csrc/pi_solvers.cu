@@ -21,6 +21,7 @@
 #include "pi_batch.hpp"
 #include "pi_dense.hpp"
 #include "pi_handle.hpp"
+#include "pi_precond.hpp"
 
 namespace picuda {
 namespace {
@@ -50,7 +51,8 @@ struct Run {
   long long n;
   cudaError_t err = cudaSuccess;
   int applications = 0;
-  explicit Run(pi_plan* plan) : p(plan), s(plan->stream), n(plan->host.dim) {}
+  int coords = 0;  // PI_COORDS_* of every vector of the solve
+  explicit Run(pi_plan* plan, int c = 0) : p(plan), s(plan->stream), n(plan->host.dim), coords(c) {}
   bool ok() const { return err == cudaSuccess; }
   void chk(cudaError_t e) {
     if (e != cudaSuccess && err == cudaSuccess) err = e;
@@ -71,37 +73,45 @@ struct Run {
   double norm(const double2* w) { return std::sqrt(norm2(w)); }
   // y = L x (unbordered)
   void apply(const double2* x, double2* y) {
-    BorderArgs b{1.0, nullptr, 0};
+    BorderArgs b{1.0, nullptr, coords};
     chk(launch_apply_f64(p->dev, (const double*)x, (double*)y, 1, n, b, s));
     ++applications;
   }
   // y = L x / scale + (t^H x) v  (krylov.jl:855-860)
   void apply_bordered(const double2* x, double2* y, double invscale, double2* alpha_dev) {
-    chk(trace_dot(p->dev, x, 0, 0, alpha_dev, s));
-    BorderArgs b{invscale, alpha_dev, 0};
+    chk(trace_dot(p->dev, x, 0, coords, alpha_dev, s));
+    BorderArgs b{invscale, alpha_dev, coords};
     chk(launch_apply_f64(p->dev, (const double*)x, (double*)y, 1, n, b, s));
     ++applications;
   }
-  void apply_bordered_f32(const float2* x, float2* y, double invscale, double2* alpha_dev, int coords) {
+  void apply_bordered_f32(const float2* x, float2* y, double invscale, double2* alpha_dev) {
     chk(trace_dot(p->dev, x, 1, coords, alpha_dev, s));
     BorderArgs b{invscale, alpha_dev, coords};
     chk(launch_apply_f32(p->dev, (const float*)x, (float*)y, 1, n, b, s));
     ++applications;
   }
+  // z = P r (left preconditioner of the bordered system); FP64 or FP32 in and out
+  void precondition(const pi_precond* P, const void* r, void* z, int f32) {
+    chk(precond_apply(P, r, f32, z, f32, precond_scale(P), s));
+  }
   cd trace(const double2* x) {
     double2* out = p->rs.result;
-    chk(trace_dot(p->dev, x, 0, 0, out, s));
+    chk(trace_dot(p->dev, x, 0, coords, out, s));
     double h[2] = {0, 0};
     fetch(h, out, sizeof(double2));
     return cd(h[0], h[1]);
   }
 };
 
-// Dense normalized trace vector v = t / (t^H t) in x coordinates.
+// Dense normalized trace vector v = t / (t^H t) in x coordinates (coords 0) or its image
+// in population coordinates (coords 1).
 __global__ void k_fill_border(const DevSector* __restrict__ sectors, const int* __restrict__ diag_sector,
-                              const long long* __restrict__ diag_index, int ndiag, double2* __restrict__ v) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndiag; i += gridDim.x * blockDim.x)
-    v[diag_index[i]] = make_double2(sectors[diag_sector[i]].border_x, 0.0);
+                              const long long* __restrict__ diag_index, int ndiag, double2* __restrict__ v,
+                              int coords) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndiag; i += gridDim.x * blockDim.x) {
+    const DevSector& sec = sectors[diag_sector[i]];
+    v[diag_index[i]] = make_double2(coords ? sec.border_z : sec.border_x, 0.0);
+  }
 }
 
 // r = b - w
@@ -191,30 +201,48 @@ double estimate_scale(Run& R, double2* probe, double2* image) {
   return scale;
 }
 
-// Restarted GMRES(m) on the bordered system (krylov.jl:732-787), FP64.
+// Restarted GMRES(m) on the bordered system (krylov.jl:732-787), FP64.  With a
+// preconditioner P it runs the reference's left-preconditioned form: the Krylov space of
+// P A, the preconditioned residual |P r| tested against atol + rtol |P b| and the raw residual
+// |r| against atol + rtol |b|, both after every restart (krylov.jl:737-786).
 GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, double rtol, int maxiter,
-                      double invscale, DeviceBuffers& buf) {
+                      double invscale, DeviceBuffers& buf, const pi_precond* P) {
   GmresResult res;
   const long long n = R.n;
   double2* V = (double2*)buf.get(sizeof(double2) * n * (m + 1));
   double2* w = (double2*)buf.get(sizeof(double2) * n);
   double2* r = (double2*)buf.get(sizeof(double2) * n);
+  double2* pz = P ? (double2*)buf.get(sizeof(double2) * n) : nullptr;
   double2* hd = (double2*)buf.get(sizeof(double2) * 2 * kMaxDots);
   double2* alpha = (double2*)buf.get(sizeof(double2) * 4);
   double2* yd = (double2*)buf.get(sizeof(double2) * kMaxDots);
-  if (!V || !w || !r || !hd || !alpha || !yd) {
+  if (!V || !w || !r || !hd || !alpha || !yd || (P && !pz)) {
     R.chk(buf.err);
     return res;
   }
   double2* h1d = hd;
   double2* h2d = hd + kMaxDots;
-  const double bnorm = R.norm(b);
+  const double raw_bnorm = R.norm(b);
+  const double rawtol = atol + rtol * raw_bnorm;
+  double bnorm = raw_bnorm;
+  if (P) {
+    R.precondition(P, b, pz, 0);
+    bnorm = R.norm(pz);
+  }
   const double tol = atol + rtol * bnorm;
-  R.apply_bordered(x, w, invscale, alpha);
-  R.chk((k_sub<<<grid_n(n), 256, 0, R.s>>>(b, w, r, n), cudaGetLastError()));
-  double beta = R.norm(r);
+  // residual of the current x: r = b - A x, its raw and (preconditioned) norms
+  auto residual = [&](double* rawbeta) {
+    R.apply_bordered(x, w, invscale, alpha);
+    R.chk((k_sub<<<grid_n(n), 256, 0, R.s>>>(b, w, r, n), cudaGetLastError()));
+    *rawbeta = R.norm(r);
+    if (!P) return *rawbeta;
+    R.precondition(P, r, pz, 0);
+    return R.norm(pz);
+  };
+  double rawbeta = 0.0;
+  double beta = residual(&rawbeta);
   res.residual = beta;
-  if (beta <= tol) {
+  if (beta <= tol && rawbeta <= rawtol) {
     res.converged = true;
     return res;
   }
@@ -224,33 +252,38 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
   while (res.iterations < maxiter && R.ok()) {
     for (auto& col : H) std::fill(col.begin(), col.end(), cd(0, 0));
     std::fill(g.begin(), g.end(), cd(0, 0));
-    R.chk(scale_f64(r, V, n, make_double2(1.0 / beta, 0.0), 0, R.s));
+    R.chk(scale_f64(P ? pz : r, V, n, make_double2(1.0 / beta, 0.0), 0, R.s));
     g[0] = beta;
     int kdone = 0;
     const int steps = std::min(m, maxiter - res.iterations);
     for (int j = 0; j < steps && R.ok(); ++j) {
       R.apply_bordered(V + (long long)j * n, w, invscale, alpha);
+      double2* q = w;
+      if (P) {
+        R.precondition(P, w, pz, 0);
+        q = pz;
+      }
       double rem2 = 0.0;
-      cgs2_f64(R, V, j + 1, w, h1d, h2d, H[j], &rem2);
+      cgs2_f64(R, V, j + 1, q, h1d, h2d, H[j], &rem2);
       H[j][j + 1] = std::sqrt(rem2);
       if (H[j][j + 1] != cd(0, 0))
-        R.chk(scale_f64(w, V + (long long)(j + 1) * n, n, make_double2(1.0 / H[j][j + 1].real(), 0.0), 0, R.s));
+        R.chk(scale_f64(q, V + (long long)(j + 1) * n, n, make_double2(1.0 / H[j][j + 1].real(), 0.0), 0, R.s));
       for (int i = 0; i < j; ++i) {
         const cd h1 = H[j][i], h2 = H[j][i + 1];
         H[j][i] = cs[i] * h1 + sn[i] * h2;
         H[j][i + 1] = -std::conj(sn[i]) * h1 + cs[i] * h2;
       }
       double c;
-      cd s;
-      complex_givens(H[j][j], H[j][j + 1], &c, &s);
+      cd sg;
+      complex_givens(H[j][j], H[j][j + 1], &c, &sg);
       cs[j] = c;
-      sn[j] = s;
+      sn[j] = sg;
       const cd h1 = H[j][j], h2 = H[j][j + 1];
-      H[j][j] = c * h1 + s * h2;
+      H[j][j] = c * h1 + sg * h2;
       H[j][j + 1] = 0.0;
       const cd g1 = g[j], g2 = g[j + 1];
-      g[j] = c * g1 + s * g2;
-      g[j + 1] = -std::conj(s) * g1 + c * g2;
+      g[j] = c * g1 + sg * g2;
+      g[j + 1] = -std::conj(sg) * g1 + c * g2;
       ++res.iterations;
       kdone = j + 1;
       if (std::abs(g[j + 1]) <= tol) break;
@@ -260,11 +293,9 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
     R.chk(cudaMemcpyAsync(yd, y.data(), sizeof(double2) * kdone, cudaMemcpyHostToDevice, R.s));
     R.chk(combine_f64(V, n, kdone, yd, x, n, 1, R.s));
     ++res.restarts;
-    R.apply_bordered(x, w, invscale, alpha);
-    R.chk((k_sub<<<grid_n(n), 256, 0, R.s>>>(b, w, r, n), cudaGetLastError()));
-    beta = R.norm(r);
+    beta = residual(&rawbeta);
     res.residual = beta;
-    if (beta <= tol) {
+    if (beta <= tol && rawbeta <= rawtol) {
       res.converged = true;
       return res;
     }
@@ -274,25 +305,37 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
 
 // Mixed-precision GMRES with FP64 iterative refinement: every restart cycle computes the
 // true bordered residual b - A x in FP64 and solves the correction equation with FP32
-// applies, an FP32 Krylov basis and FP64-accumulated CGS2; the update x += d is FP64.
+// applies, an FP32 Krylov basis and FP64-accumulated CGS2; the update x += d is FP64.  With
+// a preconditioner the correction equation is solved left-preconditioned (FP32 sweeps) and
+// the outer tests are the reference's pair: |P r| <= atol + rtol |P b| and
+// |r| <= atol + rtol |b|, with P r and r in FP64.
 GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol, double rtol, int maxiter,
-                        int max_refinements, double invscale, DeviceBuffers& buf, int* refinements) {
+                        int max_refinements, double invscale, DeviceBuffers& buf, int* refinements,
+                        const pi_precond* P) {
   GmresResult res;
   const long long n = R.n;
   float2* V = (float2*)buf.get(sizeof(float2) * n * (m + 1));
   float2* w = (float2*)buf.get(sizeof(float2) * n);
+  float2* pw = P ? (float2*)buf.get(sizeof(float2) * n) : nullptr;
   double2* w64 = (double2*)buf.get(sizeof(double2) * n);
   double2* r = (double2*)buf.get(sizeof(double2) * n);
+  double2* pz = P ? (double2*)buf.get(sizeof(double2) * n) : nullptr;
   double2* hd = (double2*)buf.get(sizeof(double2) * 2 * kMaxDots);
   double2* alpha = (double2*)buf.get(sizeof(double2) * 4);
   double2* yd = (double2*)buf.get(sizeof(double2) * kMaxDots);
-  if (!V || !w || !w64 || !r || !hd || !alpha || !yd) {
+  if (!V || !w || !w64 || !r || !hd || !alpha || !yd || (P && (!pw || !pz))) {
     R.chk(buf.err);
     return res;
   }
   double2* h1d = hd;
   double2* h2d = hd + kMaxDots;
-  const double bnorm = R.norm(b);
+  const double raw_bnorm = R.norm(b);
+  const double rawtol = atol + rtol * raw_bnorm;
+  double bnorm = raw_bnorm;
+  if (P) {
+    R.precondition(P, b, pz, 0);
+    bnorm = R.norm(pz);
+  }
   const double tol = atol + rtol * bnorm;
   // Inner solves stop at this relative reduction: FP32 applies cannot resolve the
   // correction much below it, and the FP64 outer residual restores the rest.
@@ -304,9 +347,14 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
   while (R.ok()) {
     R.apply_bordered(x, w64, invscale, alpha);
     R.chk((k_sub<<<grid_n(n), 256, 0, R.s>>>(b, w64, r, n), cudaGetLastError()));
-    const double beta = R.norm(r);
+    const double rawbeta = R.norm(r);
+    double beta = rawbeta;
+    if (P) {
+      R.precondition(P, r, pz, 0);
+      beta = R.norm(pz);
+    }
     res.residual = beta;
-    if (beta <= tol) {
+    if (beta <= tol && rawbeta <= rawtol) {
       res.converged = true;
       return res;
     }
@@ -314,34 +362,39 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
     ++*refinements;
     for (auto& col : H) std::fill(col.begin(), col.end(), cd(0, 0));
     std::fill(g.begin(), g.end(), cd(0, 0));
-    R.chk(f64_to_f32(r, V, n, 1.0 / beta, R.s));
+    R.chk(f64_to_f32(P ? pz : r, V, n, 1.0 / beta, R.s));
     g[0] = beta;
     const double itol = std::max(tol * 0.5, inner_rtol * beta);
     int kdone = 0;
     const int steps = std::min(m, maxiter - res.iterations);
     for (int j = 0; j < steps && R.ok(); ++j) {
-      R.apply_bordered_f32(V + (long long)j * n, w, invscale, alpha, 0);
+      R.apply_bordered_f32(V + (long long)j * n, w, invscale, alpha);
+      float2* q = w;
+      if (P) {
+        R.precondition(P, w, pw, 1);
+        q = pw;
+      }
       double rem2 = 0.0;
-      cgs2_f32(R, V, j + 1, w, h1d, h2d, H[j], &rem2);
+      cgs2_f32(R, V, j + 1, q, h1d, h2d, H[j], &rem2);
       H[j][j + 1] = std::sqrt(rem2);
       if (H[j][j + 1] != cd(0, 0))
-        R.chk(scale_f32(w, V + (long long)(j + 1) * n, n, make_double2(1.0 / H[j][j + 1].real(), 0.0), R.s));
+        R.chk(scale_f32(q, V + (long long)(j + 1) * n, n, make_double2(1.0 / H[j][j + 1].real(), 0.0), R.s));
       for (int i = 0; i < j; ++i) {
         const cd h1 = H[j][i], h2 = H[j][i + 1];
         H[j][i] = cs[i] * h1 + sn[i] * h2;
         H[j][i + 1] = -std::conj(sn[i]) * h1 + cs[i] * h2;
       }
       double c;
-      cd s;
-      complex_givens(H[j][j], H[j][j + 1], &c, &s);
+      cd sg;
+      complex_givens(H[j][j], H[j][j + 1], &c, &sg);
       cs[j] = c;
-      sn[j] = s;
+      sn[j] = sg;
       const cd h1 = H[j][j], h2 = H[j][j + 1];
-      H[j][j] = c * h1 + s * h2;
+      H[j][j] = c * h1 + sg * h2;
       H[j][j + 1] = 0.0;
       const cd g1 = g[j], g2 = g[j + 1];
-      g[j] = c * g1 + s * g2;
-      g[j + 1] = -std::conj(s) * g1 + c * g2;
+      g[j] = c * g1 + sg * g2;
+      g[j + 1] = -std::conj(sg) * g1 + c * g2;
       ++res.iterations;
       kdone = j + 1;
       if (std::abs(g[j + 1]) <= itol) break;
@@ -356,6 +409,26 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
 }
 
 }  // namespace
+
+// Operator scale of the plan in the given coordinates (3 complex normal probes,
+// krylov.jl:156-169), for a preconditioner built before the solve.
+int estimate_operator_scale(pi_plan* plan, int coords, double* out) {
+  BusyGuard guard(plan);
+  if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
+  Run R(plan, coords);
+  DeviceBuffers buf;
+  buf.s = R.s;
+  double2* t1 = (double2*)buf.get(sizeof(double2) * R.n);
+  double2* t2 = (double2*)buf.get(sizeof(double2) * R.n);
+  if (!t1 || !t2) return cuda_fail(buf.err, "operator-scale workspace");
+  const double s = estimate_scale(R, t1, t2);
+  if (!R.ok()) return cuda_fail(R.err, "operator-scale estimate");
+  if (!(std::isfinite(s) && s > 0))
+    return fail(PI_ERR_INVALID_ARGUMENT, "operator_scale must be finite and positive");
+  *out = s;
+  return PI_OK;
+}
+
 }  // namespace picuda
 
 using namespace picuda;
@@ -372,6 +445,8 @@ void pi_gmres_default_opts(pi_gmres_opts_t* o) {
   o->precision = PI_FP64;
   o->use_initial = 0;
   o->max_refinements = 200;
+  o->coords = PI_COORDS_REFERENCE;
+  o->preconditioner = nullptr;
 }
 
 int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, pi_gmres_info_t* info) {
@@ -382,9 +457,21 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
   if (!(opts->atol >= 0) || !(opts->rtol >= 0)) return fail(PI_ERR_INVALID_ARGUMENT, "tolerances must be nonnegative");
   if (opts->precision != PI_FP64 && opts->precision != PI_FP32)
     return fail(PI_ERR_INVALID_ARGUMENT, "precision must be PI_FP64 or PI_FP32");
+  if (opts->coords != PI_COORDS_REFERENCE && opts->coords != PI_COORDS_POPULATION)
+    return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
+  const pi_precond* P = opts->preconditioner;
+  if (P) {
+    if (precond_plan(P) != plan)
+      return fail(PI_ERR_INVALID_ARGUMENT, "the preconditioner was built for another compiled model");
+    if (precond_coords(P) != opts->coords)
+      return fail(PI_ERR_INVALID_ARGUMENT, "the preconditioner was built for other coordinates than the solve's");
+    const double ps = precond_scale(P);
+    if (opts->operator_scale > 0 && std::abs(opts->operator_scale - ps) > std::sqrt(2.2e-16) * ps)
+      return fail(PI_ERR_INVALID_ARGUMENT, "operator_scale is inconsistent with the prepared preconditioner");
+  }
   BusyGuard guard(plan);
   if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
-  if (opts->krylovdim <= kBatchMaxKrylov) {
+  if (opts->krylovdim <= kBatchMaxKrylov && !P && opts->coords == PI_COORDS_REFERENCE) {
     // one job of the plan's batched engine: each GMRES cycle on the device, Givens included
     SteadyJob job(plan, x_dev, *opts, 0x51ca1eULL, true);
     const int rc = run_single_job(plan, &job, opts->krylovdim, opts->precision == PI_FP32, "GMRES");
@@ -392,7 +479,8 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
     if (info) *info = job.info();
     return job.rc == PI_OK ? PI_OK : fail(job.rc, job.msg);
   }
-  Run R(plan);
+  const int coords = opts->coords;
+  Run R(plan, coords);
   const long long n = R.n;
   const int m = (int)std::min<long long>(opts->krylovdim, n);
   pi_gmres_info_t loc;
@@ -404,14 +492,19 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
     double2* v = (double2*)buf.get(sizeof(double2) * n);
     double2* t1 = (double2*)buf.get(sizeof(double2) * n);
     double2* t2 = (double2*)buf.get(sizeof(double2) * n);
-    if (!v || !t1 || !t2) return cuda_fail(buf.err, "solver workspace");
-    double2* x = (double2*)x_dev;
+    // the solve's vector: x itself, or z = sqrt(f) x in population coordinates
+    double2* x = coords == PI_COORDS_POPULATION ? (double2*)buf.get(sizeof(double2) * n) : (double2*)x_dev;
+    if (!v || !t1 || !t2 || !x) return cuda_fail(buf.err, "solver workspace");
     R.chk(cudaMemsetAsync(v, 0, sizeof(double2) * n, R.s));
     R.chk((k_fill_border<<<grid_n(plan->dev.ndiag), 256, 0, R.s>>>(plan->dev.sectors, plan->dev.diag_sector,
-                                                                    plan->dev.diag_index, plan->dev.ndiag, v),
+                                                                    plan->dev.diag_index, plan->dev.ndiag, v,
+                                                                    coords),
            cudaGetLastError()));
-    if (!opts->use_initial) R.chk(cudaMemcpyAsync(x, v, sizeof(double2) * n, cudaMemcpyDeviceToDevice, R.s));
-    double s = opts->operator_scale > 0 ? opts->operator_scale : estimate_scale(R, t1, t2);
+    if (!opts->use_initial)
+      R.chk(cudaMemcpyAsync(x, v, sizeof(double2) * n, cudaMemcpyDeviceToDevice, R.s));
+    else if (coords == PI_COORDS_POPULATION)
+      R.chk(x_to_z_f64(plan->dev, (const double2*)x_dev, x, 1.0, R.s));
+    double s = P ? precond_scale(P) : (opts->operator_scale > 0 ? opts->operator_scale : estimate_scale(R, t1, t2));
     if (!R.ok()) return cuda_fail(R.err, "operator-scale estimate");
     if (!(std::isfinite(s) && s > 0))
       return fail(PI_ERR_INVALID_ARGUMENT,
@@ -421,15 +514,15 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
     int refinements = 0;
     try {
       if (opts->precision == PI_FP64)
-        gr = gmres_f64(R, x, v, m, opts->atol, opts->rtol, opts->maxiter, 1.0 / s, buf);
+        gr = gmres_f64(R, x, v, m, opts->atol, opts->rtol, opts->maxiter, 1.0 / s, buf, P);
       else
         gr = gmres_mixed(R, x, v, m, opts->atol, opts->rtol, opts->maxiter, std::max(1, opts->max_refinements),
-                         1.0 / s, buf, &refinements);
+                         1.0 / s, buf, &refinements, P);
     } catch (const std::exception& ex) {
       return fail(PI_ERR_NOT_CONVERGED, ex.what());
     }
     if (!R.ok()) return cuda_fail(R.err, "GMRES");
-    // Final checks in the reference's terms (krylov.jl:868-873).
+    // Final checks in the reference's terms (krylov.jl:868-873), in the solve's coordinates.
     R.apply(x, t1);
     const double residual = R.norm(t1);
     const double normalized = residual / s;
@@ -437,6 +530,8 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
     const double terr = std::abs(tr - cd(1, 0));
     const double xn = R.norm(x);
     const double tol = opts->atol + opts->rtol * std::max(xn, 1.0);
+    if (coords == PI_COORDS_POPULATION) R.chk(z_to_x_f64(plan->dev, x, (double2*)x_dev, 1.0, 0, R.s));
+    R.chk(cudaStreamSynchronize(R.s));
     if (!R.ok()) return cuda_fail(R.err, "GMRES final check");
     loc.converged = gr.converged && normalized <= tol && terr <= opts->atol + opts->rtol;
     loc.iterations = gr.iterations;

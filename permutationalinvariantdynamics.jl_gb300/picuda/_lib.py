@@ -22,6 +22,9 @@ PI_ERR_UNSUPPORTED = -6
 PI_ERR_NO_DEVICE = -7
 PI_ERR_BUSY = -8
 
+PI_CONCURRENCY_WAIT = 0
+PI_CONCURRENCY_REJECT = 1
+
 PI_TERM_HAMILTONIAN = 0
 PI_TERM_LOCAL_JUMP = 1
 PI_TERM_COLLECTIVE_JUMP = 2
@@ -48,6 +51,11 @@ class PiNotConverged(PiError):
     """Krylov solve that did not converge (krylov.jl:873, krylov_extensions.jl:1559-1561)."""
 
 
+class PiBusy(PiError):
+    """A compiled model in use by another host thread, with concurrency mode "reject"
+    (the ThreadedLiouvillianWorkspace rule, threaded_apply.jl:575)."""
+
+
 class pi_capability_t(C.Structure):
     _fields_ = [("functional", C.c_int), ("supports_matrixfree_pi", C.c_int),
                 ("device_count", C.c_int), ("sm_count", C.c_int), ("cc_major", C.c_int),
@@ -65,7 +73,23 @@ class pi_plan_info_t(C.Structure):
 class pi_gmres_opts_t(C.Structure):
     _fields_ = [("krylovdim", C.c_int), ("maxiter", C.c_int), ("atol", C.c_double),
                 ("rtol", C.c_double), ("operator_scale", C.c_double), ("precision", C.c_int),
-                ("use_initial", C.c_int), ("max_refinements", C.c_int)]
+                ("use_initial", C.c_int), ("max_refinements", C.c_int), ("coords", C.c_int),
+                ("preconditioner", C.c_void_p)]
+
+
+class pi_precond_info_t(C.Structure):
+    _fields_ = [("coords", C.c_int), ("fp64", C.c_int), ("operator_scale", C.c_double),
+                ("regularization", C.c_double), ("chains", C.c_int), ("levels", C.c_int),
+                ("entries", C.c_longlong), ("max_level", C.c_int), ("direction", C.c_int),
+                ("singular", C.c_int), ("device_bytes", C.c_size_t), ("setup_seconds", C.c_double)]
+
+
+class pi_precond_tables_t(C.Structure):
+    _fields_ = [("chain_lev", C.POINTER(C.c_int)), ("lev_ent", C.POINTER(C.c_int)),
+                ("elem", C.POINTER(C.c_int)), ("W", C.POINTER(C.c_double)), ("A", C.POINTER(C.c_double)),
+                ("C", C.POINTER(C.c_double)), ("gsrc", C.POINTER(C.c_int)), ("G", C.POINTER(C.c_double)),
+                ("t0", C.POINTER(C.c_double)), ("v0", C.POINTER(C.c_double)), ("w0", C.POINTER(C.c_double)),
+                ("meta", C.c_int * 8), ("sm_coef", C.c_double * 2)]
 
 
 class pi_gmres_info_t(C.Structure):
@@ -154,6 +178,7 @@ PROTOTYPES = {
                                  C.POINTER(_P)]),
     "pi_plan_destroy": (C.c_int, [_P]),
     "pi_plan_info": (C.c_int, [_P, C.POINTER(pi_plan_info_t)]),
+    "pi_plan_set_concurrency": (C.c_int, [_P, C.c_int]),
     "pi_plan_sectors": (C.c_int, [_P, _I, _LL, _I]),
     "pi_plan_gt_patterns": (C.c_int, [_P, C.c_int, _I]),
     "pi_plan_trace_functional": (C.c_int, [_P, _LL, _D]),
@@ -173,6 +198,12 @@ PROTOTYPES = {
     "pi_mdot_f64_noalloc": (C.c_int, [_P, C.c_longlong, C.c_int, _P, C.c_longlong, _P, _P]),
     "pi_gmres_default_opts": (None, [C.POINTER(pi_gmres_opts_t)]),
     "pi_steady_state": (C.c_int, [_P, _P, C.POINTER(pi_gmres_opts_t), C.POINTER(pi_gmres_info_t)]),
+    "pi_precond_create": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.POINTER(_P)]),
+    "pi_precond_destroy": (C.c_int, [_P]),
+    "pi_precond_info": (C.c_int, [_P, C.POINTER(pi_precond_info_t)]),
+    "pi_precond_apply": (C.c_int, [_P, _P, _P, _P]),
+    "pi_precond_export": (C.c_int, [C.c_int, C.c_int, C.c_int, _I, C.c_int, _I, _D, _D, _D, C.c_int,
+                                    C.c_double, C.c_double, _LL, C.POINTER(pi_precond_tables_t)]),
     "pi_expv_default_opts": (None, [C.POINTER(pi_expv_opts_t)]),
     "pi_expv": (C.c_int, [_P, _P, C.c_double, C.POINTER(pi_expv_opts_t),
                           C.POINTER(pi_expv_info_t)]),
@@ -240,6 +271,8 @@ def check(rc: int, what: str = "libpicuda call") -> None:
         raise PiDimensionMismatch(msg)
     if rc == PI_ERR_NOT_CONVERGED:
         raise PiNotConverged(msg)
+    if rc == PI_ERR_BUSY:
+        raise PiBusy(msg)
     raise PiError(f"{msg} (status {rc})")
 
 

@@ -150,6 +150,17 @@ class CompiledPIModel:
     def isautonomous(self):
         return True
 
+    def set_concurrency(self, mode: str = "wait"):
+        """How concurrent calls on this compiled model from several host threads behave:
+        "wait" (default) serializes them like the reference's locked MatrixFreeLiouvillian
+        (liouvillian.jl:35-60); "reject" raises PiBusy in the later caller, the rule of the
+        reference's per-task workspaces (threaded_apply.jl:575)."""
+        modes = {"wait": _lib.PI_CONCURRENCY_WAIT, "reject": _lib.PI_CONCURRENCY_REJECT}
+        if mode not in modes:
+            raise PiArgumentError("mode must be 'wait' or 'reject'")
+        _lib.check(_lib.load().pi_plan_set_concurrency(self.handle, modes[mode]), "set_concurrency")
+        return self
+
     def adjoint(self):
         """The adjoint generator (pi_plan_adjoint), built on first use and kept with the model."""
         adj = getattr(self, "_adjoint", None)
@@ -1028,8 +1039,9 @@ class GMRESAlgorithm:
             raise PiArgumentError("krylovdim must be at least 1")
         if isinstance(self.maxiter, bool) or self.maxiter < 1:
             raise PiArgumentError("maxiter must be at least 1")
-        if self.preconditioner is not None:
-            raise PiArgumentError("the CUDA backend runs unpreconditioned GMRES")
+        if self.preconditioner is not None and not isinstance(self.preconditioner, LevelPreconditioner):
+            raise PiArgumentError("the CUDA backend takes a LevelPreconditioner (level_preconditioner(compiled)) "
+                                  "as the GMRES preconditioner")
         if self.precision not in ("fp64", "mixed"):
             raise PiArgumentError("precision must be 'fp64' or 'mixed'")
 
@@ -1141,9 +1153,108 @@ def _as_compiled(x) -> CompiledPIModel:
     raise PiArgumentError("expected a PIModel or a CompiledPIModel")
 
 
+_COORDS = {"reference": _lib.PI_COORDS_REFERENCE, "population": _lib.PI_COORDS_POPULATION}
+
+
+class LevelPreconditioner:
+    """Left preconditioner of the trace-fixed steady-state GMRES (pi_precond_create), the CUDA
+    path's counterpart of schur_sector_preconditioner (krylov.jl:594-700).
+
+    It inverts exactly, by level sweeps on the GPU, M = L0/s + v t', where L0 keeps every term
+    of L that preserves the charge m - m' (the Jz-covariant dissipators and the diagonal of
+    the Hamiltonian) and leaves out the drive (Jx, Jy), which changes it.  `coords` fixes the
+    coordinates of the solves it serves: "population" (z = sqrt(f) x, whose norms weigh
+    populations; FP32 sweeps) or "reference" (FP64 sweeps).  The operator scale s is
+    estimated from three random probes in those coordinates unless given, and the solve uses
+    it, as the reference's prepared preconditioner does."""
+
+    def __init__(self, compiled, coords="population", regularization=0.0, operator_scale=None):
+        if coords not in _COORDS:
+            raise PiArgumentError("coords must be 'reference' or 'population'")
+        self.compiled = _as_compiled(compiled)
+        self.coords = coords
+        handle = C.c_void_p()
+        _lib.check(_lib.load().pi_precond_create(self.compiled.handle, _COORDS[coords], float(regularization),
+                                                 float(operator_scale) if operator_scale else 0.0,
+                                                 C.byref(handle)), "level_preconditioner")
+        self._handle = handle
+        info = _lib.pi_precond_info_t()
+        _lib.check(_lib.load().pi_precond_info(handle, C.byref(info)), "pi_precond_info")
+        self.info = {f: getattr(info, f) for f, _ in info._fields_}
+
+    @property
+    def handle(self):
+        if self._handle is None:
+            raise _lib.PiError("the preconditioner has been closed")
+        return self._handle
+
+    @property
+    def operator_scale(self):
+        return self.info["operator_scale"]
+
+    def apply(self, z, r):
+        """z = M^-1 r for complex128 CUDA tensors in the preconditioner's coordinates
+        (the ldiv! of krylov.jl:202-209), on torch's current stream."""
+        torch = _torch()
+        n = len(self.compiled.basis)
+        if r.shape != (n,) or z.shape != (n,) or r.dtype != torch.complex128 or z.dtype != torch.complex128:
+            raise PiDimensionMismatch("preconditioner vector has wrong length or type")
+        stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _lib.check(_lib.load().pi_precond_apply(self.handle, _ptr(z), _ptr(r), stream), "ldiv!")
+        return z
+
+    def close(self):
+        if getattr(self, "_handle", None) is not None:
+            _lib.load().pi_precond_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def level_preconditioner(compiled, coords="population", regularization=0.0, operator_scale=None):
+    """Builds a LevelPreconditioner for a compiled model (see its docstring)."""
+    return LevelPreconditioner(compiled, coords=coords, regularization=regularization, operator_scale=operator_scale)
+
+
+def level_preconditioner_tables(model, coords="population", regularization=0.0, operator_scale=1.0):
+    """Host-only export of the preconditioner tables (pi_precond_export) for a PIModel: a
+    dict of numpy arrays; no device needed."""
+    lib = _lib.load()
+    kinds, ops, rates, hbar, ks = _term_arrays(model)
+    counts = np.zeros(4, dtype=np.int64)
+    args = (model.basis.N, model.basis.d, len(ks), _lib.iptr(ks), len(model.terms), _lib.iptr(kinds),
+            _lib.dptr(ops), _lib.dptr(rates), _lib.dptr(hbar), _COORDS[coords], float(regularization),
+            float(operator_scale), _lib.llptr(counts))
+    _lib.check(lib.pi_precond_export(*args, None), "pi_precond_export")
+    nc, nl, ne, n0 = (int(v) for v in counts)
+    out = dict(chain_lev=np.zeros(nc + 1, np.int32), lev_ent=np.zeros(nl + 1, np.int32), elem=np.zeros(ne, np.int32),
+               W=np.zeros(ne, np.complex128), A=np.zeros(ne, np.complex128), C=np.zeros(ne, np.complex128),
+               gsrc=np.zeros(ne, np.int32), G=np.zeros(3 * ne, np.complex128), t0=np.zeros(n0), v0=np.zeros(n0),
+               w0=np.zeros(n0, np.complex128))
+    t = _lib.pi_precond_tables_t()
+    for name in ("chain_lev", "lev_ent", "elem", "gsrc"):
+        setattr(t, name, out[name].ctypes.data_as(C.POINTER(C.c_int)))
+    for name in ("W", "A", "C", "G", "t0", "v0", "w0"):
+        setattr(t, name, out[name].ctypes.data_as(C.POINTER(C.c_double)))
+    _lib.check(lib.pi_precond_export(*args, C.byref(t)), "pi_precond_export")
+    meta = list(t.meta)
+    out.update(chain0=meta[0], chain0_ent=meta[1], mode=meta[2], free_ent=meta[3], direction=meta[4],
+               max_level=meta[5], sm_coef=complex(t.sm_coef[0], t.sm_coef[1]), operator_scale=float(operator_scale))
+    return out
+
+
 def stationary_state(x, algorithm=None, return_info=False, atol=1e-10, rtol=1e-8, operator_scale=None,
-                     initial_state=None, max_refinements=200):
-    """stationary_state(x; algorithm=GMRESAlgorithm(...)) (highlevel.jl:321-371) on the GPU."""
+                     initial_state=None, max_refinements=200, coords="reference"):
+    """stationary_state(x; algorithm=GMRESAlgorithm(...)) (highlevel.jl:321-371) on the GPU.
+
+    coords="population" runs the solve on z = sqrt(f) x, where the residual and trace tests
+    weigh populations (in reference coordinates the entries of high-multiplicity sectors
+    vanish from every norm at large N); the state is returned in reference coordinates
+    either way.  A LevelPreconditioner in the algorithm fixes the coordinates to its own."""
     torch = _torch()
     algorithm = algorithm or GMRESAlgorithm()
     if isinstance(algorithm, str):
@@ -1152,6 +1263,13 @@ def stationary_state(x, algorithm=None, return_info=False, atol=1e-10, rtol=1e-8
         algorithm = GMRESAlgorithm()
     compiled = _as_compiled(x)
     n = len(compiled.basis)
+    P = algorithm.preconditioner
+    if P is not None:
+        coords = P.coords
+        if P.compiled is not compiled:
+            raise PiArgumentError("the preconditioner was built for another compiled model")
+    if coords not in _COORDS:
+        raise PiArgumentError("coords must be 'reference' or 'population'")
     o = _lib.pi_gmres_opts_t()
     lib = _lib.load()
     lib.pi_gmres_default_opts(C.byref(o))
@@ -1161,6 +1279,8 @@ def stationary_state(x, algorithm=None, return_info=False, atol=1e-10, rtol=1e-8
     o.operator_scale = float(operator_scale) if operator_scale else 0.0
     o.precision = _lib.PI_FP32 if algorithm.precision == "mixed" else _lib.PI_FP64
     o.max_refinements = max_refinements
+    o.coords = _COORDS[coords]
+    o.preconditioner = P.handle if P is not None else None
     xd = torch.zeros(n, dtype=torch.complex128, device="cuda")
     if initial_state is not None:
         init = initial_state.data if isinstance(initial_state, PIState) else np.asarray(initial_state)
@@ -1177,7 +1297,8 @@ def stationary_state(x, algorithm=None, return_info=False, atol=1e-10, rtol=1e-8
         return rho
     d = {f: getattr(info, f) for f, _ in info._fields_}
     d.update(method="krylov", krylov_dimension=algorithm.krylovdim, precision=algorithm.precision,
-             state=rho.data)
+             state=rho.data, coords=coords, preconditioned=P is not None,
+             preconditioner="LevelPreconditioner" if P is not None else None)
     return SteadyStateResult(rho, d, algorithm)
 
 
@@ -1508,6 +1629,9 @@ def stationary_state_batch(models, algorithm: GMRESAlgorithm | None = None, atol
     converged=False (a scan keeps the points that did converge)."""
     torch = _torch()
     algorithm = algorithm or GMRESAlgorithm()
+    if algorithm.preconditioner is not None:
+        raise PiArgumentError("batched steady states run unpreconditioned; solve preconditioned steady states "
+                              "with stationary_state")
     compiled = [_as_compiled(m) for m in models]
     n = len(compiled)
     o = _lib.pi_gmres_opts_t()

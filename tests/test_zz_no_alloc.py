@@ -1,4 +1,4 @@
-"""The allocation-free multi-dot (pi_mdot_f64_noalloc) against the plan-owned dot.
+"""The allocation-free multi-dot (pi_mdot_f64_noalloc) against the plan-owned dot and numpy.
 
 pi_mdot_f64_noalloc serves callers that cannot allocate device memory when they reduce --
 for example a Julia caller whose device memory belongs to its own pool, or a serving loop
@@ -35,6 +35,12 @@ def _dot_existing(lib, compiled, a, b):
     return complex(out[0], out[1])
 
 
+def _noalloc(lib, V, ldv, nv, w, n, h):
+    rc = lib.pi_mdot_f64_noalloc(C.c_void_p(V.data_ptr()), ldv, nv, C.c_void_p(w.data_ptr()), n,
+                                 C.c_void_p(h.data_ptr()), None)
+    _lib.check(rc, "pi_mdot_f64_noalloc")
+
+
 def test_noalloc_multidot_matches_plan_dot_twice(torch_cuda):
     torch = torch_cuda
     lib = picuda.load_library()
@@ -46,14 +52,47 @@ def test_noalloc_multidot_matches_plan_dot_twice(torch_cuda):
         V = torch.randn((nv, n), dtype=torch.complex128, device="cuda", generator=g)
         w = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
         h = torch.full((nv,), complex(np.nan, np.nan), dtype=torch.complex128, device="cuda")
-        rc = lib.pi_mdot_f64_noalloc(C.c_void_p(V.data_ptr()), n, nv, C.c_void_p(w.data_ptr()), n,
-                                     C.c_void_p(h.data_ptr()), None)
-        _lib.check(rc, "pi_mdot_f64_noalloc")
+        _noalloc(lib, V, n, nv, w, n, h)
         torch.cuda.synchronize()
         got = h.cpu().numpy()
         for i in range(nv):
             ref = _dot_existing(lib, compiled, V[i], w)
             assert abs(got[i] - ref) <= TOL * max(abs(ref), 1.0), (call, i, got[i], ref)
+
+
+# n = 200,003 with ldv > n: the partial-sum grid reaches the cap of 256 blocks shared by
+# the 8-vector groups (gy = 4 groups of 8 at nv = 32, 2 at nv = 9 with a partly filled last
+# group, 1 at nv = 1).
+@pytest.mark.parametrize("nv", [1, 9, 32])
+def test_noalloc_multidot_groups_and_leading_dimension(torch_cuda, nv):
+    torch = torch_cuda
+    lib = picuda.load_library()
+    compiled = picuda.compile(M.ensemble_c2(30))
+    n, ldv = 200_003, 200_003 + 37
+    g = torch.Generator(device="cuda").manual_seed(100 + nv)
+    for call in range(2):
+        Vs = torch.randn((nv, ldv), dtype=torch.complex128, device="cuda", generator=g)
+        w = torch.randn(n, dtype=torch.complex128, device="cuda", generator=g)
+        h = torch.full((nv,), complex(np.nan, np.nan), dtype=torch.complex128, device="cuda")
+        _noalloc(lib, Vs, ldv, nv, w, n, h)
+        torch.cuda.synchronize()
+        got = h.cpu().numpy()
+        Vh = Vs.cpu().numpy()[:, :n]
+        wh = w.cpu().numpy()
+        ref = Vh.conj() @ wh
+        bound = np.abs(Vh) @ np.abs(wh)  # sum |V_i||w|: the scale of the rounding error
+        assert np.all(np.abs(got - ref) <= TOL * bound), (call, nv, np.max(np.abs(got - ref) / bound))
+        # the existing entry point on the plan's dot: only defined for vectors of the plan's
+        # length, so compare the first group of columns cut to a PI vector of that length
+        npi = len(compiled.basis)
+        for i in range(min(nv, 3)):
+            a = Vs[i, :npi].contiguous()
+            b = w[:npi].contiguous()
+            h1 = torch.empty(1, dtype=torch.complex128, device="cuda")
+            _noalloc(lib, a, npi, 1, b, npi, h1)
+            torch.cuda.synchronize()
+            ref1 = _dot_existing(lib, compiled, a, b)
+            assert abs(h1.cpu().numpy()[0] - ref1) <= TOL * max(abs(ref1), 1.0)
 
 
 def test_noalloc_multidot_rejects_too_many_vectors(torch_cuda):
