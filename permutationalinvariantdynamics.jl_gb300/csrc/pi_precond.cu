@@ -36,16 +36,20 @@
 // chain.
 //
 // Device layout: one thread block per charge chain (2 n_max - 1 chains, the longest first),
-// two warps each.  Warp 1 stages the next level's right-hand sides and factors into shared
-// memory while warp 0 runs the current level: all lanes form the right-hand sides from the
-// previous level's solution, then lane 0 runs the forward and backward Thomas recurrences
-// and all lanes write the level's entries out.  Population coordinates run in FP32 (the
+// four warps each.  A ring of four shared-memory level slots keeps the sweep fed: warps 1-3
+// copy the factors of level l+3 and gather r at the elements of level l+2 with cp.async
+// (each thread gathers the entries whose indices it copied), while warp 0 solves level l.
+// Warp 0 subtracts the gains from the previous level's solution and runs both Thomas
+// recurrences as warp-wide scans of affine maps (each lane composes a chunk of at most five
+// entries, five shuffle steps combine the lanes), so a level costs a few dozen dependent
+// steps however many sectors it spans.  Population coordinates run in FP32 (the
 // preconditioner is an approximation of L^-1 either way, and every entry is a bounded
 // population); reference coordinates run in FP64, since their entries span many decades at
 // large N.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <complex>
@@ -62,7 +66,7 @@ namespace picuda {
 
 namespace {
 
-constexpr int kSweepThreads = 64;
+constexpr int kSweepThreads = 128;
 constexpr int kNoGain = 1023;
 
 template <typename T>
@@ -118,7 +122,7 @@ __device__ __forceinline__ void store_as<float2, double2>(float2* p, double2 v) 
   *p = make_float2((float)v.x, (float)v.y);
 }
 
-// Block-wide sum of two doubles per thread over a 64-thread block (fixed order).
+// Block-wide sum of two doubles per thread (fixed order).
 __device__ __forceinline__ double2 block_sum2(double2 v, double* red) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -141,108 +145,228 @@ __device__ __forceinline__ double2 block_sum2(double2 v, double* red) {
   return out;
 }
 
-template <typename T>
-struct Stage {
+constexpr int kStagers = kSweepThreads - 32;  // warps 1.. stage levels ahead of warp 0
+constexpr int kChunk = (kPrecondMaxLevel + 31) / 32;  // entries per lane of warp 0
+constexpr int kSlots = 4;                      // level ring: solved, gathered, copied, in flight
+constexpr int kMaxChainLevels = 2 * kPrecondMaxLevel + 4;
+
+__device__ __forceinline__ float2 shfl_up_c(float2 v, int d) {
+  return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+__device__ __forceinline__ double2 shfl_up_c(double2 v, int d) {
+  return make_double2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+__device__ __forceinline__ float2 shfl_down_c(float2 v, int d) {
+  return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+__device__ __forceinline__ double2 shfl_down_c(double2 v, int d) {
+  return make_double2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+
+__device__ __forceinline__ void cpa(void* smem, const void* gmem, int bytes) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(smem);
+  if (bytes == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(a), "l"(gmem) : "memory");
+  else if (bytes == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpa_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// One staged level: r at the level's elements (as stored) and the level's factors and gain
+// tables.
+template <typename T, typename TI>
+struct Slot {
   using T2 = typename V2<T>::type;
-  T2 rhs[2][kPrecondMaxLevel];   // s r of each entry
-  T2 w[2][kPrecondMaxLevel];     // 1 / pivot
-  T2 a[2][kPrecondMaxLevel];     // forward multiplier
-  T2 c[2][kPrecondMaxLevel];     // backward multiplier
-  T2 g[2][kPrecondMaxLevel][3];  // gain coefficients
-  int gp[2][kPrecondMaxLevel];   // packed gain positions in the previous level
-  int el[2][kPrecondMaxLevel];   // element index
-  T2 y[kPrecondMaxLevel];        // forward values
-  T2 u[2][kPrecondMaxLevel];     // solution of the previous / current level
-  double red[2 * (kSweepThreads / 32)];
+  TI rv[kPrecondMaxLevel];    // r at the level's elements
+  T2 w[kPrecondMaxLevel];     // 1 / pivot
+  T2 a[kPrecondMaxLevel];     // forward multiplier
+  T2 c[kPrecondMaxLevel];     // backward multiplier
+  T2 g[3][kPrecondMaxLevel];  // gain coefficients
+  int gp[kPrecondMaxLevel];   // packed gain positions in the previous level
+  int el[kPrecondMaxLevel];   // element index
 };
 
 template <typename T, typename TI>
-__device__ __forceinline__ void stage_level(const PrecondDev& P, const TI* __restrict__ r, Stage<T>& S, int slot,
-                                            int lev, int lane, double s) {
+struct SweepSmem {
   using T2 = typename V2<T>::type;
-  const T2* W = reinterpret_cast<const T2*>(P.W);
-  const T2* A = reinterpret_cast<const T2*>(P.A);
-  const T2* C = reinterpret_cast<const T2*>(P.C);
-  const T2* G = reinterpret_cast<const T2*>(P.G);
-  const int e0 = P.lev_ent[lev], cnt = P.lev_ent[lev + 1] - e0;
-  for (int i = lane; i < cnt; i += 32) {
-    const int e = e0 + i;
-    const int el = P.elem[e];
-    const double2 rv = load_d2(r + el);
-    S.rhs[slot][i] = V2<T>::make((T)(s * rv.x), (T)(s * rv.y));
-    S.w[slot][i] = W[e];
-    S.a[slot][i] = A[e];
-    S.c[slot][i] = C[e];
-    S.gp[slot][i] = P.gsrc[e];
+  Slot<T, TI> slot[kSlots];
+  T2 u[2][kPrecondMaxLevel];     // solution of the previous / current level
+  int lev_ent[kMaxChainLevels];  // the chain's level bounds
+  double red[2 * (kSweepThreads / 32)];
+};
+
+// Stager thread t copies the factors of entries t, t + kStagers, ... of chain level k into
+// its slot with cp.async (one commit group per call, empty past the chain's end).
+template <typename T, typename TI>
+__device__ __forceinline__ void issue_factors(const PrecondDev& P, SweepSmem<T, TI>& S, int k, int nlev, int t) {
+  using T2 = typename V2<T>::type;
+  if (k < nlev) {
+    Slot<T, TI>& L = S.slot[k % kSlots];
+    const T2* W = reinterpret_cast<const T2*>(P.W);
+    const T2* A = reinterpret_cast<const T2*>(P.A);
+    const T2* C = reinterpret_cast<const T2*>(P.C);
+    const T2* G = reinterpret_cast<const T2*>(P.G);
+    const int e0 = S.lev_ent[k], cnt = S.lev_ent[k + 1] - e0;
+    for (int i = t; i < cnt; i += kStagers) {
+      const int e = e0 + i;
+      cpa(&L.el[i], P.elem + e, 4);
+      cpa(&L.gp[i], P.gsrc + e, 4);
+      cpa(&L.w[i], W + e, sizeof(T2));
+      cpa(&L.a[i], A + e, sizeof(T2));
+      cpa(&L.c[i], C + e, sizeof(T2));
 #pragma unroll
-    for (int k = 0; k < 3; ++k) S.g[slot][i][k] = G[3LL * e + k];
-    S.el[slot][i] = el;
+      for (int q = 0; q < 3; ++q) cpa(&L.g[q][i], G + 3LL * e + q, sizeof(T2));
+    }
   }
+  cpa_commit();
+}
+
+// The same stager thread gathers r at the elements whose indices it copied, with cp.async.
+template <typename T, typename TI>
+__device__ __forceinline__ void issue_gather(const TI* __restrict__ r, SweepSmem<T, TI>& S, int k, int nlev, int t) {
+  if (k < nlev) {
+    Slot<T, TI>& L = S.slot[k % kSlots];
+    const int cnt = S.lev_ent[k + 1] - S.lev_ent[k];
+    for (int i = t; i < cnt; i += kStagers) cpa(&L.rv[i], r + L.el[i], sizeof(TI));
+  }
+  cpa_commit();
 }
 
 template <typename T, typename TI, typename TO>
 __global__ void __launch_bounds__(kSweepThreads)
-    k_level_sweep(const PrecondDev P, const TI* __restrict__ r, TO* __restrict__ z, double s) {
+    k_level_sweep(const PrecondDev Pd, const TI* __restrict__ r, TO* __restrict__ z, double s) {
   using T2 = typename V2<T>::type;
-  __shared__ Stage<T> S;
-  __shared__ double2 rho_r;  // residual of the dropped free equation (d = 0 chain, mode 0)
-  const int chain = P.chain_order[blockIdx.x];
-  const int lev0 = P.chain_lev[chain], lev1 = P.chain_lev[chain + 1];
-  const bool chain0 = chain == P.chain0;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SweepSmem<T, TI>& S = *reinterpret_cast<SweepSmem<T, TI>*>(smem_raw);
+  const int chain = Pd.chain_order[blockIdx.x];
+  const int lev0 = Pd.chain_lev[chain], lev1 = Pd.chain_lev[chain + 1];
+  const int nlev = lev1 - lev0;
+  const bool chain0 = chain == Pd.chain0;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (tid == 0) rho_r = make_double2(0.0, 0.0);
-  if (warp == 1) stage_level<T, TI>(P, r, S, 0, lev0, lane, s);
+  const int st = tid - 32;  // stager index
+  for (int k = tid; k <= nlev; k += blockDim.x) S.lev_ent[k] = Pd.lev_ent[lev0 + k];
+  __syncthreads();
+  // Ring invariant at the start of level k: the factors of k + 1 and k + 2 and the gather of
+  // k + 1 are issued; level k has landed and is visible to the block.
+  if (warp > 0) {
+    issue_factors<T, TI>(Pd, S, 0, nlev, st);
+    issue_factors<T, TI>(Pd, S, 1, nlev, st);
+    cpa_wait<1>();  // factors of 0
+    issue_gather<T, TI>(r, S, 0, nlev, st);
+    cpa_wait<1>();  // factors of 1
+    issue_gather<T, TI>(r, S, 1, nlev, st);
+    issue_factors<T, TI>(Pd, S, 2, nlev, st);
+    cpa_wait<2>();  // gather of 0
+  }
   __syncthreads();
   double2 tsum = make_double2(0.0, 0.0);
+  double2 rho_r = make_double2(0.0, 0.0);  // residual of the dropped free equation (lane-held)
+  bool has_rho = false;
   int prev = 0, cur = 1;
-  for (int lev = lev0; lev < lev1; ++lev) {
-    const int slot = (lev - lev0) & 1;
-    if (warp == 1) {
-      if (lev + 1 < lev1) stage_level<T, TI>(P, r, S, slot ^ 1, lev + 1, lane, s);
+  const T sT = (T)s;
+  for (int k = 0; k < nlev; ++k) {
+    if (warp > 0) {
+      issue_factors<T, TI>(Pd, S, k + 3, nlev, st);
+      cpa_wait<1>();  // this thread's factors of k + 2 and gather of k + 1 have landed
+      issue_gather<T, TI>(r, S, k + 2, nlev, st);
     } else {
-      const int e0 = P.lev_ent[lev];
-      const int cnt = P.lev_ent[lev + 1] - e0;
-      for (int i = lane; i < cnt; i += 32) {
-        T2 rv = S.rhs[slot][i];
-        const int packed = S.gp[slot][i];
+      // Warp 0 solves the level.  Lane l owns the K consecutive entries l K .. l K + K - 1
+      // (K <= 5).  Both Thomas recurrences, y_i = A_i y_{i-1} + B_i with B_i = W_i rhs_i and
+      // u_i = C_i u_{i+1} + y_i, are affine maps composed over each lane's chunk, combined
+      // across lanes by a five-step shuffle scan, then replayed inside the chunk.
+      const Slot<T, TI>& L = S.slot[k % kSlots];
+      const int e0 = S.lev_ent[k];
+      const int cnt = S.lev_ent[k + 1] - e0;
+      const int K = (cnt + 31) >> 5;
+      const int i0 = lane * K;
+      T2 Bv[kChunk], Av[kChunk], Cv[kChunk];
+      const T2 one = V2<T>::make((T)1, (T)0), zero = V2<T>::make((T)0, (T)0);
+      T2 P = one, Q = zero;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const int pos = (packed >> (10 * k)) & 1023;
-          if (pos != kNoGain) {
-            const T2 g = S.g[slot][i][k];
-            const T2 un = S.u[prev][pos];
-            T2 m;
-            m.x = -g.x;
-            m.y = -g.y;
-            rv = cfma(m, un, rv);
+      for (int q = 0; q < kChunk; ++q) {
+        const int i = i0 + q;
+        Bv[q] = zero;
+        Av[q] = zero;
+        Cv[q] = zero;
+        if (q < K && i < cnt) {
+          const TI x = L.rv[i];
+          T2 rv = V2<T>::make(sT * (T)x.x, sT * (T)x.y);
+          const int packed = L.gp[i];
+#pragma unroll
+          for (int g3 = 0; g3 < 3; ++g3) {
+            const int pos = (packed >> (10 * g3)) & 1023;
+            if (pos != kNoGain) {
+              const T2 g = L.g[g3][i];
+              T2 m;
+              m.x = -g.x;
+              m.y = -g.y;
+              rv = cfma(m, S.u[prev][pos], rv);
+            }
           }
-        }
-        if (e0 + i == P.free_ent) rho_r = make_double2((double)rv.x, (double)rv.y);
-        S.y[i] = cmul(S.w[slot][i], rv);
-      }
-      __syncwarp();
-      if (lane == 0) {
-        // forward: y_i += A_i y_{i-1}; backward: u_i = y_i + C_i u_{i+1}
-        T2 yp = S.y[0];
-        for (int i = 1; i < cnt; ++i) {
-          yp = cfma(S.a[slot][i], yp, S.y[i]);
-          S.y[i] = yp;
-        }
-        T2 un = S.y[cnt - 1];
-        S.u[cur][cnt - 1] = un;
-        for (int i = cnt - 2; i >= 0; --i) {
-          un = cfma(S.c[slot][i], un, S.y[i]);
-          S.u[cur][i] = un;
+          if (e0 + i == Pd.free_ent) {
+            rho_r = make_double2((double)rv.x, (double)rv.y);
+            has_rho = true;
+          }
+          Bv[q] = cmul(L.w[i], rv);
+          Av[q] = L.a[i];
+          Cv[q] = L.c[i];
+          Q = cfma(Av[q], Q, Bv[q]);
+          P = cmul(Av[q], P);
         }
       }
-      __syncwarp();
-      for (int i = lane; i < cnt; i += 32) {
-        const T2 uv = S.u[cur][i];
-        store_as<TO, T2>(z + S.el[slot][i], uv);
-        if (chain0 && P.mode == 1) {
-          const double t = P.t0[e0 + i - P.chain0_ent];
-          tsum.x = fma(t, (double)uv.x, tsum.x);
-          tsum.y = fma(t, (double)uv.y, tsum.y);
+      // inclusive scan in lane order: (P, Q) <- (P, Q) o (P_prev, Q_prev)
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const T2 Pn = shfl_up_c(P, d), Qn = shfl_up_c(Q, d);
+        if (lane >= d) {
+          Q = cfma(P, Qn, Q);
+          P = cmul(P, Pn);
+        }
+      }
+      T2 y = shfl_up_c(Q, 1);
+      if (lane == 0) y = zero;
+#pragma unroll
+      for (int q = 0; q < kChunk; ++q) {
+        y = cfma(Av[q], y, Bv[q]);  // Av = Bv = 0 past the lane's entries: harmless zeros
+        Bv[q] = y;                  // Bv now holds y_i
+      }
+      T2 P2 = one, Q2 = zero;
+#pragma unroll
+      for (int q = kChunk - 1; q >= 0; --q) {
+        if (q < K && i0 + q < cnt) {  // only this lane's entries of the level
+          Q2 = cfma(Cv[q], Q2, Bv[q]);
+          P2 = cmul(Cv[q], P2);
+        }
+      }
+      // suffix scan in reverse lane order
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const T2 Pn = shfl_down_c(P2, d), Qn = shfl_down_c(Q2, d);
+        if (lane + d < 32) {
+          Q2 = cfma(P2, Qn, Q2);
+          P2 = cmul(P2, Pn);
+        }
+      }
+      T2 uv = shfl_down_c(Q2, 1);
+      if (lane == 31) uv = zero;
+#pragma unroll
+      for (int q = kChunk - 1; q >= 0; --q) {
+        const int i = i0 + q;
+        if (q < K && i < cnt) {
+          uv = cfma(Cv[q], uv, Bv[q]);
+          S.u[cur][i] = uv;
+          store_as<TO, T2>(z + L.el[i], uv);
+          if (chain0 && Pd.mode == 1) {
+            const double t = Pd.t0[e0 + i - Pd.chain0_ent];
+            tsum.x = fma(t, (double)uv.x, tsum.x);
+            tsum.y = fma(t, (double)uv.y, tsum.y);
+          }
         }
       }
     }
@@ -251,41 +375,70 @@ __global__ void __launch_bounds__(kSweepThreads)
     cur ^= 1;
   }
   if (!chain0) return;
-  const int c0 = P.chain0_ent, c1 = P.lev_ent[lev1];
-  if (P.mode == 0) {
+  const int c0 = Pd.chain0_ent, c1 = Pd.lev_ent[lev1];
+  if (Pd.mode == 0) {
     // beta = rho_r / rho_v; y = y_r - beta y_v; z_f = (beta - t^H y) / t_f
-    const double2 rv = P.sm_coef;  // rho_v
+    double* rr = S.red;  // the lane that met the free entry hands rho_r over
+    __syncthreads();
+    if (has_rho) {
+      rr[0] = rho_r.x;
+      rr[1] = rho_r.y;
+    }
+    __syncthreads();
+    const double2 rrv = make_double2(rr[0], rr[1]);
+    __syncthreads();
+    const double2 rv = Pd.sm_coef;  // rho_v
     const double den = rv.x * rv.x + rv.y * rv.y;
-    const double2 beta = make_double2((rho_r.x * rv.x + rho_r.y * rv.y) / den, (rho_r.y * rv.x - rho_r.x * rv.y) / den);
+    const double2 beta =
+        make_double2((rrv.x * rv.x + rrv.y * rv.y) / den, (rrv.y * rv.x - rrv.x * rv.y) / den);
     for (int e = c0 + tid; e < c1; e += blockDim.x) {
-      const int el = P.elem[e];
-      const double2 yv = P.w0[e - c0];
+      const int el = Pd.elem[e];
+      const double2 yv = Pd.w0[e - c0];
       double2 zv = load_d2(z + el);
       zv.x -= beta.x * yv.x - beta.y * yv.y;
       zv.y -= beta.x * yv.y + beta.y * yv.x;
       store_as<TO, double2>(z + el, zv);
-      const double t = P.t0[e - c0];
+      const double t = Pd.t0[e - c0];
       tsum.x = fma(t, zv.x, tsum.x);
       tsum.y = fma(t, zv.y, tsum.y);
     }
     const double2 tz = block_sum2(tsum, S.red);
-    if (tid == 0 && P.free_ent >= 0) {
-      const double t = P.t0[P.free_ent - c0];
-      store_as<TO, double2>(z + P.elem[P.free_ent], make_double2((beta.x - tz.x) / t, (beta.y - tz.y) / t));
+    if (tid == 0 && Pd.free_ent >= 0) {
+      const double t = Pd.t0[Pd.free_ent - c0];
+      store_as<TO, double2>(z + Pd.elem[Pd.free_ent], make_double2((beta.x - tz.x) / t, (beta.y - tz.y) / t));
     }
   } else {
     // Sherman-Morrison: z -= w0 (t^H y) / (1 + t^H w0)
     const double2 tz = block_sum2(tsum, S.red);
-    const double2 k = make_double2(tz.x * P.sm_coef.x - tz.y * P.sm_coef.y, tz.x * P.sm_coef.y + tz.y * P.sm_coef.x);
+    const double2 kk =
+        make_double2(tz.x * Pd.sm_coef.x - tz.y * Pd.sm_coef.y, tz.x * Pd.sm_coef.y + tz.y * Pd.sm_coef.x);
     for (int e = c0 + tid; e < c1; e += blockDim.x) {
-      const int el = P.elem[e];
-      const double2 w0 = P.w0[e - c0];
+      const int el = Pd.elem[e];
+      const double2 w0 = Pd.w0[e - c0];
       double2 zv = load_d2(z + el);
-      zv.x -= w0.x * k.x - w0.y * k.y;
-      zv.y -= w0.x * k.y + w0.y * k.x;
+      zv.x -= w0.x * kk.x - w0.y * kk.y;
+      zv.y -= w0.x * kk.y + w0.y * kk.x;
       store_as<TO, double2>(z + el, zv);
     }
   }
+}
+
+template <typename T, typename TI, typename TO>
+cudaError_t launch_sweep(const PrecondDev& D, int blocks, const void* r, void* z, double scale, cudaStream_t stream) {
+  const size_t smem = sizeof(SweepSmem<T, TI>);
+  // the shared-memory opt-in is a per-function, per-device attribute: set once per device
+  static std::atomic<unsigned long long> configured{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = 1ULL << (dev & 63);
+  if (!(configured.load() & bit)) {
+    e = cudaFuncSetAttribute(k_level_sweep<T, TI, TO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured.fetch_or(bit);
+  }
+  k_level_sweep<T, TI, TO><<<blocks, kSweepThreads, smem, stream>>>(D, (const TI*)r, (TO*)z, scale);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------------------
@@ -463,6 +616,11 @@ int build_level_precond(const QubitPlan& hp, int coords, double regularization, 
     chain_len.push_back((int)H.elem.size() - chain_first_entry);
   }
   H.maxdiag = maxdiag;
+  for (size_t c = 0; c + 1 < H.chain_lev.size(); ++c)
+    if (H.chain_lev[c + 1] - H.chain_lev[c] > 2 * kPrecondMaxLevel + 2) {
+      *err = "a charge chain has more levels than the sweep kernel stages";
+      return PI_ERR_UNSUPPORTED;
+    }
   if ((long long)H.elem.size() != hp.dim) {
     *err = "level decomposition does not cover the basis";
     return PI_ERR_UNSUPPORTED;
@@ -603,26 +761,12 @@ cudaError_t precond_apply(const pi_precond* P, const void* r, int r_f32, void* z
                           cudaStream_t stream) {
   const PrecondDev& D = P->dev;
   const int blocks = (int)P->host.chain_order.size();
-  if (P->fp64) {
-    if (!r_f32 && !z_f32)
-      k_level_sweep<double, double2, double2><<<blocks, kSweepThreads, 0, stream>>>(D, (const double2*)r,
-                                                                                   (double2*)z, scale);
-    else if (r_f32 && z_f32)
-      k_level_sweep<double, float2, float2><<<blocks, kSweepThreads, 0, stream>>>(D, (const float2*)r,
-                                                                                 (float2*)z, scale);
-    else
-      return cudaErrorInvalidValue;
-  } else {
-    if (!r_f32 && !z_f32)
-      k_level_sweep<float, double2, double2><<<blocks, kSweepThreads, 0, stream>>>(D, (const double2*)r,
-                                                                                  (double2*)z, scale);
-    else if (r_f32 && z_f32)
-      k_level_sweep<float, float2, float2><<<blocks, kSweepThreads, 0, stream>>>(D, (const float2*)r,
-                                                                                (float2*)z, scale);
-    else
-      return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
+  if (r_f32 != z_f32) return cudaErrorInvalidValue;
+  if (P->fp64)
+    return r_f32 ? launch_sweep<double, float2, float2>(D, blocks, r, z, scale, stream)
+                 : launch_sweep<double, double2, double2>(D, blocks, r, z, scale, stream);
+  return r_f32 ? launch_sweep<float, float2, float2>(D, blocks, r, z, scale, stream)
+               : launch_sweep<float, double2, double2>(D, blocks, r, z, scale, stream);
 }
 
 int precond_coords(const pi_precond* P) { return P->host.coords; }

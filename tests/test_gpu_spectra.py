@@ -260,7 +260,9 @@ def test_implicitly_restarted_arnoldi_on_device(torch_cuda):
     for j, lam in enumerate(res["values"]):
         x = X[:, j]
         r = np.linalg.norm(L @ x - lam * x) / np.linalg.norm(x)
-        assert r <= max(10 * res["residuals"][j], 1e-9), (j, r, res["residuals"][j])
+        # the Hessenberg estimate omits the rounding of the restarted basis: allow 1e-8 of
+        # the operator scale on top of it
+        assert r <= 10 * res["residuals"][j] + 1e-8 * res["residual_scale"], (j, r, res["residuals"][j])
     # the spectral entry points that select it
     lr = picuda.liouvillian_spectrum(model, nev=3, algorithm="iram", krylovdim=40)
     assert len(lr) == 3
