@@ -363,6 +363,76 @@ def steady_rates(picuda, torch, count=16, seed=7, family="driven"):
     return out
 
 
+def btc_model(picuda, N, omega_over_kappa):
+    """Boundary-time-crystal-like steady-state configuration: H = Omega Jx with
+    Omega = omega_over_kappa * kappa, collective decay kappa = 1/N on J-, local dephasing 0.01,
+    all Schur sectors."""
+    s = picuda.spin_matrices(2)
+    kappa = 1.0 / N
+    return picuda.qubit_ensemble_model(N, hamiltonian=omega_over_kappa * kappa * s["jx"], collective_emission=kappa,
+                                       dephasing=0.01)
+
+
+def steady_c3_rates(picuda, torch, N=200, omegas=(0.5, 1.0, 2.0), repeats=5, tol=5e-11, plain=True):
+    """Steady states of the N=200 boundary-time-crystal-like model (dim 1,373,701) for
+    Omega in {0.5, 1, 2} kappa: restarted GMRES(50) left-preconditioned by the level sweep,
+    in population coordinates, to a normalized residual and trace error of 1e-10
+    (atol = rtol = 5e-11), plain FP64 against mixed precision (FP32 applies, Krylov basis and
+    sweeps; FP64 residual refinement).  Plans and preconditioners are built before the clock;
+    each solve is timed alone (host call to host return).  The reference's unpreconditioned
+    GMRES(50) is run once per Omega in population coordinates with maxiter 500 to record
+    whether it gets there."""
+    out = {"N": N, "krylovdim": 50, "omegas_over_kappa": list(omegas), "repeats": repeats,
+           "tolerance": {"atol": tol, "rtol": tol}, "coords": "population"}
+    per = {}
+    lat = {"fp64": [], "mixed": []}
+    for w in omegas:
+        c = picuda.compile(btc_model(picuda, N, w))
+        t0 = time.perf_counter()
+        P = picuda.level_preconditioner(c, coords="population")
+        setup = time.perf_counter() - t0
+        res = {}
+        states = {}
+        for prec in ("fp64", "mixed"):
+            alg = picuda.GMRESAlgorithm(krylovdim=50, maxiter=2000, preconditioner=P, precision=prec)
+            picuda.stationary_state(c, algorithm=alg, atol=tol, rtol=tol)  # warm
+            times = []
+            for _ in range(repeats):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                r = picuda.stationary_state(c, algorithm=alg, return_info=True, atol=tol, rtol=tol)
+                times.append(time.perf_counter() - t0)
+            lat[prec].extend(times)
+            states[prec] = r.state.data
+            res[prec] = {"ms_p50": statistics.median(times) * 1e3, "ms_max": max(times) * 1e3,
+                         "iterations": r.info["iterations"], "restarts": r.info["restarts"],
+                         "refinements": r.info["refinements"],
+                         "normalized_residual": r.info["normalized_residual"],
+                         "trace_error": r.info["trace_error"], "converged": bool(r.info["converged"])}
+        sq = c.sector_scales()
+        scale = np.concatenate([np.full(n * n, sq[i]) for i, n in enumerate(c.basis.dims)])
+        z64, z32 = states["fp64"] * scale, states["mixed"] * scale
+        res["mixed_state_rel_dev_vs_fp64"] = float(np.abs(z32 - z64).max() / np.abs(z64).max())
+        res["preconditioner_setup_s"] = setup
+        res["preconditioner_bytes"] = P.info["device_bytes"]
+        try:
+            if plain:
+                ref = picuda.stationary_state(c, algorithm=picuda.GMRESAlgorithm(krylovdim=50, maxiter=500),
+                                              return_info=True, atol=tol, rtol=tol, coords="population")
+                res["unpreconditioned_fp64"] = {"converged": True, "iterations": ref.info["iterations"]}
+        except picuda.PiNotConverged as err:
+            res["unpreconditioned_fp64"] = {"converged": False, "maxiter": 500, "message": str(err)[-120:]}
+        per[str(w)] = res
+        P.close()
+    out["per_omega"] = per
+    for prec in ("fp64", "mixed"):
+        a = np.array(lat[prec])
+        out[prec] = {"solves_per_s": len(a) / a.sum(), "p50_ms": float(np.percentile(a, 50) * 1e3),
+                     "p99_ms": float(np.percentile(a, 99) * 1e3), "solves": int(len(a))}
+    out["solves_per_s_ratio_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    return out
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -610,6 +680,12 @@ def main():
     ap.add_argument("--scan-precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--only-steady", action="store_true", help="run only the steady-state rate section")
+    ap.add_argument("--only-steady-c3", action="store_true",
+                    help="run only the N=200 preconditioned steady-state section")
+    ap.add_argument("--c3-repeats", type=int, default=5)
+    ap.add_argument("--c3-omegas", default="0.5,1,2", help="Omega/kappa values of the N=200 steady-state section")
+    ap.add_argument("--c3-no-plain", action="store_true",
+                    help="skip the unpreconditioned reference-method attempt (profiling runs)")
     ap.add_argument("--steady-requests", type=int, default=16)
     ap.add_argument("--only-rk4", default=None, choices=["fp64", "mixed"],
                     help="one short RK4 solve of the large time-evolution model (a profiling target)")
@@ -640,6 +716,12 @@ def main():
         print(json.dumps({"only_steady": True, "steady": steady_rates(picuda, torch, args.steady_requests),
                           "steady_served_family": steady_rates(picuda, torch, args.steady_requests,
                                                                family="served")}))
+        return 0
+    if args.only_steady_c3:
+        omegas = tuple(float(v) for v in args.c3_omegas.split(","))
+        print(json.dumps({"only_steady_c3": True,
+                          "steady_c3": steady_c3_rates(picuda, torch, omegas=omegas, repeats=args.c3_repeats,
+                                                       plain=not args.c3_no_plain)}))
         return 0
     if args.only_serve:
         print(json.dumps({"only_serve": True, "serve": serve_rates(picuda, torch, args.serve_requests)}))
@@ -770,6 +852,7 @@ def main():
     steady = steady_rates(picuda, torch, args.steady_requests) if rank == 0 else None
     steady_served = (steady_rates(picuda, torch, args.steady_requests, family="served")
                      if rank == 0 else None)
+    steady_c3 = steady_c3_rates(picuda, torch, repeats=args.c3_repeats) if rank == 0 else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -819,6 +902,7 @@ def main():
             "serve": serve,
             "steady": steady,
             "steady_served_family": steady_served,
+            "steady_c3": steady_c3,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": cl,

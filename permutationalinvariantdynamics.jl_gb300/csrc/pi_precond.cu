@@ -146,8 +146,21 @@ __device__ __forceinline__ double2 block_sum2(double2 v, double* red) {
 }
 
 constexpr int kStagers = kSweepThreads - 32;  // warps 1.. stage levels ahead of warp 0
-constexpr int kChunk = (kPrecondMaxLevel + 31) / 32;  // entries per lane of warp 0
-constexpr int kSlots = 4;                      // level ring: solved, gathered, copied, in flight
+static_assert(kPrecondMaxLevel <= 5 * 32, "warp 0 solves levels of at most five entries per lane");
+// Depth of the level ring: the factors of level k + DF and the gather of r at level k + DG are
+// issued while level k is solved, so copies have DF - DG and gathers DG - 1 levels of time to
+// land.  FP32 sweeps keep six slots (about 70 KB of shared memory, three blocks per SM);
+// FP64 sweeps keep four to stay at two blocks per SM.
+template <typename T>
+struct Ring;
+template <>
+struct Ring<float> {
+  static constexpr int DF = 5, DG = 3;
+};
+template <>
+struct Ring<double> {
+  static constexpr int DF = 3, DG = 2;
+};
 constexpr int kMaxChainLevels = 2 * kPrecondMaxLevel + 4;
 
 __device__ __forceinline__ float2 shfl_up_c(float2 v, int d) {
@@ -180,6 +193,10 @@ __device__ __forceinline__ void cpa_wait() {
 
 // One staged level: r at the level's elements (as stored) and the level's factors and gain
 // tables.
+// Slot position of entry i of a level with K = ceil(cnt / 32) entries per lane: lane l's q-th
+// entry (i = l K + q) sits at q * 32 + l, so warp 0's accesses of one q are bank-conflict free.
+__device__ __forceinline__ int slot_pos(int i, int K) { return (i % K) * 32 + i / K; }
+
 template <typename T, typename TI>
 struct Slot {
   using T2 = typename V2<T>::type;
@@ -195,8 +212,10 @@ struct Slot {
 template <typename T, typename TI>
 struct SweepSmem {
   using T2 = typename V2<T>::type;
+  static constexpr int kSlots = Ring<T>::DF + 1;
   Slot<T, TI> slot[kSlots];
   T2 u[2][kPrecondMaxLevel];     // solution of the previous / current level
+  T2 b[kPrecondMaxLevel];        // W_i (s r_i - gains), slot order
   int lev_ent[kMaxChainLevels];  // the chain's level bounds
   double red[2 * (kSweepThreads / 32)];
 };
@@ -206,22 +225,24 @@ struct SweepSmem {
 template <typename T, typename TI>
 __device__ __forceinline__ void issue_factors(const PrecondDev& P, SweepSmem<T, TI>& S, int k, int nlev, int t) {
   using T2 = typename V2<T>::type;
-  if (k < nlev) {
-    Slot<T, TI>& L = S.slot[k % kSlots];
+  if (k >= 0 && k < nlev) {
+    Slot<T, TI>& L = S.slot[k % SweepSmem<T, TI>::kSlots];
     const T2* W = reinterpret_cast<const T2*>(P.W);
     const T2* A = reinterpret_cast<const T2*>(P.A);
     const T2* C = reinterpret_cast<const T2*>(P.C);
     const T2* G = reinterpret_cast<const T2*>(P.G);
     const int e0 = S.lev_ent[k], cnt = S.lev_ent[k + 1] - e0;
+    const int K = (cnt + 31) >> 5;
     for (int i = t; i < cnt; i += kStagers) {
       const int e = e0 + i;
-      cpa(&L.el[i], P.elem + e, 4);
-      cpa(&L.gp[i], P.gsrc + e, 4);
-      cpa(&L.w[i], W + e, sizeof(T2));
-      cpa(&L.a[i], A + e, sizeof(T2));
-      cpa(&L.c[i], C + e, sizeof(T2));
+      const int p = slot_pos(i, K);
+      cpa(&L.el[p], P.elem + e, 4);
+      cpa(&L.gp[p], P.gsrc + e, 4);
+      cpa(&L.w[p], W + e, sizeof(T2));
+      cpa(&L.a[p], A + e, sizeof(T2));
+      cpa(&L.c[p], C + e, sizeof(T2));
 #pragma unroll
-      for (int q = 0; q < 3; ++q) cpa(&L.g[q][i], G + 3LL * e + q, sizeof(T2));
+      for (int q = 0; q < 3; ++q) cpa(&L.g[q][p], G + 3LL * e + q, sizeof(T2));
     }
   }
   cpa_commit();
@@ -230,12 +251,142 @@ __device__ __forceinline__ void issue_factors(const PrecondDev& P, SweepSmem<T, 
 // The same stager thread gathers r at the elements whose indices it copied, with cp.async.
 template <typename T, typename TI>
 __device__ __forceinline__ void issue_gather(const TI* __restrict__ r, SweepSmem<T, TI>& S, int k, int nlev, int t) {
-  if (k < nlev) {
-    Slot<T, TI>& L = S.slot[k % kSlots];
+  if (k >= 0 && k < nlev) {
+    Slot<T, TI>& L = S.slot[k % SweepSmem<T, TI>::kSlots];
     const int cnt = S.lev_ent[k + 1] - S.lev_ent[k];
-    for (int i = t; i < cnt; i += kStagers) cpa(&L.rv[i], r + L.el[i], sizeof(TI));
+    const int K = (cnt + 31) >> 5;
+    for (int i = t; i < cnt; i += kStagers) {
+      const int p = slot_pos(i, K);
+      cpa(&L.rv[p], r + L.el[p], sizeof(TI));
+    }
   }
   cpa_commit();
+}
+
+// Right-hand sides of one level, all warps: b_i = W_i (s r_i - sum of the gains from the
+// previous level's solution), at slot positions.  Absent gains read slot 0 with a zero
+// coefficient; the thread that meets the free entry keeps its unscaled residual.
+template <typename T, typename TI>
+__device__ __forceinline__ void level_rhs(const PrecondDev& Pd, const Slot<T, TI>& L,
+                                          const typename V2<T>::type* __restrict__ uprev,
+                                          typename V2<T>::type* __restrict__ b, int e0, int cnt, T sT, int tid,
+                                          double2& rho_r, bool& has_rho) {
+  using T2 = typename V2<T>::type;
+  const int K = (cnt + 31) >> 5;
+  for (int p = tid; p < 32 * K; p += kSweepThreads) {
+    const int i = (p & 31) * K + (p >> 5);  // entry of slot p
+    if (i >= cnt) continue;
+    const TI x = L.rv[p];
+    T2 rv = V2<T>::make(sT * (T)x.x, sT * (T)x.y);
+    const int packed = L.gp[p];
+#pragma unroll
+    for (int g3 = 0; g3 < 3; ++g3) {
+      int pos = (packed >> (10 * g3)) & 1023;  // slot position in the previous level
+      pos = pos == kNoGain ? 0 : pos;          // an absent gain has a zero coefficient
+      const T2 g = L.g[g3][p];
+      T2 m;
+      m.x = -g.x;
+      m.y = -g.y;
+      rv = cfma(m, uprev[pos], rv);
+    }
+    const bool hit = e0 + i == Pd.free_ent;
+    rho_r.x = hit ? (double)rv.x : rho_r.x;
+    rho_r.y = hit ? (double)rv.y : rho_r.y;
+    has_rho = has_rho || hit;
+    b[p] = cmul(L.w[p], rv);
+  }
+}
+
+// Warp 0's solve of one level of cnt entries, K = ceil(cnt / 32) of them per lane.  Lane l
+// owns the K consecutive entries l K .. l K + K - 1 (slots q 32 + l).  Both Thomas
+// recurrences, y_i = A_i y_{i-1} + b_i and u_i = C_i u_{i+1} + y_i, are affine maps composed
+// over each lane's chunk, combined across lanes by a five-step shuffle scan, then replayed
+// inside the chunk.  Specialised on K so that short levels issue short code.
+template <typename T, typename TI, typename TO, int K>
+__device__ __forceinline__ void solve_level(const PrecondDev& Pd, const Slot<T, TI>& L,
+                                            const typename V2<T>::type* __restrict__ b,
+                                            typename V2<T>::type* __restrict__ ucur, TO* __restrict__ z, int e0,
+                                            int cnt, bool sum_t, int lane, double2& tsum) {
+  using T2 = typename V2<T>::type;
+  const int i0 = lane * K;
+  T2 Bv[K], Av[K], Cv[K];
+  bool ok[K];
+  const T2 one = V2<T>::make((T)1, (T)0), zero = V2<T>::make((T)0, (T)0);
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    ok[q] = i0 + q < cnt;
+    const int p = q * 32 + lane;
+    const T2 bb = b[p], a = L.a[p], c = L.c[p];
+    Bv[q] = ok[q] ? bb : zero;
+    Av[q] = ok[q] ? a : zero;
+    Cv[q] = ok[q] ? c : zero;
+  }
+  // the lane's forward map y_out = P y_in + Q
+  T2 P = one, Q = zero;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    const T2 Pq = cmul(Av[q], P), Qq = cfma(Av[q], Q, Bv[q]);
+    P = ok[q] ? Pq : P;
+    Q = ok[q] ? Qq : Q;
+  }
+  // inclusive scan in lane order: (P, Q) <- (P, Q) o (P_prev, Q_prev)
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T2 Pn = shfl_up_c(P, d), Qn = shfl_up_c(Q, d);
+    if (lane >= d) {
+      Q = cfma(P, Qn, Q);
+      P = cmul(P, Pn);
+    }
+  }
+  T2 y = shfl_up_c(Q, 1);
+  if (lane == 0) y = zero;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    y = cfma(Av[q], y, Bv[q]);  // Av = Bv = 0 past the level: harmless zeros
+    Bv[q] = y;                  // Bv now holds y_i
+  }
+  // the lane's backward map u_in = P2 u_next + Q2 over its entries of the level
+  T2 P2 = one, Q2 = zero;
+#pragma unroll
+  for (int q = K - 1; q >= 0; --q) {
+    const T2 Pq = cmul(Cv[q], P2), Qq = cfma(Cv[q], Q2, Bv[q]);
+    P2 = ok[q] ? Pq : P2;
+    Q2 = ok[q] ? Qq : Q2;
+  }
+  // suffix scan in reverse lane order
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const T2 Pn = shfl_down_c(P2, d), Qn = shfl_down_c(Q2, d);
+    if (lane + d < 32) {
+      Q2 = cfma(P2, Qn, Q2);
+      P2 = cmul(P2, Pn);
+    }
+  }
+  T2 uv = shfl_down_c(Q2, 1);
+  if (lane == 31) uv = zero;
+  T2 U[K];
+#pragma unroll
+  for (int q = K - 1; q >= 0; --q) {
+    uv = cfma(Cv[q], uv, Bv[q]);
+    U[q] = uv;
+  }
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    if (ok[q]) {
+      ucur[q * 32 + lane] = U[q];
+      store_as<TO, T2>(z + L.el[q * 32 + lane], U[q]);
+    }
+  }
+  if (sum_t) {
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      if (ok[q]) {
+        const double t = Pd.t0[e0 + i0 + q - Pd.chain0_ent];
+        tsum.x = fma(t, (double)U[q].x, tsum.x);
+        tsum.y = fma(t, (double)U[q].y, tsum.y);
+      }
+    }
+  }
 }
 
 template <typename T, typename TI, typename TO>
@@ -251,128 +402,46 @@ __global__ void __launch_bounds__(kSweepThreads)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int st = tid - 32;  // stager index
   for (int k = tid; k <= nlev; k += blockDim.x) S.lev_ent[k] = Pd.lev_ent[lev0 + k];
+  for (int i = tid; i < 2 * kPrecondMaxLevel; i += blockDim.x)  // absent gains read finite zeros
+    S.u[i / kPrecondMaxLevel][i % kPrecondMaxLevel] = V2<T>::make((T)0, (T)0);
   __syncthreads();
-  // Ring invariant at the start of level k: the factors of k + 1 and k + 2 and the gather of
-  // k + 1 are issued; level k has landed and is visible to the block.
-  if (warp > 0) {
-    issue_factors<T, TI>(Pd, S, 0, nlev, st);
-    issue_factors<T, TI>(Pd, S, 1, nlev, st);
-    cpa_wait<1>();  // factors of 0
-    issue_gather<T, TI>(r, S, 0, nlev, st);
-    cpa_wait<1>();  // factors of 1
-    issue_gather<T, TI>(r, S, 1, nlev, st);
-    issue_factors<T, TI>(Pd, S, 2, nlev, st);
-    cpa_wait<2>();  // gather of 0
-  }
-  __syncthreads();
+  // Level j's step issues the factors of j + DF, waits until this thread's factors of j + DG
+  // and gather of j + 1 have landed (after the gather of j + 1 it has committed 2 DG - 3
+  // groups, after the factors of j + DG 2 (DF - DG)), and issues the gather of j + DG; steps
+  // j < 0 fill the ring before warp 0 starts (empty groups keep the commit counts uniform).
+  constexpr int DF = Ring<T>::DF, DG = Ring<T>::DG;
   double2 tsum = make_double2(0.0, 0.0);
   double2 rho_r = make_double2(0.0, 0.0);  // residual of the dropped free equation (lane-held)
   bool has_rho = false;
   int prev = 0, cur = 1;
   const T sT = (T)s;
-  for (int k = 0; k < nlev; ++k) {
+  for (int k = -DF; k < nlev; ++k) {
+    const Slot<T, TI>& L = S.slot[(k + SweepSmem<T, TI>::kSlots) % SweepSmem<T, TI>::kSlots];
+    const int e0 = k >= 0 ? S.lev_ent[k] : 0;
+    const int cnt = k >= 0 ? S.lev_ent[k + 1] - e0 : 0;
+    if (k >= 0) {
+      level_rhs<T, TI>(Pd, L, S.u[prev], S.b, e0, cnt, sT, tid, rho_r, has_rho);
+      __syncthreads();
+    }
     if (warp > 0) {
-      issue_factors<T, TI>(Pd, S, k + 3, nlev, st);
-      cpa_wait<1>();  // this thread's factors of k + 2 and gather of k + 1 have landed
-      issue_gather<T, TI>(r, S, k + 2, nlev, st);
-    } else {
-      // Warp 0 solves the level.  Lane l owns the K consecutive entries l K .. l K + K - 1
-      // (K <= 5).  Both Thomas recurrences, y_i = A_i y_{i-1} + B_i with B_i = W_i rhs_i and
-      // u_i = C_i u_{i+1} + y_i, are affine maps composed over each lane's chunk, combined
-      // across lanes by a five-step shuffle scan, then replayed inside the chunk.
-      const Slot<T, TI>& L = S.slot[k % kSlots];
-      const int e0 = S.lev_ent[k];
-      const int cnt = S.lev_ent[k + 1] - e0;
-      const int K = (cnt + 31) >> 5;
-      const int i0 = lane * K;
-      T2 Bv[kChunk], Av[kChunk], Cv[kChunk];
-      const T2 one = V2<T>::make((T)1, (T)0), zero = V2<T>::make((T)0, (T)0);
-      T2 P = one, Q = zero;
-#pragma unroll
-      for (int q = 0; q < kChunk; ++q) {
-        const int i = i0 + q;
-        Bv[q] = zero;
-        Av[q] = zero;
-        Cv[q] = zero;
-        if (q < K && i < cnt) {
-          const TI x = L.rv[i];
-          T2 rv = V2<T>::make(sT * (T)x.x, sT * (T)x.y);
-          const int packed = L.gp[i];
-#pragma unroll
-          for (int g3 = 0; g3 < 3; ++g3) {
-            const int pos = (packed >> (10 * g3)) & 1023;
-            if (pos != kNoGain) {
-              const T2 g = L.g[g3][i];
-              T2 m;
-              m.x = -g.x;
-              m.y = -g.y;
-              rv = cfma(m, S.u[prev][pos], rv);
-            }
-          }
-          if (e0 + i == Pd.free_ent) {
-            rho_r = make_double2((double)rv.x, (double)rv.y);
-            has_rho = true;
-          }
-          Bv[q] = cmul(L.w[i], rv);
-          Av[q] = L.a[i];
-          Cv[q] = L.c[i];
-          Q = cfma(Av[q], Q, Bv[q]);
-          P = cmul(Av[q], P);
-        }
-      }
-      // inclusive scan in lane order: (P, Q) <- (P, Q) o (P_prev, Q_prev)
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const T2 Pn = shfl_up_c(P, d), Qn = shfl_up_c(Q, d);
-        if (lane >= d) {
-          Q = cfma(P, Qn, Q);
-          P = cmul(P, Pn);
-        }
-      }
-      T2 y = shfl_up_c(Q, 1);
-      if (lane == 0) y = zero;
-#pragma unroll
-      for (int q = 0; q < kChunk; ++q) {
-        y = cfma(Av[q], y, Bv[q]);  // Av = Bv = 0 past the lane's entries: harmless zeros
-        Bv[q] = y;                  // Bv now holds y_i
-      }
-      T2 P2 = one, Q2 = zero;
-#pragma unroll
-      for (int q = kChunk - 1; q >= 0; --q) {
-        if (q < K && i0 + q < cnt) {  // only this lane's entries of the level
-          Q2 = cfma(Cv[q], Q2, Bv[q]);
-          P2 = cmul(Cv[q], P2);
-        }
-      }
-      // suffix scan in reverse lane order
-#pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        const T2 Pn = shfl_down_c(P2, d), Qn = shfl_down_c(Q2, d);
-        if (lane + d < 32) {
-          Q2 = cfma(P2, Qn, Q2);
-          P2 = cmul(P2, Pn);
-        }
-      }
-      T2 uv = shfl_down_c(Q2, 1);
-      if (lane == 31) uv = zero;
-#pragma unroll
-      for (int q = kChunk - 1; q >= 0; --q) {
-        const int i = i0 + q;
-        if (q < K && i < cnt) {
-          uv = cfma(Cv[q], uv, Bv[q]);
-          S.u[cur][i] = uv;
-          store_as<TO, T2>(z + L.el[i], uv);
-          if (chain0 && Pd.mode == 1) {
-            const double t = Pd.t0[e0 + i - Pd.chain0_ent];
-            tsum.x = fma(t, (double)uv.x, tsum.x);
-            tsum.y = fma(t, (double)uv.y, tsum.y);
-          }
-        }
+      issue_factors<T, TI>(Pd, S, k + DF, nlev, st);
+      cpa_wait<(2 * DG - 3 < 2 * (DF - DG) ? 2 * DG - 3 : 2 * (DF - DG))>();
+      issue_gather<T, TI>(r, S, k + DG, nlev, st);
+    } else if (k >= 0) {
+      const bool sum_t = chain0 && Pd.mode == 1;
+      switch ((cnt + 31) >> 5) {
+        case 1: solve_level<T, TI, TO, 1>(Pd, L, S.b, S.u[cur], z, e0, cnt, sum_t, lane, tsum); break;
+        case 2: solve_level<T, TI, TO, 2>(Pd, L, S.b, S.u[cur], z, e0, cnt, sum_t, lane, tsum); break;
+        case 3: solve_level<T, TI, TO, 3>(Pd, L, S.b, S.u[cur], z, e0, cnt, sum_t, lane, tsum); break;
+        case 4: solve_level<T, TI, TO, 4>(Pd, L, S.b, S.u[cur], z, e0, cnt, sum_t, lane, tsum); break;
+        default: solve_level<T, TI, TO, 5>(Pd, L, S.b, S.u[cur], z, e0, cnt, sum_t, lane, tsum); break;
       }
     }
     __syncthreads();
-    prev ^= 1;
-    cur ^= 1;
+    if (k >= 0) {
+      prev ^= 1;
+      cur ^= 1;
+    }
   }
   if (!chain0) return;
   const int c0 = Pd.chain0_ent, c1 = Pd.lev_ent[lev1];
@@ -820,7 +889,27 @@ int pi_precond_create(pi_plan* plan, int coords, double regularization, double o
   P->dev.lev_ent = ip;
   if ((rc = upload_vec(P, H.elem, &ip))) return free_precond(P), rc;
   P->dev.elem = ip;
-  if ((rc = upload_vec(P, H.gsrc, &ip))) return free_precond(P), rc;
+  {
+    // the kernel keeps each level in slot order (entry i of a level with K = ceil(cnt / 32)
+    // entries per lane at (i mod K) 32 + i / K): store the gain positions as slots of the
+    // previous level
+    std::vector<int> gslot(H.gsrc.size());
+    for (size_t c = 0; c + 1 < H.chain_lev.size(); ++c) {
+      for (int lev = H.chain_lev[c]; lev < H.chain_lev[c + 1]; ++lev) {
+        const int Kp = lev > H.chain_lev[c] ? (H.lev_ent[lev] - H.lev_ent[lev - 1] + 31) / 32 : 1;
+        for (int e = H.lev_ent[lev]; e < H.lev_ent[lev + 1]; ++e) {
+          int packed = 0;
+          for (int q = 0; q < 3; ++q) {
+            int pos = (H.gsrc[e] >> (10 * q)) & 1023;
+            if (pos != 1023) pos = (pos % Kp) * 32 + pos / Kp;
+            packed |= pos << (10 * q);
+          }
+          gslot[e] = packed;
+        }
+      }
+    }
+    if ((rc = upload_vec(P, gslot, &ip))) return free_precond(P), rc;
+  }
   P->dev.gsrc = ip;
   rc = P->fp64 ? upload_factors<double>(P) : upload_factors<float>(P);
   if (rc) return free_precond(P), rc;

@@ -155,14 +155,34 @@ void cgs2_f64(Run& R, const double2* V, int nv, double2* w, double2* h1d, double
   cgs2_fetch<double2>(R, nv, h1d, hcol, rem2);
 }
 
-void cgs2_f32(Run& R, const float2* V, int nv, float2* w, double2* h1d, double2* h2d, std::vector<cd>& hcol,
-              double* rem2) {
+// Classical Gram-Schmidt of an FP32 w against V[0..nv) with selective reorthogonalisation
+// (Daniel-Gragg-Kaufman-Stewart): the second pass runs only when the first removed more than
+// half of |w|^2, i.e. |w_1|^2 < |w_0|^2 / 2; otherwise w_1 is already orthogonal to the basis
+// to working precision.  H column += h1 (+ h2) and *rem2 = |w|^2 at the end.  The mixed
+// precision solves use it (as the batched engine does); the plain FP64 path keeps two passes.
+void cgs_dgks_f32(Run& R, const float2* V, int nv, float2* w, double2* h1d, double2* h2d, std::vector<cd>& hcol,
+                  double* rem2) {
   pi_plan* p = R.p;
+  double* hp = p->host_pinned;
+  R.chk(norm2_f32(w, R.n, p->rs, 1, R.s));  // |w_0|^2 -> rresult[1]
   R.chk(mdot_f32(V, R.n, nv, w, R.n, p->rs, h1d, R.s));
-  R.chk(maxpy_f32(V, R.n, nv, h1d, w, R.n, p->rs, -1, R.s));
+  R.chk(maxpy_f32(V, R.n, nv, h1d, w, R.n, p->rs, 0, R.s));  // |w_1|^2 -> rresult[0]
+  R.chk(cudaMemcpyAsync(hp, h1d, sizeof(double2) * nv, cudaMemcpyDeviceToHost, R.s));
+  R.chk(cudaMemcpyAsync(hp + 2 * kMaxDots, p->rs.rresult, sizeof(double) * 2, cudaMemcpyDeviceToHost, R.s));
+  R.chk(cudaStreamSynchronize(R.s));
+  if (!R.ok()) return;
+  for (int i = 0; i < nv; ++i) hcol[i] += cd(hp[2 * i], hp[2 * i + 1]);
+  const double w1 = hp[2 * kMaxDots], w0 = hp[2 * kMaxDots + 1];
+  *rem2 = w1;
+  if (!(w1 < 0.5 * w0)) return;
   R.chk(mdot_f32(V, R.n, nv, w, R.n, p->rs, h2d, R.s));
   R.chk(maxpy_f32(V, R.n, nv, h2d, w, R.n, p->rs, 0, R.s));
-  cgs2_fetch<float2>(R, nv, h1d, hcol, rem2);
+  R.chk(cudaMemcpyAsync(hp, h2d, sizeof(double2) * nv, cudaMemcpyDeviceToHost, R.s));
+  R.chk(cudaMemcpyAsync(hp + 2 * kMaxDots, p->rs.rresult, sizeof(double), cudaMemcpyDeviceToHost, R.s));
+  R.chk(cudaStreamSynchronize(R.s));
+  if (!R.ok()) return;
+  for (int i = 0; i < nv; ++i) hcol[i] += cd(hp[2 * i], hp[2 * i + 1]);
+  *rem2 = hp[2 * kMaxDots];
 }
 
 void upper_triangular_solve(const std::vector<std::vector<cd>>& H, const std::vector<cd>& g, int k,
@@ -375,7 +395,7 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
         q = pw;
       }
       double rem2 = 0.0;
-      cgs2_f32(R, V, j + 1, q, h1d, h2d, H[j], &rem2);
+      cgs_dgks_f32(R, V, j + 1, q, h1d, h2d, H[j], &rem2);
       H[j][j + 1] = std::sqrt(rem2);
       if (H[j][j + 1] != cd(0, 0))
         R.chk(scale_f32(q, V + (long long)(j + 1) * n, n, make_double2(1.0 / H[j][j + 1].real(), 0.0), R.s));
