@@ -84,6 +84,17 @@ def solve_rates(picuda, torch):
                                  "normalized_residual": r.info["normalized_residual"],
                                  "trace_error": r.info["trace_error"]}
     ref = None
+    # the FP64 oracle's expv observables of the same 20 intervals (tests/golden, made by the
+    # oracle on the CPU): every dynamics result states its error against them
+    golden = ROOT / "tests" / "golden" / "ensemble_c2_N120_expv.npz"
+    oracle_obs = np.load(golden) if golden.exists() else None
+
+    def vs_oracle(vals):
+        if oracle_obs is None:
+            return None
+        return float(max(np.abs(v - oracle_obs[k]).max() / np.abs(oracle_obs[k]).max()
+                         for k, v in zip(("Jz", "JpJm"), vals)))
+
     c2 = picuda.compile(model_c2(picuda))
     rho0 = picuda.computational_product_state(c2.basis, 2)
     obs = {"Jz": picuda.collective_operator(c2.basis, sm["jz"]),
@@ -105,7 +116,8 @@ def solve_rates(picuda, torch):
         out[f"expv_{prec}"] = {"intervals_per_s": 1.0 / per, "ms_per_interval": per * 1e3,
                                "p50_ms_per_call": statistics.median(times) * 1e3, "p99_ms_per_call": max(times) * 1e3,
                                "intervals_per_call": nint,
-                               "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref).max()))}
+                               "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref).max())),
+                               "max_obs_rel_err_vs_oracle": vs_oracle(vals)}
     # The reference's default dynamics algorithm: fixed-step RK4, 64 steps per saved interval.
     ref_expv = ref
     for prec in ("fp64", "mixed"):
@@ -126,7 +138,8 @@ def solve_rates(picuda, torch):
                               "intervals_per_call": nint, "steps_per_interval": 64,
                               "max_obs_rel_err_vs_fp64": float(np.max(np.abs(vals - ref) / np.abs(ref).max())),
                               "max_obs_rel_dev_vs_expv_fp64": float(np.max(np.abs(vals - ref_expv)
-                                                                           / np.abs(ref_expv).max()))}
+                                                                           / np.abs(ref_expv).max())),
+                              "max_obs_rel_err_vs_oracle": vs_oracle(vals)}
     return out
 
 

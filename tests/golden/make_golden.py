@@ -22,7 +22,30 @@ def driven_c1():
     return O.driven_qubits(8, drive=1.0, emission=0.5, pumping=0.0)
 
 
+def ensemble_c2(N=120):
+    """The large time-evolution configuration: H = 0.3 Jz + 1.2 Jx, local decay 0.2, local
+    dephasing 0.1, collective decay 0.05/N on J-."""
+    s = O.spin_matrices(2)
+    return O.qubit_ensemble_model(N, hamiltonian=0.3 * s["jz"] + 1.2 * s["jx"], emission=0.2, dephasing=0.1,
+                                  collective_emission=0.05 / N)
+
+
+def c2_dynamics(nint=20):
+    """Oracle FP64 expv dynamics of the N=120 configuration from the all-excited state: saved
+    every dt = 0.05 for nint intervals (m = 30, atol 1e-10, rtol 1e-8), observables Jz and
+    J+J- (the references for the mixed and FP64 GPU paths)."""
+    plan = O.Plan(ensemble_c2(120))
+    b = plan.basis
+    s = O.spin_matrices(2)
+    obs = {"Jz": O.collective_operator(b, s["jz"]), "JpJm": O.collective_operator(b, s["jp"] @ s["jm"])}
+    rho0 = O.computational_product_state(b, 2)
+    dyn = O.solve_dynamics_expv(plan, rho0, (0.0, 0.05 * nint), saveat=0.05, observables=obs, save_states=False)
+    np.savez_compressed(OUT / "ensemble_c2_N120_expv.npz", t=np.array(dyn["t"]), Jz=dyn["values"]["Jz"],
+                        JpJm=dyn["values"]["JpJm"])
+
+
 def main():
+    c2_dynamics()
     rng = np.random.default_rng(20261203)
     plan = O.Plan(driven_c1())
     b = plan.basis
