@@ -157,6 +157,41 @@ __global__ void k_em_split_planes(const DevSector* __restrict__ sectors, const i
     }
 }
 
+// Separable line planes (SplitPlanes::srow / scol): per row a and per column b of sector
+// blockIdx.y, the factors of every merged coefficient in the order em_coef combines them.
+__global__ void k_sep_planes(const DevSector* __restrict__ sectors, const int4* __restrict__ canon,
+                             const float2* __restrict__ coef, const int* __restrict__ line_off, int nf4,
+                             float4* __restrict__ srow, float4* __restrict__ scol) {
+  // sandwich positions of the canonical table (slot * 3 + p + 1) in plane order
+  constexpr int kPos[9] = {4, 3, 0, 1, 6, 7, 5, 2, 8};
+  const int s = blockIdx.y;
+  const DevSector sec = sectors[s];
+  const int n = sec.n;
+  const int4* ct = canon + (long long)s * kCanonEntries;
+  const int npos = nf4 == kSepF4Plus ? 9 : 6;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float r[4 * kSepF4Plus], c[4 * kSepF4Plus];
+    for (int k = 0; k < 4 * nf4; ++k) r[k] = c[k] = 0.f;
+    const float2 aa = coef[ct[0].x + i], bb = coef[ct[0].y + i];
+    const float2 l0 = coef[ct[1].x + i], l1 = coef[ct[2].x + i];
+    const float2 r0 = coef[ct[3].y + i], r1 = coef[ct[4].y + i];
+    r[0] = aa.x; r[1] = aa.y; r[2] = l0.x; r[3] = l0.y; r[4] = l1.x; r[5] = l1.y;
+    c[0] = bb.x; c[1] = bb.y; c[2] = r0.x; c[3] = r0.y; c[4] = r1.x; c[5] = r1.y;
+    for (int p = 0; p < npos; ++p)
+      for (int t = 0; t < kCanonPerPos; ++t) {
+        const int4 e = ct[5 + kPos[p] * kCanonPerPos + t];
+        r[6 + 3 * p + t] = coef[e.x + i].x;
+        c[6 + 3 * p + t] = coef[e.y + i].x;
+      }
+    float4* ro = srow + (long long)(line_off[s] + i) * nf4;
+    float4* co = scol + (long long)(line_off[s] + i) * nf4;
+    for (int k = 0; k < nf4; ++k) {
+      ro[k] = make_float4(r[4 * k], r[4 * k + 1], r[4 * k + 2], r[4 * k + 3]);
+      co[k] = make_float4(c[4 * k], c[4 * k + 1], c[4 * k + 2], c[4 * k + 3]);
+    }
+  }
+}
+
 __device__ __forceinline__ void cmac2(float4& acc, const float cr, const float ci, const float4 v) {
   // acc.(xy) += c * v.(xy), acc.(zw) += c * v.(zw) (complex c = cr + i ci)
   acc.x = fmaf(cr, v.x, acc.x);
@@ -752,6 +787,20 @@ static int em_prepare_split(pi_plan* plan, int which, pi_plan::EmSplit* out) {
     sp.lrow = (const float4*)l_d;
     sp.rcol = (const float4*)r_d;
   }
+  if (!sp.srow) {
+    const int nf4 = dp.canon_plus ? kSepF4Plus : kSepF4;
+    void* sr = plan_alloc(plan, sizeof(float4) * (size_t)plan->em_nlines * nf4);
+    void* sc = plan_alloc(plan, sizeof(float4) * (size_t)plan->em_nlines * nf4);
+    if (!sr || !sc) return fail(PI_ERR_OUT_OF_MEMORY, "separable line planes");
+    dim3 grid(4, (unsigned)dp.nsectors);
+    k_sep_planes<<<grid, 128, 0, plan->stream>>>(dp.sectors, dp.canon, which ? dp.coef32z : dp.coef32x,
+                                                 plan->em_line_off, nf4, (float4*)sr, (float4*)sc);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(plan->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "separable line planes");
+    sp.srow = (const float4*)sr;
+    sp.scol = (const float4*)sc;
+  }
   *out = sp;
   return PI_OK;
 }
@@ -765,6 +814,8 @@ int em_split_planes(pi_plan* plan, int which, SplitPlanes* out) {
   out->rcol = sp.rcol;
   out->line_off = plan->em_line_off;
   out->plus = plan->dev.canon_plus ? 1 : 0;
+  out->srow = sp.srow;
+  out->scol = sp.scol;
   return PI_OK;
 }
 

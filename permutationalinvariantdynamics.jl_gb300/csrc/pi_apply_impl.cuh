@@ -305,6 +305,99 @@ __device__ __forceinline__ void apply_tile_planes_to(const DevSector* __restrict
   }
 }
 
+// The same tile from the separable line planes: each thread loads its row's factors once and
+// each column's factors as broadcast loads, and forms every merged coefficient with a few
+// FMAs in the order the entry plane was built, so y is bitwise the same as
+// apply_tile_planes_to's while only 16 bytes per entry (x in, y out) come from memory.
+template <bool PLUS, typename Sink>
+__device__ __forceinline__ void apply_tile_sep_to(const DevSector* __restrict__ sectors, const DevTile tile,
+                                                  const float2* __restrict__ x, const Sink& sink,
+                                                  const BorderArgs& border, const double2* alpha,
+                                                  const SplitPlanes& pl, float2* win) {
+  constexpr int NF4 = PLUS ? kSepF4Plus : kSepF4;
+  __shared__ __align__(16) float4 colp[kTileCols * NF4];  // the tile's column planes
+  const DevSector& sec = sectors[tile.sector];
+  const int la = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int n = sec.n;
+  const int loff = __ldg(pl.line_off + tile.sector);
+  // column planes of the tile's 32 columns land with the source windows (one cp.async wait)
+  for (int i = threadIdx.x; i < kTileCols * NF4; i += blockDim.x) {
+    const int b = tile.b0 + i / NF4;
+    const bool ok = b < n;
+    cp_async_zfill<16>(colp + i, ok ? pl.scol + (long long)(loff + b) * NF4 + i % NF4 : pl.scol, ok);
+  }
+  // this thread's row factors, in flight during the staging
+  const int a = tile.a0 + la;
+  const int ar = a < n ? a : 0;
+  float4 rv[NF4];
+#pragma unroll
+  for (int k = 0; k < NF4; ++k) rv[k] = __ldg(pl.srow + (long long)(loff + ar) * NF4 + k);
+  stage_windows<float>(sectors, sec, tile, x, win);
+  const int lb = warp * kColsPerThread;
+  const int b0 = tile.b0 + lb;
+  if (a >= n || b0 >= n) return;
+  const int ncol = min(kColsPerThread, n - b0);
+  float r[4 * NF4];
+#pragma unroll
+  for (int k = 0; k < NF4; ++k) {
+    r[4 * k] = rv[k].x;
+    r[4 * k + 1] = rv[k].y;
+    r[4 * k + 2] = rv[k].z;
+    r[4 * k + 3] = rv[k].w;
+  }
+  const float2* wb = win + (la + kHalo) + (lb + kHalo) * kWinRows;
+  const long long e0 = sec.offset + a + (long long)b0 * n;
+  const float scale = (float)border.scale;
+  const bool has_sm = sec.src[0] >= 0, has_lg = sec.src[2] >= 0;  // block-uniform
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) {
+    if (k >= ncol) break;
+    // the same column for the whole warp: broadcast shared reads at their point of use
+    const float* c = reinterpret_cast<const float*>(colp + (lb + k) * NF4);
+    // sandwich position p: alpha_0 beta_0 + alpha_1 beta_1 + alpha_2 beta_2
+    auto sand = [&](int p) {
+      const int o = 6 + 3 * p;
+      return fmaf(r[o + 2], c[o + 2], fmaf(r[o + 1], c[o + 1], r[o] * c[o]));
+    };
+    const float cre = fmaf(r[8], c[8], fmaf(r[7], c[7], fmaf(r[6], c[6], r[0] + c[0])));
+    const float cim = r[1] + c[1];
+    const float2* w = wb + k * kWinRows;
+    const float2* own = w + kWinElems;
+    float2 acc = make_float2(0.f, 0.f);
+    pmac(acc, cre, cim, own[0]);                          // centre
+    pmac(acc, r[2], r[3], own[-1]);                       // LEFT -1
+    pmac(acc, r[4], r[5], own[1]);                        // LEFT +1
+    pmac(acc, c[2], c[3], own[-kWinRows]);                // RIGHT -1
+    pmac(acc, c[4], c[5], own[kWinRows]);                 // RIGHT +1
+    prmac(acc, sand(1), own[-1 - kWinRows]);              // own (-1,-1)
+    if (has_sm) {
+      prmac(acc, sand(2), w[-1 - kWinRows]);              // smaller (-2,-2)
+      prmac(acc, sand(3), w[0]);                          // smaller (-1,-1)
+    }
+    if (has_lg) {
+      prmac(acc, sand(4), w[2 * kWinElems - 1 - kWinRows]);  // larger (0,0)
+      prmac(acc, sand(5), w[2 * kWinElems]);                 // larger (1,1)
+    }
+    if (PLUS) {
+      prmac(acc, sand(6), own[1 + kWinRows]);                          // own (1,1)
+      if (has_sm) prmac(acc, sand(7), w[1 + kWinRows]);                // smaller (0,0)
+      if (has_lg) prmac(acc, sand(8), w[2 * kWinElems + 1 + kWinRows]);  // larger (2,2)
+    }
+    if (border.scale != 1.0) {
+      acc.x *= scale;
+      acc.y *= scale;
+    }
+    if (b0 + k == a && alpha != nullptr) {
+      const double2 al = *alpha;
+      const double v = border.coords ? sec.border_z : sec.border_x;
+      acc.x += (float)(al.x * v);
+      acc.y += (float)(al.y * v);
+    }
+    sink(e0 + (long long)k * n, acc);
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ void apply_tile(const DevSector* __restrict__ sectors, const DevTerm* __restrict__ terms,
                                            const typename Vec2<T>::type* __restrict__ coef, const DevTile tile,

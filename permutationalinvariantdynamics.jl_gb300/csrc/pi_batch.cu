@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kRT) k_s1_trace(DevInst* __restrict__ st) {
 // Applies over the (instance, tile) list.  AUX: ay = aux_scale L ax (+ border), FP64;
 // otherwise the Arnoldi step w = scale L V_j (+ border) in the basis precision.
 template <typename T, bool AUX>
-__global__ void __launch_bounds__(kApplyThreads)
+__global__ void __launch_bounds__(kApplyThreads, sizeof(T) == 4 && !AUX ? 4 : 1)
     k_bapply(const DevInst* __restrict__ st, const int* __restrict__ tile_inst, const int* __restrict__ tile_local) {
   using T2 = typename Vec2<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -195,10 +195,16 @@ __global__ void __launch_bounds__(kApplyThreads)
     if constexpr (sizeof(T) == sizeof(float)) {
       if (S.planes.eplane != nullptr && S.coords == S.pwhich) {  // block-uniform
         const StoreSink<float2> sink{(float2*)S.w};
-        if (S.planes.plus)
+        if (S.planes.srow != nullptr) {  // separable line planes: x in, y out per entry
+          if (S.planes.plus)
+            apply_tile_sep_to<true>(S.sectors, tile, xin, sink, b, S.border ? &S.alpha : nullptr, S.planes, win);
+          else
+            apply_tile_sep_to<false>(S.sectors, tile, xin, sink, b, S.border ? &S.alpha : nullptr, S.planes, win);
+        } else if (S.planes.plus) {
           apply_tile_planes_to<true>(S.sectors, tile, xin, sink, b, S.border ? &S.alpha : nullptr, S.planes, win);
-        else
+        } else {
           apply_tile_planes_to<false>(S.sectors, tile, xin, sink, b, S.border ? &S.alpha : nullptr, S.planes, win);
+        }
         return;
       }
     }

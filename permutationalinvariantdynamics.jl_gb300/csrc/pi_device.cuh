@@ -81,6 +81,19 @@ struct SplitPlanes {
   const float4* rcol;
   const int* line_off;  // per sector: start of its row and column planes
   int plus;             // three entry float4 (pumping terms at the +1 diagonal shifts)
+  // Separable line planes (kSepF4 or kSepF4Plus float4 per row and per column): every merged
+  // coefficient is (alpha_add[a] + beta_add[b]) or a sum of at most three real products
+  // alpha_t[a] beta_t[b], so a single-column tile rebuilds it from its row's and column's
+  // factors instead of streaming 32-48 bytes per entry.  Row floats: alpha_add (re, im),
+  // LEFT -1 (re, im), LEFT +1 (re, im), then alpha_t of the sandwich positions own centre,
+  // own (-1,-1), smaller (-2,-2), smaller (-1,-1), larger (0,0), larger (1,1)[, own (1,1),
+  // smaller (0,0), larger (2,2)], three terms each; column floats the same with beta_add,
+  // RIGHT -1, RIGHT +1 and beta_t.
+  const float4* srow;
+  const float4* scol;
 };
+
+constexpr int kSepF4 = 6;      // 24 floats: 6 + 3 x 6 positions
+constexpr int kSepF4Plus = 9;  // 36 floats: 6 + 3 x 9 positions, padded
 
 }  // namespace picuda

@@ -55,6 +55,8 @@ struct pi_plan {
     const float4* eplane = nullptr;
     const float4* lrow = nullptr;
     const float4* rcol = nullptr;
+    const float4* srow = nullptr;  // separable line planes of the single-column tile apply
+    const float4* scol = nullptr;
   };
   EmSplit em_split[2];
   const int* em_line_off = nullptr;
