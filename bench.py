@@ -234,7 +234,7 @@ def request_stream(count, seed=0, nmin=10, nmax=300, steady_fraction=0.3):
     return reqs
 
 
-def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9):
+def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9, precisions=("fp64", "mixed")):
     """Continuous-batching server on a Poisson request stream at `rate` req/s (the lowest
     rate of the served configuration; the stream saturates the GPU): p50/p99 latency
     (finish - submit) and completed solves/s, FP64 vs mixed, same requests and arrival
@@ -251,7 +251,7 @@ def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9):
            "steady": sum(1 for r in reqs if r["kind"] == "steady"),
            "max_dim": int(max(len(m.basis) for m in models))}
     states, finals = {}, {}
-    for prec in ("fp64", "mixed"):
+    for prec in precisions:
         with picuda.Server(precision=prec, memory_budget=budget) as srv:
             t0 = time.perf_counter()
             done = []
@@ -278,11 +278,15 @@ def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9):
                 res[f"{kind}_p50_ms"] = float(np.percentile(kl, 50) * 1e3)
                 res[f"{kind}_p99_ms"] = float(np.percentile(kl, 99) * 1e3)
         res["failed"] = [f"{c.tag}:{c.message[:80]}" for c in done if not c.ok][:5]
+        res["ok_by_kind"] = {k: sum(1 for c in ok if c.kind == k) for k in ("dynamics", "steady")}
+        res["failed_by_kind"] = {k: sum(1 for c in done if not c.ok and c.kind == k) for k in ("dynamics", "steady")}
         dyn = [c for c in done if c.ok and c.kind == "dynamics"]
         res["max_final_trace_error_dynamics"] = max((abs(c.values["tr"][-1] - 1) for c in dyn), default=None)
         out[prec] = res
         states[prec] = {c.tag: c.state for c in done if c.ok}
         finals[prec] = {c.tag: (c.values["tr"][-1], c.values["Jz"][-1]) for c in dyn}
+    if len(precisions) < 2:
+        return out
     # observable deviation on requests whose FP64 trace stayed within 1e-6 (the reference's
     # reference-coordinate error control loses trace at large N; see the FP64 trace errors)
     jdev, kept = 0.0, 0
@@ -306,6 +310,17 @@ def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9):
             out[f"worst_{kind}_request"] = {"N": reqs[worst - 1]["params"][0], "params": reqs[worst - 1]["params"],
                                             "t_final": reqs[worst - 1]["t_final"]}
     out["solves_per_s_ratio_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    return out
+
+
+def serve_sweep(picuda, torch, rates, count, fp64_rates=1):
+    """The served configuration's rate sweep: `count` requests per rate, mixed precision at
+    every rate, plain FP64 at the first `fp64_rates` rates (the FP64 server needs minutes per
+    rate at this size)."""
+    out = {"requests_per_rate": count, "rates": list(rates), "per_rate": {}}
+    for i, rate in enumerate(rates):
+        precs = ("fp64", "mixed") if i < fp64_rates else ("mixed",)
+        out["per_rate"][str(rate)] = serve_rates(picuda, torch, count, rate, precisions=precs)
     return out
 
 
@@ -692,6 +707,8 @@ def main():
     ap.add_argument("--scan-intervals", type=int, default=2)
     ap.add_argument("--scan-precision", default="both", choices=["both", "fp64", "mixed"])
     ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-sweep", default=None,
+                    help="comma-separated request rates: run only the served rate sweep (e.g. 50,200,1000,2000)")
     ap.add_argument("--only-steady", action="store_true", help="run only the steady-state rate section")
     ap.add_argument("--only-steady-c3", action="store_true",
                     help="run only the N=200 preconditioned steady-state section")
@@ -735,6 +752,10 @@ def main():
         print(json.dumps({"only_steady_c3": True,
                           "steady_c3": steady_c3_rates(picuda, torch, omegas=omegas, repeats=args.c3_repeats,
                                                        plain=not args.c3_no_plain)}))
+        return 0
+    if args.serve_sweep:
+        rates = [float(v) for v in args.serve_sweep.split(",")]
+        print(json.dumps({"serve_sweep": serve_sweep(picuda, torch, rates, args.serve_requests)}))
         return 0
     if args.only_serve:
         print(json.dumps({"only_serve": True, "serve": serve_rates(picuda, torch, args.serve_requests)}))
