@@ -401,7 +401,8 @@ def btc_model(picuda, N, omega_over_kappa):
                                        dephasing=0.01)
 
 
-def steady_c3_rates(picuda, torch, N=200, omegas=(0.5, 1.0, 2.0), repeats=5, tol=5e-11, plain=True):
+def steady_c3_rates(picuda, torch, N=200, omegas=(0.5, 1.0, 2.0), repeats=5, tol=5e-11, plain=True, concurrent=True,
+                    served_per_omega=3):
     """Steady states of the N=200 boundary-time-crystal-like model (dim 1,373,701) for
     Omega in {0.5, 1, 2} kappa: restarted GMRES(50) left-preconditioned by the level sweep,
     in population coordinates, to a normalized residual and trace error of 1e-10
@@ -458,6 +459,47 @@ def steady_c3_rates(picuda, torch, N=200, omegas=(0.5, 1.0, 2.0), repeats=5, tol
         out[prec] = {"solves_per_s": len(a) / a.sum(), "p50_ms": float(np.percentile(a, 50) * 1e3),
                      "p99_ms": float(np.percentile(a, 99) * 1e3), "solves": int(len(a))}
     out["solves_per_s_ratio_mixed_vs_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    if concurrent:
+        out["served"] = steady_c3_served(picuda, torch, N, omegas, repeats, tol, per_omega=served_per_omega)
+        out["served_mixed_vs_plain_fp64"] = out["served"]["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    return out
+
+
+def steady_c3_served(picuda, torch, N, omegas, repeats, tol, per_omega=2):
+    """The same solves in served form: per_omega host threads per Omega, each with its own
+    compiled model, preconditioner and CUDA stream, keep solving, so independent requests
+    overlap on the GPU.  Throughput = solves / wall time; latency = each solve's own duration."""
+    from concurrent.futures import ThreadPoolExecutor
+    comps = [picuda.compile(btc_model(picuda, N, w)) for w in omegas for _ in range(per_omega)]
+    precs = [picuda.level_preconditioner(c, coords="population") for c in comps]
+    nw = len(comps)
+    out = {"workers": nw, "solves_per_worker": repeats}
+    for prec in ("fp64", "mixed"):
+        algs = [picuda.GMRESAlgorithm(krylovdim=50, maxiter=2000, preconditioner=P, precision=prec) for P in precs]
+        for c, a in zip(comps, algs):
+            picuda.stationary_state(c, algorithm=a, atol=tol, rtol=tol)  # warm
+
+        def worker(i):
+            torch.cuda.set_device(torch.cuda.current_device())
+            lat = []
+            for _ in range(repeats):
+                t0 = time.perf_counter()
+                r = picuda.stationary_state(comps[i], algorithm=algs[i], return_info=True, atol=tol, rtol=tol)
+                lat.append(time.perf_counter() - t0)
+                if not r.info["converged"]:
+                    raise RuntimeError("served C3 solve did not converge")
+            return lat
+
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=nw) as ex:
+            lats = [x for part in ex.map(worker, range(nw)) for x in part]
+        wall = time.perf_counter() - t0
+        a = np.array(lats)
+        out[prec] = {"solves_per_s": len(a) / wall, "wall_s": wall, "p50_ms": float(np.percentile(a, 50) * 1e3),
+                     "p99_ms": float(np.percentile(a, 99) * 1e3), "solves": int(len(a))}
+    for P in precs:
+        P.close()
     return out
 
 
@@ -713,6 +755,8 @@ def main():
     ap.add_argument("--only-steady-c3", action="store_true",
                     help="run only the N=200 preconditioned steady-state section")
     ap.add_argument("--c3-repeats", type=int, default=5)
+    ap.add_argument("--c3-served-per-omega", type=int, default=3,
+                    help="concurrent solvers per Omega in the served form of the N=200 section")
     ap.add_argument("--c3-omegas", default="0.5,1,2", help="Omega/kappa values of the N=200 steady-state section")
     ap.add_argument("--c3-no-plain", action="store_true",
                     help="skip the unpreconditioned reference-method attempt (profiling runs)")
@@ -751,7 +795,8 @@ def main():
         omegas = tuple(float(v) for v in args.c3_omegas.split(","))
         print(json.dumps({"only_steady_c3": True,
                           "steady_c3": steady_c3_rates(picuda, torch, omegas=omegas, repeats=args.c3_repeats,
-                                                       plain=not args.c3_no_plain)}))
+                                                       plain=not args.c3_no_plain,
+                                                       served_per_omega=args.c3_served_per_omega)}))
         return 0
     if args.serve_sweep:
         rates = [float(v) for v in args.serve_sweep.split(",")]
