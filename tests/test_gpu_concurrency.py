@@ -80,6 +80,7 @@ def test_reject_mode_raises_busy_while_in_use(torch_cuda):
     t = threading.Thread(target=long_call)
     t.start()
     running.wait()
+    time.sleep(0.3)  # let the long call take the model (its 800 saved intervals run for seconds)
     busy = False
     deadline = time.time() + 30
     while not done.is_set() and time.time() < deadline:
