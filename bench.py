@@ -209,6 +209,8 @@ def scan_rates(picuda, torch, count=256, intervals=2, seed=0, precisions=("fp64"
                      "accepted_steps": int(sum(i["accepted_steps"] for i in infos)),
                      "operator_applications": int(sum(i["operator_applications"] for i in infos))}
         out[prec]["applies_per_s"] = out[prec]["operator_applications"] / dt
+        if prec == "mixed":  # the FP32 engine's step-apply schedule (chosen in the untimed call)
+            out[prec]["apply_schedule"] = picuda.engine_schedule_info()
     if len(vals) < 2:
         return out
     dev = 0.0
@@ -748,6 +750,8 @@ def main():
     ap.add_argument("--scan-instances", type=int, default=256)
     ap.add_argument("--scan-intervals", type=int, default=2)
     ap.add_argument("--scan-precision", default="both", choices=["both", "fp64", "mixed"])
+    ap.add_argument("--engine-schedule", default="auto",
+                    help="FP32 engine step-apply schedule: auto, per_tile or blocks per SM (an int)")
     ap.add_argument("--serve-requests", type=int, default=24)
     ap.add_argument("--serve-sweep", default=None,
                     help="comma-separated request rates: run only the served rate sweep (e.g. 50,200,1000,2000)")
@@ -778,6 +782,8 @@ def main():
     __graft_entry__.build()
     import picuda
     torch.cuda.set_device(local)
+    sched = args.engine_schedule
+    picuda.set_engine_schedule(int(sched) if sched.lstrip("-").isdigit() else sched)
     if args.only_solves:
         print(json.dumps({"only_solves": True, "solves": solve_rates(picuda, torch)}))
         return 0

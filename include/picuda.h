@@ -460,6 +460,31 @@ int pi_dynamics_batch(int njobs, const pi_dynamics_job_t* jobs, const pi_expv_op
 int pi_steady_state_batch(int ninst, pi_plan* const* plans, double* const* x_devs,
                           const pi_gmres_opts_t* opts, pi_gmres_info_t* infos);
 
+/* Schedule of the FP32 Arnoldi-step apply of the batched engine (the batched entry points
+ * above and PI_FP32 servers).  PI_SCHEDULE_PER_TILE launches one block per (instance,
+ * sector-tile) item; k >= 1 launches k blocks per SM (clamped to the resident limit) that
+ * walk the item list persistently, prefetching each next tile's staged windows while
+ * computing the current one.  PI_SCHEDULE_AUTO (the default) times every candidate with
+ * CUDA events on the engine stream before the first Krylov cycle of a job set whose shape
+ * (work-list size class, canonical or general stencils) has not been seen by that engine,
+ * and keeps the fastest; the timed launches write only the step's scratch column, which
+ * the cycle recomputes.  Every schedule gives bitwise the same results.  Process-wide;
+ * applies to engines that choose a schedule after the call. */
+enum { PI_SCHEDULE_AUTO = 0, PI_SCHEDULE_PER_TILE = -1 };
+int pi_engine_set_apply_schedule(int schedule);
+
+typedef struct {
+  int choices;        /* schedules chosen so far, process-wide (tuned or cached or set) */
+  int tunings;        /* of which timed */
+  int schedule;       /* the last choice: PI_SCHEDULE_PER_TILE or blocks per SM */
+  int items;          /* work-list items of the job set it was made for */
+  int resident_max;   /* resident blocks per SM of the persistent launch */
+  int ncand;          /* candidates of the last timing (0 if the last choice was not timed) */
+  int cand[8];        /* PI_SCHEDULE_PER_TILE or blocks per SM */
+  double cand_us[8];  /* median launch time of each, microseconds */
+} pi_schedule_info_t;
+int pi_engine_schedule_info(pi_schedule_info_t* out);
+
 /* ---- serving: continuous batching of time-evolution and steady-state requests --------
  * A server owns one batched engine and a worker thread.  Requests are admitted in arrival
  * order between engine ticks while their device footprint (Krylov basis, image and state

@@ -305,10 +305,71 @@ __device__ __forceinline__ void apply_tile_planes_to(const DevSector* __restrict
   }
 }
 
+// The output entries (a, b0 .. b0 + ncol - 1) of one thread from the separable line planes:
+// r holds row a's factors, colp the tile's column factors, wb points at the thread's entry
+// (a, b0) in the own-sector-relative window frame of staged windows with WR rows and WE
+// elements per slot.  Every merged coefficient is formed with a few FMAs in the order the
+// entry plane was built, so the result is bitwise apply_tile_planes_to's.
+template <bool PLUS, int WR, int WE, typename Sink>
+__device__ __forceinline__ void sep_entries(const float* r, const float4* colp, const float2* wb, int lb, int ncol,
+                                            int a, int b0, const DevSector& sec, const BorderArgs& border,
+                                            const double2* alpha, const Sink& sink) {
+  constexpr int NF4 = PLUS ? kSepF4Plus : kSepF4;
+  const int n = sec.n;
+  const long long e0 = sec.offset + a + (long long)b0 * n;
+  const float scale = (float)border.scale;
+  const bool has_sm = sec.src[0] >= 0, has_lg = sec.src[2] >= 0;  // block-uniform
+#pragma unroll
+  for (int k = 0; k < kColsPerThread; ++k) {
+    if (k >= ncol) break;
+    // the same column for the whole warp: broadcast shared reads at their point of use
+    const float* c = reinterpret_cast<const float*>(colp + (lb + k) * NF4);
+    // sandwich position p: alpha_0 beta_0 + alpha_1 beta_1 + alpha_2 beta_2
+    auto sand = [&](int p) {
+      const int o = 6 + 3 * p;
+      return fmaf(r[o + 2], c[o + 2], fmaf(r[o + 1], c[o + 1], r[o] * c[o]));
+    };
+    const float cre = fmaf(r[8], c[8], fmaf(r[7], c[7], fmaf(r[6], c[6], r[0] + c[0])));
+    const float cim = r[1] + c[1];
+    const float2* w = wb + k * WR;
+    const float2* own = w + WE;
+    float2 acc = make_float2(0.f, 0.f);
+    pmac(acc, cre, cim, own[0]);                          // centre
+    pmac(acc, r[2], r[3], own[-1]);                       // LEFT -1
+    pmac(acc, r[4], r[5], own[1]);                        // LEFT +1
+    pmac(acc, c[2], c[3], own[-WR]);                      // RIGHT -1
+    pmac(acc, c[4], c[5], own[WR]);                       // RIGHT +1
+    prmac(acc, sand(1), own[-1 - WR]);                    // own (-1,-1)
+    if (has_sm) {
+      prmac(acc, sand(2), w[-1 - WR]);                    // smaller (-2,-2)
+      prmac(acc, sand(3), w[0]);                          // smaller (-1,-1)
+    }
+    if (has_lg) {
+      prmac(acc, sand(4), w[2 * WE - 1 - WR]);            // larger (0,0)
+      prmac(acc, sand(5), w[2 * WE]);                     // larger (1,1)
+    }
+    if (PLUS) {
+      prmac(acc, sand(6), own[1 + WR]);                          // own (1,1)
+      if (has_sm) prmac(acc, sand(7), w[1 + WR]);                // smaller (0,0)
+      if (has_lg) prmac(acc, sand(8), w[2 * WE + 1 + WR]);       // larger (2,2)
+    }
+    if (border.scale != 1.0) {
+      acc.x *= scale;
+      acc.y *= scale;
+    }
+    if (b0 + k == a && alpha != nullptr) {
+      const double2 al = *alpha;
+      const double v = border.coords ? sec.border_z : sec.border_x;
+      acc.x += (float)(al.x * v);
+      acc.y += (float)(al.y * v);
+    }
+    sink(e0 + (long long)k * n, acc);
+  }
+}
+
 // The same tile from the separable line planes: each thread loads its row's factors once and
-// each column's factors as broadcast loads, and forms every merged coefficient with a few
-// FMAs in the order the entry plane was built, so y is bitwise the same as
-// apply_tile_planes_to's while only 16 bytes per entry (x in, y out) come from memory.
+// each column's factors as broadcast loads, so y is bitwise the same as apply_tile_planes_to's
+// while only 16 bytes per entry (x in, y out) come from memory.
 template <bool PLUS, typename Sink>
 __device__ __forceinline__ void apply_tile_sep_to(const DevSector* __restrict__ sectors, const DevTile tile,
                                                   const float2* __restrict__ x, const Sink& sink,
@@ -337,7 +398,6 @@ __device__ __forceinline__ void apply_tile_sep_to(const DevSector* __restrict__ 
   const int lb = warp * kColsPerThread;
   const int b0 = tile.b0 + lb;
   if (a >= n || b0 >= n) return;
-  const int ncol = min(kColsPerThread, n - b0);
   float r[4 * NF4];
 #pragma unroll
   for (int k = 0; k < NF4; ++k) {
@@ -347,55 +407,107 @@ __device__ __forceinline__ void apply_tile_sep_to(const DevSector* __restrict__ 
     r[4 * k + 3] = rv[k].w;
   }
   const float2* wb = win + (la + kHalo) + (lb + kHalo) * kWinRows;
-  const long long e0 = sec.offset + a + (long long)b0 * n;
-  const float scale = (float)border.scale;
-  const bool has_sm = sec.src[0] >= 0, has_lg = sec.src[2] >= 0;  // block-uniform
-#pragma unroll
-  for (int k = 0; k < kColsPerThread; ++k) {
-    if (k >= ncol) break;
-    // the same column for the whole warp: broadcast shared reads at their point of use
-    const float* c = reinterpret_cast<const float*>(colp + (lb + k) * NF4);
-    // sandwich position p: alpha_0 beta_0 + alpha_1 beta_1 + alpha_2 beta_2
-    auto sand = [&](int p) {
-      const int o = 6 + 3 * p;
-      return fmaf(r[o + 2], c[o + 2], fmaf(r[o + 1], c[o + 1], r[o] * c[o]));
-    };
-    const float cre = fmaf(r[8], c[8], fmaf(r[7], c[7], fmaf(r[6], c[6], r[0] + c[0])));
-    const float cim = r[1] + c[1];
-    const float2* w = wb + k * kWinRows;
-    const float2* own = w + kWinElems;
-    float2 acc = make_float2(0.f, 0.f);
-    pmac(acc, cre, cim, own[0]);                          // centre
-    pmac(acc, r[2], r[3], own[-1]);                       // LEFT -1
-    pmac(acc, r[4], r[5], own[1]);                        // LEFT +1
-    pmac(acc, c[2], c[3], own[-kWinRows]);                // RIGHT -1
-    pmac(acc, c[4], c[5], own[kWinRows]);                 // RIGHT +1
-    prmac(acc, sand(1), own[-1 - kWinRows]);              // own (-1,-1)
-    if (has_sm) {
-      prmac(acc, sand(2), w[-1 - kWinRows]);              // smaller (-2,-2)
-      prmac(acc, sand(3), w[0]);                          // smaller (-1,-1)
-    }
-    if (has_lg) {
-      prmac(acc, sand(4), w[2 * kWinElems - 1 - kWinRows]);  // larger (0,0)
-      prmac(acc, sand(5), w[2 * kWinElems]);                 // larger (1,1)
-    }
-    if (PLUS) {
-      prmac(acc, sand(6), own[1 + kWinRows]);                          // own (1,1)
-      if (has_sm) prmac(acc, sand(7), w[1 + kWinRows]);                // smaller (0,0)
-      if (has_lg) prmac(acc, sand(8), w[2 * kWinElems + 1 + kWinRows]);  // larger (2,2)
-    }
-    if (border.scale != 1.0) {
-      acc.x *= scale;
-      acc.y *= scale;
-    }
-    if (b0 + k == a && alpha != nullptr) {
-      const double2 al = *alpha;
-      const double v = border.coords ? sec.border_z : sec.border_x;
-      acc.x += (float)(al.x * v);
-      acc.y += (float)(al.y * v);
-    }
-    sink(e0 + (long long)k * n, acc);
+  sep_entries<PLUS, kWinRows, kWinElems>(r, colp, wb, lb, min(kColsPerThread, n - b0), a, b0, sec, border, alpha,
+                                         sink);
+}
+
+// ---------------------------------------------------------------------------------------
+// Two-stage separable-plane tiles for persistent launches.  The canonical positions read
+// only the shifts -1..+1 around (a + e, b + e), so each source window needs a halo of one
+// (34 x 34) instead of the general stencil's two (36 x 36).  One stage holds the three
+// windows and the tile's 32 row and 32 column factor lines; a block computes the tile of one
+// stage while the next tile's stage is in flight.
+// ---------------------------------------------------------------------------------------
+constexpr int kSepRows = kTileRows + 2;
+constexpr int kSepCols = kTileCols + 2;
+constexpr int kSepElems = kSepRows * kSepCols;
+constexpr int kSepLineBytes = kTileRows * kSepF4Plus * 16;                    // row or column factors
+constexpr int kSepStageBytes = 3 * kSepElems * (int)sizeof(float2) + 2 * kSepLineBytes;
+constexpr int kSepSmemBytes = 2 * kSepStageBytes;
+static_assert(kSepStageBytes % 16 == 0, "stages must keep 16-byte cp.async destinations aligned");
+static_assert(kTileRows == kTileCols, "row and column factor lines share one stage layout");
+
+struct SepStage {
+  float2* win;   // [3][kSepElems]: slot e + 1 starts at (a0 + e - 1, b0 + e - 1)
+  float4* colp;  // [kTileCols][NF4]
+  float4* rowp;  // [kTileRows][NF4]
+};
+
+__device__ __forceinline__ SepStage sep_stage(unsigned char* smem, int stage) {
+  unsigned char* p = smem + stage * kSepStageBytes;
+  constexpr int kWinBytes = 3 * kSepElems * (int)sizeof(float2);
+  return SepStage{reinterpret_cast<float2*>(p), reinterpret_cast<float4*>(p + kWinBytes),
+                  reinterpret_cast<float4*>(p + kWinBytes + kSepLineBytes)};
+}
+
+// Issues (and commits as one cp.async group) the stage of `tile`: the zero-padded windows
+// x_src[a0 + e - 2 .. a0 + e + 31, b0 + e - 2 .. b0 + e + 31] of the source sectors that exist
+// (lane = window row, plus rows 32..33 on lanes 0..1; warps stride over the 34 columns) and
+// the factor lines of the tile's rows and columns (zeros past the block edge).
+template <int NF4>
+__device__ __forceinline__ void sep_issue(const DevSector* __restrict__ sectors, const DevTile tile,
+                                          const float2* __restrict__ x, const SplitPlanes& pl, SepStage sg) {
+  const DevSector& sec = sectors[tile.sector];
+  const int n = sec.n;
+  const int loff = __ldg(pl.line_off + tile.sector);
+  for (int i = threadIdx.x; i < 2 * kTileCols * NF4; i += blockDim.x) {
+    const bool col = i < kTileCols * NF4;
+    const int ii = col ? i : i - kTileCols * NF4;
+    const int q = (col ? tile.b0 : tile.a0) + ii / NF4;
+    const float4* src = col ? pl.scol : pl.srow;
+    const bool ok = q < n;
+    cp_async_zfill<16>((col ? sg.colp : sg.rowp) + ii, ok ? src + (long long)(loff + q) * NF4 + ii % NF4 : src, ok);
   }
+  const int la = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const bool extra = la < kSepRows - 32;
+#pragma unroll 1
+  for (int slot = 0; slot < 3; ++slot) {
+    const int s2 = sec.src[slot];
+    if (s2 < 0) continue;
+    const int m = sectors[s2].n;
+    const float2* xs = x + sectors[s2].offset;
+    const int r0 = tile.a0 + slot - 2, c0 = tile.b0 + slot - 2;
+    float2* w = sg.win + slot * kSepElems;
+    const int R = r0 + la, R2 = r0 + 32 + la;
+    const bool rv = (unsigned)R < (unsigned)m, rv2 = extra && (unsigned)R2 < (unsigned)m;
+#pragma unroll
+    for (int j = warp; j < kSepCols; j += kApplyWarps) {
+      const int C = c0 + j;
+      const bool cv = (unsigned)C < (unsigned)m;
+      const bool v1 = rv && cv, v2 = rv2 && cv;
+      cp_async_zfill<sizeof(float2)>(w + la + j * kSepRows, v1 ? xs + R + (long long)C * m : x, v1);
+      if (extra) cp_async_zfill<sizeof(float2)>(w + 32 + la + j * kSepRows, v2 ? xs + R2 + (long long)C * m : x, v2);
+    }
+  }
+  cp_async_commit();
+}
+
+// The tile of a landed stage (the caller has waited for its group and synchronised).
+template <bool PLUS, typename Sink>
+__device__ __forceinline__ void sep_compute(const DevSector* __restrict__ sectors, const DevTile tile, const Sink& sink,
+                                            const BorderArgs& border, const double2* alpha, SepStage sg) {
+  constexpr int NF4 = PLUS ? kSepF4Plus : kSepF4;
+  const DevSector& sec = sectors[tile.sector];
+  const int la = threadIdx.x & 31;
+  const int lb = (threadIdx.x >> 5) * kColsPerThread;
+  const int n = sec.n;
+  const int a = tile.a0 + la;
+  const int b0 = tile.b0 + lb;
+  if (a >= n || b0 >= n) return;
+  float r[4 * NF4];
+  const float4* rp = sg.rowp + la * NF4;
+#pragma unroll
+  for (int k = 0; k < NF4; ++k) {
+    const float4 v = rp[k];
+    r[4 * k] = v.x;
+    r[4 * k + 1] = v.y;
+    r[4 * k + 2] = v.z;
+    r[4 * k + 3] = v.w;
+  }
+  const float2* wb = sg.win + (la + 1) + (lb + 1) * kSepRows;
+  sep_entries<PLUS, kSepRows, kSepElems>(r, sg.colp, wb, lb, min(kColsPerThread, n - b0), a, b0, sec, border, alpha,
+                                         sink);
 }
 
 template <typename T>

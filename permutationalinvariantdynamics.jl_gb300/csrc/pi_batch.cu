@@ -4,10 +4,13 @@
 #include "pi_batch.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
 #include <random>
 #include <tuple>
 #include <unordered_set>
@@ -210,6 +213,85 @@ __global__ void __launch_bounds__(kApplyThreads, sizeof(T) == 4 && !AUX ? 4 : 1)
     }
     apply_tile<T>(S.sectors, S.terms, (const T2*)S.coefb, tile, xin, (T2*)S.w, b, S.border ? &S.alpha : nullptr, win,
                   sterms, ge);
+  }
+}
+
+// Persistent FP32 Arnoldi-step apply w = scale L V_j (+ border) over the (instance, tile)
+// list: gridDim.x blocks (a multiple of the SM count, picked by the engine's autotuner)
+// stride over the list.  Tiles of instances with separable line planes run two-stage: a
+// block computes one tile while the stage of its next such tile is in flight; any other
+// tile runs the general stencil synchronously.  Per-entry arithmetic is k_bapply<float,
+// false>'s, so w is bitwise the same for every grid size and for the one-block-per-tile
+// launch.
+__global__ void __launch_bounds__(kApplyThreads, 3)
+    k_bapply_persist(const DevInst* __restrict__ st, const int* __restrict__ tile_inst,
+                     const int* __restrict__ tile_local, int ntotal) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // work kind of list item i, block-uniform: 0 skip (instance stopped this cycle), 1 / 2
+  // separable planes without / with the +1 diagonal shifts, 3 general stencil
+  auto kind = [&](int i) -> int {
+    if (i >= ntotal) return -1;
+    const DevInst& S = st[tile_inst[i]];
+    if (S.done) return 0;
+    if (S.planes.srow != nullptr && S.coords == S.pwhich) return S.planes.plus ? 2 : 1;
+    return 3;
+  };
+  auto issue = [&](int i, int k, int stage) {
+    const DevInst& S = st[tile_inst[i]];
+    const DevTile tile = S.tiles[tile_local[i]];
+    const float2* xin = (const float2*)S.V + (long long)S.j * S.ldv;
+    if (k == 2)
+      sep_issue<kSepF4Plus>(S.sectors, tile, xin, S.planes, sep_stage(smem_raw, stage));
+    else
+      sep_issue<kSepF4>(S.sectors, tile, xin, S.planes, sep_stage(smem_raw, stage));
+  };
+  int i = blockIdx.x;
+  int stage = 0;
+  bool staged = false;  // item i's stage was issued by the previous iteration
+  while (i < ntotal) {
+    const int ki = kind(i);
+    if (ki == 0) {
+      i += gridDim.x;
+      continue;
+    }
+    const DevInst& S = st[tile_inst[i]];
+    const DevTile tile = S.tiles[tile_local[i]];
+    const BorderArgs b{S.scale, nullptr, S.coords};
+    const double2* al = S.border ? &S.alpha : nullptr;
+    if (ki == 3) {  // nothing is in flight here: only separable tiles are prefetched
+      float2* win = reinterpret_cast<float2*>(smem_raw);
+      int4* sterms = reinterpret_cast<int4*>(smem_raw + 3 * kWinElems * sizeof(float2));
+      int* ge = reinterpret_cast<int*>(sterms + kMaxSectorTerms);
+      apply_tile<float>(S.sectors, S.terms, (const float2*)S.coefb, tile, (const float2*)S.V + (long long)S.j * S.ldv,
+                        (float2*)S.w, b, al, win, sterms, ge);
+      __syncthreads();  // the windows are restaged by the next item
+      i += gridDim.x;
+      continue;
+    }
+    if (!staged) issue(i, ki, stage);
+    int j = i + gridDim.x;
+    int kj = kind(j);
+    while (kj == 0) {
+      j += gridDim.x;
+      kj = kind(j);
+    }
+    const bool pre = kj == 1 || kj == 2;
+    if (pre) {
+      issue(j, kj, stage ^ 1);
+      cp_async_wait<1>();  // item i's group has landed, item j's stays in flight
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const StoreSink<float2> sink{(float2*)S.w};
+    if (ki == 2)
+      sep_compute<true>(S.sectors, tile, sink, b, al, sep_stage(smem_raw, stage));
+    else
+      sep_compute<false>(S.sectors, tile, sink, b, al, sep_stage(smem_raw, stage));
+    __syncthreads();  // this stage is refilled by the prefetch of the item after j
+    staged = pre;
+    if (pre) stage ^= 1;
+    i = kj < 0 ? ntotal : j;
   }
 }
 
@@ -1616,6 +1698,13 @@ Engine::Engine(int device, int krylovdim, bool f32, bool use_graphs)
   set_smem(k_bapply<double, true>, smem64, err);
   set_smem(k_bapply<double, false>, smem64, err);
   set_smem(k_bapply<float, false>, smem32, err);
+  set_smem(k_bapply_persist, kSepSmemBytes, err);
+  chk(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&persist_max_, k_bapply_persist, kApplyThreads,
+                                                    kSepSmemBytes) != cudaSuccess) {
+    persist_max_ = 0;
+    (void)cudaGetLastError();  // no persistent schedule; the error is not the engine's
+  }
   rec_stride_ = (size_t)(m_ + 5) * (m_ + 2);
 }
 
@@ -1747,7 +1836,106 @@ void Engine::rebuild() {
     cudaGraphExecDestroy(graph_);
     graph_ = nullptr;
   }
+  schedule_chosen_ = false;
   dirty_ = false;
+}
+
+namespace {
+
+// Process-wide schedule setting, choice cache and the record of the last choice.
+std::atomic<int> g_apply_schedule{PI_SCHEDULE_AUTO};
+std::mutex g_schedule_mu;
+std::map<long long, int> g_schedule_cache;  // (device, job-set shape) -> schedule
+pi_schedule_info_t g_schedule_info{};
+
+}  // namespace
+
+void Engine::launch_step_apply(int schedule) {
+  DevInst* st = (DevInst*)st_;
+  const int* ti = (const int*)tile_inst_;
+  const int* tl = (const int*)tile_local_;
+  if (schedule > 0) {
+    const int grid = std::max(1, std::min(total_tiles_, schedule * sm_count_));
+    launch(k_bapply_persist, grid, kApplyThreads, kSepSmemBytes, (const DevInst*)st, ti, tl, total_tiles_);
+  } else {
+    launch(k_bapply<float, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(float2), (const DevInst*)st,
+           ti, tl);
+  }
+}
+
+// Picks the FP32 step-apply schedule of the current job set.  Runs on the engine stream
+// after the cycle's control blocks and first basis columns are on the device and before the
+// cycle's steps are launched or captured: the timed applies write only each running job's
+// step column w, which the first step overwrites.
+void Engine::choose_apply_schedule() {
+  schedule_chosen_ = true;
+  apply_schedule_ = PI_SCHEDULE_PER_TILE;
+  if (!f32_ || total_tiles_ == 0 || persist_max_ < 1 || sm_count_ < 1) return;
+  const int setting = g_apply_schedule.load();
+  bool general = false;
+  for (const DevInst& d : base_) general = general || d.planes.srow == nullptr;
+  int size_class = 0;
+  while ((2LL << size_class) <= total_tiles_) ++size_class;
+  const long long key = ((long long)device_ << 16) | (size_class << 1) | (general ? 1 : 0);
+  pi_schedule_info_t rec{};
+  rec.items = total_tiles_;
+  rec.resident_max = persist_max_;
+  if (setting != PI_SCHEDULE_AUTO) {
+    apply_schedule_ = setting > 0 ? std::min(setting, persist_max_) : PI_SCHEDULE_PER_TILE;
+  } else {
+    bool cached = false;
+    {
+      std::lock_guard<std::mutex> lk(g_schedule_mu);
+      auto it = g_schedule_cache.find(key);
+      if (it != g_schedule_cache.end()) {
+        apply_schedule_ = std::min(it->second, persist_max_);
+        cached = true;
+      }
+    }
+    if (!cached) {
+      std::vector<int> cand{PI_SCHEDULE_PER_TILE};
+      for (int b = 1; b <= std::min(persist_max_, 7); ++b) cand.push_back(b);
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      chk(cudaEventCreate(&e0));
+      chk(cudaEventCreate(&e1));
+      constexpr int kReps = 3;
+      double best = 0;
+      for (size_t c = 0; c < cand.size() && err == cudaSuccess; ++c) {
+        launch_step_apply(cand[c]);  // warm-up
+        float t[kReps];
+        for (int r = 0; r < kReps; ++r) {
+          chk(cudaEventRecord(e0, s_));
+          launch_step_apply(cand[c]);
+          chk(cudaEventRecord(e1, s_));
+          chk(cudaEventSynchronize(e1));
+          t[r] = 0.f;
+          chk(cudaEventElapsedTime(&t[r], e0, e1));
+        }
+        std::sort(t, t + kReps);
+        const double us = 1e3 * t[kReps / 2];
+        rec.cand[rec.ncand] = cand[c];
+        rec.cand_us[rec.ncand] = us;
+        ++rec.ncand;
+        if (c == 0 || us < best) {
+          best = us;
+          apply_schedule_ = cand[c];
+        }
+      }
+      chk(cudaGetLastError());
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+      if (err == cudaSuccess) {
+        std::lock_guard<std::mutex> lk(g_schedule_mu);
+        g_schedule_cache[key] = apply_schedule_;
+        ++g_schedule_info.tunings;
+      }
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_schedule_mu);
+  rec.choices = g_schedule_info.choices + 1;
+  rec.tunings = g_schedule_info.tunings;
+  rec.schedule = apply_schedule_;
+  g_schedule_info = rec;
 }
 
 // Launches a kernel on the engine stream, or appends it as the next node of the graph under
@@ -1790,7 +1978,7 @@ void Engine::arnoldi_step() {
   const int C = total_chunks_;
   if (f32_) {
     if (any_border_) launch(k_step_trace<float2>, n, kRT, 0, st);
-    launch(k_bapply<float, false>, total_tiles_, kApplyThreads, 3 * kWinElems * sizeof(float2), (const DevInst*)st, ti, tl);
+    launch_step_apply(apply_schedule_);
     // CGS with selective reorthogonalisation: the first pass also takes the image norm
     // |w0|^2 (every job) and the first update the |w1|^2 partials (second half of part);
     // the second pass runs only for jobs whose first projection removed more than half of
@@ -1829,6 +2017,8 @@ void Engine::arnoldi_step() {
 }
 
 void Engine::run_cycle_steps() {
+  if (!schedule_chosen_) choose_apply_schedule();
+  if (err != cudaSuccess) return;
   if (!graphs_) {
     for (int j = 0; j < m_; ++j) arnoldi_step();
     return;
@@ -2128,6 +2318,20 @@ int pi_dynamics_batch(int njobs, const pi_dynamics_job_t* specs, const pi_expv_o
     for (Job* j : base) delete j;
   }
   return rc;
+}
+
+int pi_engine_set_apply_schedule(int schedule) {
+  if (schedule < PI_SCHEDULE_PER_TILE || schedule > 64)
+    return fail(PI_ERR_INVALID_ARGUMENT, "schedule must be PI_SCHEDULE_AUTO, PI_SCHEDULE_PER_TILE or 1..64 blocks per SM");
+  g_apply_schedule.store(schedule);
+  return PI_OK;
+}
+
+int pi_engine_schedule_info(pi_schedule_info_t* out) {
+  if (!out) return fail(PI_ERR_INVALID_ARGUMENT, "null output");
+  std::lock_guard<std::mutex> lk(g_schedule_mu);
+  *out = g_schedule_info;
+  return PI_OK;
 }
 
 int pi_steady_state_batch(int ninst, pi_plan* const* plans, double* const* x_devs, const pi_gmres_opts_t* opts,

@@ -317,6 +317,16 @@ class Engine {
   cudaGraphExec_t graph_ = nullptr;
   cudaGraph_t build_ = nullptr;       // graph under construction
   cudaGraphNode_t last_ = nullptr;    // its last node
+  // FP32 step-apply schedule: PI_SCHEDULE_PER_TILE (one block per work item) or the blocks
+  // per SM of the persistent launch; chosen per job set before its first cycle, by the
+  // process-wide setting or by timing the candidates (cached process-wide per device and
+  // job-set shape)
+  void choose_apply_schedule();
+  void launch_step_apply(int schedule);
+  int apply_schedule_ = PI_SCHEDULE_PER_TILE;
+  bool schedule_chosen_ = false;
+  int sm_count_ = 0;
+  int persist_max_ = 0;  // resident blocks per SM of the persistent apply (0: unavailable)
 };
 
 }  // namespace picuda

@@ -774,8 +774,10 @@ static int apply_host(pi_plan* plan, void* y_host, const void* x_host, int ncols
     }
     plan->stage_bytes = bytes;
   }
-  // about 8 chunks, each at least 1 column
-  const int chunk = std::max(1, (ncols + 7) / 8);
+  // about 16 chunks, each at least 1 column: the first upload and the last download overlap
+  // nothing, so smaller chunks shorten them; at 128 columns of N=120, 16 chunks measured 5%
+  // faster than 8 and 32 chunks 6% slower (launch and copy setup per chunk)
+  const int chunk = std::max(1, (ncols + 15) / 16);
   BorderArgs border{1.0, nullptr, coords};
   int k = 0;
   for (int c0 = 0; c0 < ncols && e == cudaSuccess; c0 += chunk, ++k) {

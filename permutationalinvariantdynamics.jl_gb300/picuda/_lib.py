@@ -32,6 +32,8 @@ PI_TERM_COLLECTIVE_JUMP = 2
 PI_FP64 = 0
 PI_FP32 = 1
 PI_COORDS_REFERENCE = 0
+PI_SCHEDULE_AUTO = 0
+PI_SCHEDULE_PER_TILE = -1
 PI_COORDS_POPULATION = 1
 
 
@@ -82,6 +84,11 @@ class pi_precond_info_t(C.Structure):
                 ("regularization", C.c_double), ("chains", C.c_int), ("levels", C.c_int),
                 ("entries", C.c_longlong), ("max_level", C.c_int), ("direction", C.c_int),
                 ("singular", C.c_int), ("device_bytes", C.c_size_t), ("setup_seconds", C.c_double)]
+
+
+class pi_schedule_info_t(C.Structure):
+    _fields_ = [("choices", C.c_int), ("tunings", C.c_int), ("schedule", C.c_int), ("items", C.c_int),
+                ("resident_max", C.c_int), ("ncand", C.c_int), ("cand", C.c_int * 8), ("cand_us", C.c_double * 8)]
 
 
 class pi_precond_tables_t(C.Structure):
@@ -226,6 +233,8 @@ PROTOTYPES = {
     "pi_steady_state_batch": (C.c_int, [C.c_int, C.POINTER(_P), C.POINTER(_P),
                                         C.POINTER(pi_gmres_opts_t),
                                         C.POINTER(pi_gmres_info_t)]),
+    "pi_engine_set_apply_schedule": (C.c_int, [C.c_int]),
+    "pi_engine_schedule_info": (C.c_int, [C.POINTER(pi_schedule_info_t)]),
     "pi_server_default_opts": (None, [C.POINTER(pi_server_opts_t)]),
     "pi_server_create": (C.c_int, [C.POINTER(pi_server_opts_t), C.c_int, C.POINTER(_P)]),
     "pi_server_submit": (C.c_int, [_P, C.POINTER(pi_request_t)]),

@@ -1654,3 +1654,34 @@ def stationary_state_batch(models, algorithm: GMRESAlgorithm | None = None, atol
     if return_info:
         return states, [{f: getattr(i, f) for f, _ in i._fields_} for i in infos]
     return states
+
+
+def set_engine_schedule(schedule="auto"):
+    """Step-apply schedule of the batched FP32 engine (scans, batched solves, FP32 servers):
+    "auto" (timed per job-set shape, the default), "per_tile" (one block per (instance,
+    sector-tile) item) or an int k >= 1 (a persistent launch of k blocks per SM).  Results
+    are bitwise the same for every schedule.  Process-wide."""
+    if schedule == "auto":
+        code = _lib.PI_SCHEDULE_AUTO
+    elif schedule == "per_tile":
+        code = _lib.PI_SCHEDULE_PER_TILE
+    elif isinstance(schedule, int) and not isinstance(schedule, bool) and schedule >= 1:
+        code = schedule
+    else:
+        raise _lib.PiArgumentError(f"engine schedule must be 'auto', 'per_tile' or a positive int, got {schedule!r}")
+    _lib.check(_lib.load().pi_engine_set_apply_schedule(code), "set_engine_schedule")
+
+
+def engine_schedule_info():
+    """The batched engine's last step-apply schedule choice: the schedule ("per_tile" or
+    blocks per SM), the work-list size it was made for, the resident-block limit, and the
+    median time of every candidate when the choice was timed."""
+    info = _lib.pi_schedule_info_t()
+    _lib.check(_lib.load().pi_engine_schedule_info(C.byref(info)), "engine_schedule_info")
+
+    def name(k):
+        return "per_tile" if k == _lib.PI_SCHEDULE_PER_TILE else int(k)
+
+    return {"choices": info.choices, "tunings": info.tunings, "schedule": name(info.schedule),
+            "items": info.items, "resident_max": info.resident_max,
+            "candidates_us": {str(name(info.cand[i])): info.cand_us[i] for i in range(info.ncand)}}
