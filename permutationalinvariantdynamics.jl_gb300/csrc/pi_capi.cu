@@ -774,10 +774,12 @@ static int apply_host(pi_plan* plan, void* y_host, const void* x_host, int ncols
     }
     plan->stage_bytes = bytes;
   }
-  // about 16 chunks, each at least 1 column: the first upload and the last download overlap
-  // nothing, so smaller chunks shorten them; at 128 columns of N=120, 16 chunks measured 5%
-  // faster than 8 and 32 chunks 6% slower (launch and copy setup per chunk)
-  const int chunk = std::max(1, (ncols + 15) / 16);
+  // Chunks of at least 1 column.  The first upload and the last download overlap nothing, so
+  // smaller chunks shorten them, while each chunk adds launch and copy setup.  At 128 columns
+  // of N=120: FP64 (compute-heavy chunks) 16 chunks measured 5% faster than 8 and 32 chunks
+  // 6% slower; FP32 (copy-bound chunks) 8 chunks measured faster than 16 (2.13 vs 2.33 ms).
+  const int nchunks = sizeof(T) == sizeof(double) ? 16 : 8;
+  const int chunk = std::max(1, (ncols + nchunks - 1) / nchunks);
   BorderArgs border{1.0, nullptr, coords};
   int k = 0;
   for (int c0 = 0; c0 < ncols && e == cudaSuccess; c0 += chunk, ++k) {
