@@ -275,9 +275,25 @@ typedef struct {
   int singular;           /* 1: L0 singular, its free entry fixed by the trace */
   size_t device_bytes;
   double setup_seconds;
+  int kind;                 /* PI_PRECOND_LEVEL or PI_PRECOND_DRIVE */
+  double max_asymmetry;     /* drive: largest |H_ab - H_ba| of the sector Hamiltonian blocks */
+  double max_nonhermitian;  /* drive: largest real row-shift coefficient left out */
 } pi_precond_info_t;
+enum { PI_PRECOND_LEVEL = 0, PI_PRECOND_DRIVE = 1 };
 int pi_precond_create(pi_plan* plan, int coords, double regularization, double operator_scale,
                       pi_precond** out);
+/* Drive preconditioner (PI_PRECOND_DRIVE): per Schur sector the normal part of the
+ * within-sector operator, A X + X A^H with A = -i H_s - qbar_s I (H_s the sector's Hamiltonian
+ * block, real symmetric tridiagonal; qbar_s its mean loss), solved exactly in the orthogonal
+ * eigenbasis of H_s (X = U [(U^T R U) ./ d] U^T, d_ij = (-i (h_i - h_j) - 2 qbar_s) / s), with
+ * the trace border v t^H by Sherman-Morrison; FP32 arithmetic, FP64 or FP32 vectors.  It
+ * carries the drive exactly and leaves out the loss variation along a sector, the sandwich
+ * gains and the coupling between sectors, which the level sweep (pi_precond_create) carries
+ * exactly and the drive part leaves out.  As opts.preconditioner GMRES applies it twice per
+ * step (z = D r; z += D (r - B z), B the bordered operator).  The host eigendecompositions run
+ * on the host threads.  The reference's preconditioner for the same system is the dense LU of
+ * every sector block of L/s + v t^H (krylov.jl:594-699), infeasible beyond N ~ 40. */
+int pi_precond_create_drive(pi_plan* plan, int coords, double operator_scale, pi_precond** out);
 int pi_precond_destroy(pi_precond* precond);
 int pi_precond_info(const pi_precond* precond, pi_precond_info_t* out);
 /* z = M^-1 r (complex FP64 device vectors in the preconditioner's coordinates), enqueued on
@@ -311,6 +327,13 @@ int pi_precond_export(int N, int d, int nsectors, const int* sector_ks, int nter
                       const double* ops, const double* rates, const double* hbar, int coords,
                       double regularization, double operator_scale, long long* counts,
                       pi_precond_tables_t* tables);
+/* Host-only inspection of the drive preconditioner's tables for the same model arguments:
+ * counts[0..2] = sectors, sum n_s^2, sum n_s; with U, h, c non-NULL also the eigenvector pool
+ * (sector by sector, n_s x n_s column-major, column i the eigenvector of h[i]), the eigenvalue
+ * pool and c_s = -2 x the mean loss of every sector (all unscaled). */
+int pi_precond_drive_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                            const double* ops, const double* rates, const double* hbar, long long* counts,
+                            double* U, double* h, double* c);
 
 typedef struct {
   int krylovdim;          /* GMRES restart length m (default 30) */
@@ -326,6 +349,12 @@ typedef struct {
                              sectors vanish at large N); x_dev stays in reference coordinates */
   const pi_precond* preconditioner;  /* NULL (default) or a left preconditioner built for the
                              same plan and coordinates; its operator scale is used */
+  const pi_precond* drive_preconditioner;  /* NULL (default), or with a PI_PRECOND_LEVEL
+                             `preconditioner` a PI_PRECOND_DRIVE one of the same plan, coordinates
+                             and scale: the solve starts with the level sweep and moves, after a
+                             restart cycle that reduced the raw residual by less than 3x, to the
+                             drive part applied twice, and after another such cycle to drive,
+                             level and drive in turn (regime-adaptive; no reference counterpart) */
 } pi_gmres_opts_t;
 
 typedef struct {
@@ -339,6 +368,7 @@ typedef struct {
   double trace_error;       /* |t^H x - 1| */
   double operator_scale;
   double linear_residual;
+  int preconditioner_stage; /* with both preconditioners: 0 level, 1 drive x2, 2 drive-level-drive */
 } pi_gmres_info_t;
 
 void pi_gmres_default_opts(pi_gmres_opts_t* opts);

@@ -2200,7 +2200,7 @@ int check_gmres_opts(const pi_gmres_opts_t* o) {
   if (!(o->atol >= 0) || !(o->rtol >= 0)) return fail(PI_ERR_INVALID_ARGUMENT, "tolerances must be nonnegative");
   if (o->precision != PI_FP64 && o->precision != PI_FP32)
     return fail(PI_ERR_INVALID_ARGUMENT, "precision must be PI_FP64 or PI_FP32");
-  if (o->preconditioner != nullptr || o->coords != PI_COORDS_REFERENCE)
+  if (o->preconditioner != nullptr || o->drive_preconditioner != nullptr || o->coords != PI_COORDS_REFERENCE)
     return fail(PI_ERR_UNSUPPORTED,
                 "batched steady states run unpreconditioned in reference coordinates; solve preconditioned or "
                 "population-coordinate steady states with pi_steady_state");

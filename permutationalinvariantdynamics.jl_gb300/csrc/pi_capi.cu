@@ -15,6 +15,7 @@
 #include "pi_batch.hpp"
 #include "pi_handle.hpp"
 #include "pi_precond.hpp"
+#include "pi_drive.hpp"
 
 namespace picuda {
 
@@ -455,6 +456,26 @@ int pi_stencil_export_adjoint(int N, int d, int nsectors, const int* sector_ks, 
   int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
   if (rc) return rc;
   return export_plan(adjoint_host_plan(hp), counts, term_table, coef);
+}
+
+int pi_precond_drive_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
+                            const double* ops, const double* rates, const double* hbar, long long* counts,
+                            double* U, double* h, double* c) {
+  if (!counts) return fail(PI_ERR_INVALID_ARGUMENT, "null counts");
+  QubitPlan hp;
+  int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
+  if (rc) return rc;
+  DriveHost D;
+  std::string err;
+  rc = build_drive_precond(hp, PI_COORDS_REFERENCE, 1.0, &D, &err);
+  if (rc) return fail(rc, err);
+  counts[0] = (long long)D.n.size();
+  counts[1] = (long long)D.U.size();
+  counts[2] = (long long)D.h.size();
+  if (U) std::copy(D.U.begin(), D.U.end(), U);
+  if (h) std::copy(D.h.begin(), D.h.end(), h);
+  if (c) std::copy(D.c.begin(), D.c.end(), c);
+  return PI_OK;
 }
 
 int pi_precond_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,

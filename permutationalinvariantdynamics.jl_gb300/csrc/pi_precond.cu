@@ -61,6 +61,7 @@
 #include "pi_handle.hpp"
 #include "pi_internal.hpp"
 #include "pi_precond.hpp"
+#include "pi_drive.hpp"
 
 namespace picuda {
 
@@ -769,8 +770,10 @@ int build_level_precond(const QubitPlan& hp, int coords, double regularization, 
 
 struct pi_precond {
   pi_plan* plan = nullptr;
-  picuda::LevelPrecondHost host;
+  int kind = PI_PRECOND_LEVEL;
+  picuda::LevelPrecondHost host;  // kind LEVEL: the tables; both kinds: coords and scale
   picuda::PrecondDev dev{};
+  picuda::DriveState* drive = nullptr;  // kind DRIVE
   int fp64 = 0;
   size_t bytes = 0;
   double setup_seconds = 0.0;
@@ -821,6 +824,7 @@ int upload_factors(pi_precond* P) {
 void free_precond(pi_precond* P) {
   if (!P) return;
   for (void* p : P->allocs) cudaFree(p);
+  drive_free(P->drive);
   delete P;
 }
 
@@ -828,6 +832,8 @@ void free_precond(pi_precond* P) {
 
 cudaError_t precond_apply(const pi_precond* P, const void* r, int r_f32, void* z, int z_f32, double scale,
                           cudaStream_t stream) {
+  // the drive state's scratch is written: applications on one plan are serialised by its lock
+  if (P->kind == PI_PRECOND_DRIVE) return drive_apply(P->drive, r, r_f32, z, z_f32, stream);
   const PrecondDev& D = P->dev;
   const int blocks = (int)P->host.chain_order.size();
   if (r_f32 != z_f32) return cudaErrorInvalidValue;
@@ -839,6 +845,7 @@ cudaError_t precond_apply(const pi_precond* P, const void* r, int r_f32, void* z
 }
 
 int precond_coords(const pi_precond* P) { return P->host.coords; }
+int precond_kind(const pi_precond* P) { return P->kind; }
 double precond_scale(const pi_precond* P) { return P->host.scale; }
 const pi_plan* precond_plan(const pi_precond* P) { return P->plan; }
 
@@ -933,6 +940,38 @@ int pi_precond_create(pi_plan* plan, int coords, double regularization, double o
   return PI_OK;
 }
 
+int pi_precond_create_drive(pi_plan* plan, int coords, double operator_scale, pi_precond** out) {
+  if (!plan || !out) return fail(PI_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (coords != PI_COORDS_REFERENCE && coords != PI_COORDS_POPULATION)
+    return fail(PI_ERR_INVALID_ARGUMENT, "coords must be PI_COORDS_REFERENCE or PI_COORDS_POPULATION");
+  if (operator_scale != 0 && !(std::isfinite(operator_scale) && operator_scale > 0))
+    return fail(PI_ERR_INVALID_ARGUMENT, "operator_scale must be finite and positive");
+  double s = operator_scale;
+  if (s == 0) {
+    const int rc = estimate_operator_scale(plan, coords, &s);
+    if (rc) return rc;
+  }
+  BusyGuard guard(plan);
+  if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
+  pi_precond* P = new pi_precond();
+  P->plan = plan;
+  P->kind = PI_PRECOND_DRIVE;
+  P->fp64 = 0;
+  P->host.coords = coords;
+  P->host.scale = s;
+  std::string err;
+  const int rc = drive_create(plan, coords, s, &P->drive, &err);
+  if (rc) {
+    delete P;
+    return fail(rc, err);
+  }
+  P->bytes = drive_bytes(P->drive);
+  P->setup_seconds = drive_setup_seconds(P->drive);
+  *out = P;
+  return PI_OK;
+}
+
 int pi_precond_destroy(pi_precond* P) {
   free_precond(P);
   return PI_OK;
@@ -953,6 +992,16 @@ int pi_precond_info(const pi_precond* P, pi_precond_info_t* out) {
   out->singular = H.mode == 0 ? 1 : 0;
   out->device_bytes = P->bytes;
   out->setup_seconds = P->setup_seconds;
+  out->kind = P->kind;
+  out->max_asymmetry = 0.0;
+  out->max_nonhermitian = 0.0;
+  if (P->kind == PI_PRECOND_DRIVE) {
+    const DriveHost& D = drive_host(P->drive);
+    out->chains = out->levels = out->max_level = out->direction = out->singular = 0;
+    out->entries = P->plan->host.dim;
+    out->max_asymmetry = D.max_asymmetry;
+    out->max_nonhermitian = D.max_nonhermitian;
+  }
   return PI_OK;
 }
 

@@ -74,6 +74,7 @@ int build_level_precond(const QubitPlan& hp, int coords, double regularization, 
 cudaError_t precond_apply(const pi_precond* P, const void* r, int r_f32, void* z, int z_f32, double scale,
                           cudaStream_t stream);
 int precond_coords(const pi_precond* P);
+int precond_kind(const pi_precond* P);  // PI_PRECOND_LEVEL or PI_PRECOND_DRIVE
 double precond_scale(const pi_precond* P);
 const pi_plan* precond_plan(const pi_precond* P);
 

@@ -90,10 +90,37 @@ struct Run {
     chk(launch_apply_f32(p->dev, (const float*)x, (float*)y, 1, n, b, s));
     ++applications;
   }
-  // z = P r (left preconditioner of the bordered system); FP64 or FP32 in and out
-  void precondition(const pi_precond* P, const void* r, void* z, int f32) {
-    chk(precond_apply(P, r, f32, z, f32, precond_scale(P), s));
+  // Left preconditioning of the bordered system B = L/s + v t^H.  Stage 0 applies `level`
+  // (or the only preconditioner); stage 1 the drive part twice, z = D r, z += D (r - B z);
+  // stage 2 drive, level and drive in turn, each on the current residual r - B z.  FP64 or
+  // FP32 in and out; the extra bordered applies count as operator applications.
+  double invscale = 1.0;
+  double2* palpha = nullptr;        // border scalar of the extra applies
+  void* pscr[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // [f32][0..1]: n-vectors
+  void bapply(const void* x, void* y, int f32) {
+    if (f32)
+      apply_bordered_f32((const float2*)x, (float2*)y, invscale, palpha);
+    else
+      apply_bordered((const double2*)x, (double2*)y, invscale, palpha);
   }
+  // z += M (r - B z) for one preconditioner M
+  void correct(const pi_precond* M, const void* r, void* z, int f32) {
+    void* t = pscr[f32][0];
+    void* u = pscr[f32][1];
+    bapply(z, t, f32);
+    chk(axpby(r, t, t, f32, 1.0, -1.0));  // t = r - B z
+    chk(precond_apply(M, t, f32, u, f32, precond_scale(M), s));
+    chk(axpby(z, u, z, f32, 1.0, 1.0));   // z += u
+  }
+  void precondition(const pi_precond* level, const pi_precond* drive, int stage, const void* r, void* z, int f32) {
+    const pi_precond* first = stage == 0 ? (level ? level : drive) : drive;
+    chk(precond_apply(first, r, f32, z, f32, precond_scale(first), s));
+    if (stage == 0 && (level || precond_kind(first) == PI_PRECOND_LEVEL)) return;
+    if (stage == 2) correct(level, r, z, f32);
+    correct(drive, r, z, f32);
+  }
+  // out = a x + b y elementwise (n complex entries, FP64 or FP32)
+  cudaError_t axpby(const void* x, const void* y, void* out, int f32, double a, double b);
   cd trace(const double2* x) {
     double2* out = p->rs.result;
     chk(trace_dot(p->dev, x, 0, coords, out, s));
@@ -124,6 +151,24 @@ __global__ void k_sub(const double2* __restrict__ b, const double2* __restrict__
 inline int grid_n(long long n) {
   long long g = (n + 255) / 256;
   return (int)std::max(1LL, std::min(g, 4LL * 152));
+}
+
+template <typename T2>
+__global__ void k_axpby(const T2* __restrict__ x, const T2* __restrict__ y, T2* __restrict__ out, double a, double b,
+                        long long n) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const T2 u = x[e], v = y[e];
+    out[e].x = a * u.x + b * v.x;
+    out[e].y = a * u.y + b * v.y;
+  }
+}
+
+cudaError_t Run::axpby(const void* x, const void* y, void* out, int f32, double a, double b) {
+  if (f32)
+    k_axpby<float2><<<grid_n(n), 256, 0, s>>>((const float2*)x, (const float2*)y, (float2*)out, a, b, n);
+  else
+    k_axpby<double2><<<grid_n(n), 256, 0, s>>>((const double2*)x, (const double2*)y, (double2*)out, a, b, n);
+  return cudaGetLastError();
 }
 
 // One CGS2 orthogonalisation of w against V[0..nv) (FP64): H column += h1 + h2 and
@@ -226,9 +271,13 @@ double estimate_scale(Run& R, double2* probe, double2* image) {
 // P A, the preconditioned residual |P r| tested against atol + rtol |P b| and the raw residual
 // |r| against atol + rtol |b|, both after every restart (krylov.jl:737-786).
 GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, double rtol, int maxiter,
-                      double invscale, DeviceBuffers& buf, const pi_precond* P) {
+                      double invscale, DeviceBuffers& buf, const pi_precond* Plev, const pi_precond* Pdrv,
+                      int* stage_out) {
   GmresResult res;
   const long long n = R.n;
+  const pi_precond* P = Plev ? Plev : Pdrv;
+  const bool ladder = Plev && Pdrv;
+  int stage = 0;
   double2* V = (double2*)buf.get(sizeof(double2) * n * (m + 1));
   double2* w = (double2*)buf.get(sizeof(double2) * n);
   double2* r = (double2*)buf.get(sizeof(double2) * n);
@@ -236,36 +285,45 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
   double2* hd = (double2*)buf.get(sizeof(double2) * 2 * kMaxDots);
   double2* alpha = (double2*)buf.get(sizeof(double2) * 4);
   double2* yd = (double2*)buf.get(sizeof(double2) * kMaxDots);
-  if (!V || !w || !r || !hd || !alpha || !yd || (P && !pz)) {
+  if (Pdrv) {
+    R.pscr[0][0] = buf.get(sizeof(double2) * n);
+    R.pscr[0][1] = buf.get(sizeof(double2) * n);
+  }
+  if (!V || !w || !r || !hd || !alpha || !yd || (P && !pz) || (Pdrv && (!R.pscr[0][0] || !R.pscr[0][1]))) {
     R.chk(buf.err);
     return res;
   }
+  R.invscale = invscale;
+  R.palpha = alpha + 2;
+  auto prec = [&](const void* in, void* out) { R.precondition(Plev, Pdrv, stage, in, out, 0); };
   double2* h1d = hd;
   double2* h2d = hd + kMaxDots;
   const double raw_bnorm = R.norm(b);
   const double rawtol = atol + rtol * raw_bnorm;
   double bnorm = raw_bnorm;
   if (P) {
-    R.precondition(P, b, pz, 0);
+    prec(b, pz);
     bnorm = R.norm(pz);
   }
-  const double tol = atol + rtol * bnorm;
+  double tol = atol + rtol * bnorm;
   // residual of the current x: r = b - A x, its raw and (preconditioned) norms
   auto residual = [&](double* rawbeta) {
     R.apply_bordered(x, w, invscale, alpha);
     R.chk((k_sub<<<grid_n(n), 256, 0, R.s>>>(b, w, r, n), cudaGetLastError()));
     *rawbeta = R.norm(r);
     if (!P) return *rawbeta;
-    R.precondition(P, r, pz, 0);
+    prec(r, pz);
     return R.norm(pz);
   };
   double rawbeta = 0.0;
   double beta = residual(&rawbeta);
   res.residual = beta;
+  *stage_out = stage;
   if (beta <= tol && rawbeta <= rawtol) {
     res.converged = true;
     return res;
   }
+  double prev_raw = rawbeta;
   std::vector<std::vector<cd>> H(m, std::vector<cd>(m + 1));  // H[j] = column j
   std::vector<cd> g(m + 1), sn(m), y;
   std::vector<double> cs(m);
@@ -280,7 +338,7 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
       R.apply_bordered(V + (long long)j * n, w, invscale, alpha);
       double2* q = w;
       if (P) {
-        R.precondition(P, w, pz, 0);
+        prec(w, pz);
         q = pz;
       }
       double rem2 = 0.0;
@@ -319,6 +377,19 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
       res.converged = true;
       return res;
     }
+    if (ladder && stage < 2 && rawbeta > prev_raw / 3.0) {
+      // the cycle reduced the raw residual by less than 3x: the next preconditioner stage,
+      // with the preconditioned tests rescaled to it
+      ++stage;
+      *stage_out = stage;
+      prec(b, pz);
+      bnorm = R.norm(pz);
+      tol = atol + rtol * bnorm;
+      prec(r, pz);
+      beta = R.norm(pz);
+      res.residual = beta;
+    }
+    prev_raw = rawbeta;
   }
   return res;
 }
@@ -331,9 +402,12 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
 // |r| <= atol + rtol |b|, with P r and r in FP64.
 GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol, double rtol, int maxiter,
                         int max_refinements, double invscale, DeviceBuffers& buf, int* refinements,
-                        const pi_precond* P) {
+                        const pi_precond* Plev, const pi_precond* Pdrv, int* stage_out) {
   GmresResult res;
   const long long n = R.n;
+  const pi_precond* P = Plev ? Plev : Pdrv;
+  const bool ladder = Plev && Pdrv;
+  int stage = 0;
   float2* V = (float2*)buf.get(sizeof(float2) * n * (m + 1));
   float2* w = (float2*)buf.get(sizeof(float2) * n);
   float2* pw = P ? (float2*)buf.get(sizeof(float2) * n) : nullptr;
@@ -343,20 +417,32 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
   double2* hd = (double2*)buf.get(sizeof(double2) * 2 * kMaxDots);
   double2* alpha = (double2*)buf.get(sizeof(double2) * 4);
   double2* yd = (double2*)buf.get(sizeof(double2) * kMaxDots);
-  if (!V || !w || !w64 || !r || !hd || !alpha || !yd || (P && (!pw || !pz))) {
+  if (Pdrv) {
+    for (int k = 0; k < 2; ++k) {
+      R.pscr[0][k] = buf.get(sizeof(double2) * n);
+      R.pscr[1][k] = buf.get(sizeof(float2) * n);
+    }
+  }
+  if (!V || !w || !w64 || !r || !hd || !alpha || !yd || (P && (!pw || !pz)) ||
+      (Pdrv && (!R.pscr[0][0] || !R.pscr[0][1] || !R.pscr[1][0] || !R.pscr[1][1]))) {
     R.chk(buf.err);
     return res;
   }
+  R.invscale = invscale;
+  R.palpha = alpha + 2;
+  auto prec = [&](const void* in, void* out, int f32) { R.precondition(Plev, Pdrv, stage, in, out, f32); };
   double2* h1d = hd;
   double2* h2d = hd + kMaxDots;
   const double raw_bnorm = R.norm(b);
   const double rawtol = atol + rtol * raw_bnorm;
   double bnorm = raw_bnorm;
   if (P) {
-    R.precondition(P, b, pz, 0);
+    prec(b, pz, 0);
     bnorm = R.norm(pz);
   }
-  const double tol = atol + rtol * bnorm;
+  double tol = atol + rtol * bnorm;
+  double prev_raw = -1.0;
+  *stage_out = stage;
   // Inner solves stop at this relative reduction: FP32 applies cannot resolve the
   // correction much below it, and the FP64 outer residual restores the rest.
   const double inner_rtol = 1e-5;
@@ -368,9 +454,19 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
     R.apply_bordered(x, w64, invscale, alpha);
     R.chk((k_sub<<<grid_n(n), 256, 0, R.s>>>(b, w64, r, n), cudaGetLastError()));
     const double rawbeta = R.norm(r);
+    if (ladder && stage < 2 && prev_raw > 0 && rawbeta > prev_raw / 3.0) {
+      // the last refinement cycle reduced the raw residual by less than 3x: the next
+      // preconditioner stage, with the preconditioned tests rescaled to it
+      ++stage;
+      *stage_out = stage;
+      prec(b, pz, 0);
+      bnorm = R.norm(pz);
+      tol = atol + rtol * bnorm;
+    }
+    prev_raw = rawbeta;
     double beta = rawbeta;
     if (P) {
-      R.precondition(P, r, pz, 0);
+      prec(r, pz, 0);
       beta = R.norm(pz);
     }
     res.residual = beta;
@@ -391,7 +487,7 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
       R.apply_bordered_f32(V + (long long)j * n, w, invscale, alpha);
       float2* q = w;
       if (P) {
-        R.precondition(P, w, pw, 1);
+        prec(w, pw, 1);
         q = pw;
       }
       double rem2 = 0.0;
@@ -467,6 +563,7 @@ void pi_gmres_default_opts(pi_gmres_opts_t* o) {
   o->max_refinements = 200;
   o->coords = PI_COORDS_REFERENCE;
   o->preconditioner = nullptr;
+  o->drive_preconditioner = nullptr;
 }
 
 int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, pi_gmres_info_t* info) {
@@ -489,6 +586,19 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
     if (opts->operator_scale > 0 && std::abs(opts->operator_scale - ps) > std::sqrt(2.2e-16) * ps)
       return fail(PI_ERR_INVALID_ARGUMENT, "operator_scale is inconsistent with the prepared preconditioner");
   }
+  const pi_precond* Pd = opts->drive_preconditioner;
+  if (Pd) {
+    if (!P || precond_kind(P) != PI_PRECOND_LEVEL || precond_kind(Pd) != PI_PRECOND_DRIVE)
+      return fail(PI_ERR_INVALID_ARGUMENT,
+                  "drive_preconditioner needs a PI_PRECOND_DRIVE preconditioner beside a PI_PRECOND_LEVEL one");
+    if (precond_plan(Pd) != plan || precond_coords(Pd) != opts->coords)
+      return fail(PI_ERR_INVALID_ARGUMENT, "the drive preconditioner was built for another model or coordinates");
+    const double ps = precond_scale(P);
+    if (std::abs(precond_scale(Pd) - ps) > std::sqrt(2.2e-16) * ps)
+      return fail(PI_ERR_INVALID_ARGUMENT, "the two preconditioners were built for different operator scales");
+  }
+  const pi_precond* Plev = P && precond_kind(P) == PI_PRECOND_LEVEL ? P : nullptr;
+  const pi_precond* Pdrv = P && precond_kind(P) == PI_PRECOND_DRIVE ? P : Pd;
   BusyGuard guard(plan);
   if (!guard.ok) return fail(PI_ERR_BUSY, "a pi_plan cannot be used concurrently");
   if (opts->krylovdim <= kBatchMaxKrylov && !P && opts->coords == PI_COORDS_REFERENCE) {
@@ -532,12 +642,13 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
                   "unique trace-fixed Krylov solve");
     GmresResult gr;
     int refinements = 0;
+    int stage = 0;
     try {
       if (opts->precision == PI_FP64)
-        gr = gmres_f64(R, x, v, m, opts->atol, opts->rtol, opts->maxiter, 1.0 / s, buf, P);
+        gr = gmres_f64(R, x, v, m, opts->atol, opts->rtol, opts->maxiter, 1.0 / s, buf, Plev, Pdrv, &stage);
       else
         gr = gmres_mixed(R, x, v, m, opts->atol, opts->rtol, opts->maxiter, std::max(1, opts->max_refinements),
-                         1.0 / s, buf, &refinements, P);
+                         1.0 / s, buf, &refinements, Plev, Pdrv, &stage);
     } catch (const std::exception& ex) {
       return fail(PI_ERR_NOT_CONVERGED, ex.what());
     }
@@ -563,6 +674,7 @@ int pi_steady_state(pi_plan* plan, double* x_dev, const pi_gmres_opts_t* opts, p
     loc.trace_error = terr;
     loc.operator_scale = s;
     loc.linear_residual = gr.residual;
+    loc.preconditioner_stage = stage;
     if (!loc.converged) {
       char msg[256];
       std::snprintf(msg, sizeof(msg),

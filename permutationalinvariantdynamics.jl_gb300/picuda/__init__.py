@@ -7,7 +7,7 @@ libpicuda.so (include/picuda.h), whose sm_103a kernels do all numerical work.
 from ._lib import (PI_FP32, PI_FP64, PiArgumentError, PiBusy, PiDimensionMismatch, PiError, PiNotConverged,
                    load as load_library)
 from .backend import (AcceleratorCapability, CompiledPIModel, DynamicsResult, DynamicsStreamResult,
-                      ExpvAlgorithm, GMRESAlgorithm, HarmonicArnoldiAlgorithm, LevelPreconditioner, level_preconditioner, level_preconditioner_tables, SteadyStateResult, accelerator_capability, apply_, apply_adjoint_, apply_element_major_, element_major_tuning, select_element_major_kernel,
+                      DrivePreconditioner, ExpvAlgorithm, GMRESAlgorithm, HarmonicArnoldiAlgorithm, LevelPreconditioner, drive_preconditioner, drive_preconditioner_tables, level_preconditioner, level_preconditioner_tables, SteadyStateResult, accelerator_capability, apply_, apply_adjoint_, apply_element_major_, element_major_tuning, select_element_major_kernel,
                       compile, engine_schedule_info, evolve_, krylov_expv, krylov_expv_batch, krylov_liouvillian_spectrum, harmonic_arnoldi_spectrum, implicitly_restarted_arnoldi_spectrum, liouvillian_spectrum, pi_liouvillian_gap, SpectrumResult, mul, saved_times, solve_dynamics,
                       solve_dynamics_batch, stationary_state, stationary_state_batch, steady_state,
                       set_engine_schedule, stencil_tables, time_evolve)

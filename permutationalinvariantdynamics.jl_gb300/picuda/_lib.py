@@ -33,6 +33,8 @@ PI_FP64 = 0
 PI_FP32 = 1
 PI_COORDS_REFERENCE = 0
 PI_SCHEDULE_AUTO = 0
+PI_PRECOND_LEVEL = 0
+PI_PRECOND_DRIVE = 1
 PI_SCHEDULE_PER_TILE = -1
 PI_COORDS_POPULATION = 1
 
@@ -76,14 +78,15 @@ class pi_gmres_opts_t(C.Structure):
     _fields_ = [("krylovdim", C.c_int), ("maxiter", C.c_int), ("atol", C.c_double),
                 ("rtol", C.c_double), ("operator_scale", C.c_double), ("precision", C.c_int),
                 ("use_initial", C.c_int), ("max_refinements", C.c_int), ("coords", C.c_int),
-                ("preconditioner", C.c_void_p)]
+                ("preconditioner", C.c_void_p), ("drive_preconditioner", C.c_void_p)]
 
 
 class pi_precond_info_t(C.Structure):
     _fields_ = [("coords", C.c_int), ("fp64", C.c_int), ("operator_scale", C.c_double),
                 ("regularization", C.c_double), ("chains", C.c_int), ("levels", C.c_int),
                 ("entries", C.c_longlong), ("max_level", C.c_int), ("direction", C.c_int),
-                ("singular", C.c_int), ("device_bytes", C.c_size_t), ("setup_seconds", C.c_double)]
+                ("singular", C.c_int), ("device_bytes", C.c_size_t), ("setup_seconds", C.c_double),
+                ("kind", C.c_int), ("max_asymmetry", C.c_double), ("max_nonhermitian", C.c_double)]
 
 
 class pi_schedule_info_t(C.Structure):
@@ -104,7 +107,7 @@ class pi_gmres_info_t(C.Structure):
                 ("refinements", C.c_int), ("operator_applications", C.c_int),
                 ("residual", C.c_double), ("normalized_residual", C.c_double),
                 ("trace_error", C.c_double), ("operator_scale", C.c_double),
-                ("linear_residual", C.c_double)]
+                ("linear_residual", C.c_double), ("preconditioner_stage", C.c_int)]
 
 
 class pi_expv_opts_t(C.Structure):
@@ -206,6 +209,8 @@ PROTOTYPES = {
     "pi_gmres_default_opts": (None, [C.POINTER(pi_gmres_opts_t)]),
     "pi_steady_state": (C.c_int, [_P, _P, C.POINTER(pi_gmres_opts_t), C.POINTER(pi_gmres_info_t)]),
     "pi_precond_create": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.POINTER(_P)]),
+    "pi_precond_create_drive": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(_P)]),
+    "pi_precond_drive_export": (C.c_int, [C.c_int, C.c_int, C.c_int, _I, C.c_int, _I, _D, _D, _D, _LL, _D, _D, _D]),
     "pi_precond_destroy": (C.c_int, [_P]),
     "pi_precond_info": (C.c_int, [_P, C.POINTER(pi_precond_info_t)]),
     "pi_precond_apply": (C.c_int, [_P, _P, _P, _P]),

@@ -1033,6 +1033,7 @@ class GMRESAlgorithm:
     maxiter: int = 500
     preconditioner: object = None
     precision: str = "fp64"
+    drive_preconditioner: object = None
 
     def __post_init__(self):
         if isinstance(self.krylovdim, bool) or self.krylovdim < 1:
@@ -1041,7 +1042,14 @@ class GMRESAlgorithm:
             raise PiArgumentError("maxiter must be at least 1")
         if self.preconditioner is not None and not isinstance(self.preconditioner, LevelPreconditioner):
             raise PiArgumentError("the CUDA backend takes a LevelPreconditioner (level_preconditioner(compiled)) "
-                                  "as the GMRES preconditioner")
+                                  "or a DrivePreconditioner (drive_preconditioner(compiled)) as the GMRES "
+                                  "preconditioner")
+        if self.drive_preconditioner is not None:
+            if not isinstance(self.drive_preconditioner, DrivePreconditioner):
+                raise PiArgumentError("drive_preconditioner must be a DrivePreconditioner")
+            if self.preconditioner is None or isinstance(self.preconditioner, DrivePreconditioner):
+                raise PiArgumentError("drive_preconditioner goes beside a level preconditioner "
+                                      "(preconditioner=level_preconditioner(compiled))")
         if self.precision not in ("fp64", "mixed"):
             raise PiArgumentError("precision must be 'fp64' or 'mixed'")
 
@@ -1220,6 +1228,63 @@ def level_preconditioner(compiled, coords="population", regularization=0.0, oper
     return LevelPreconditioner(compiled, coords=coords, regularization=regularization, operator_scale=operator_scale)
 
 
+class DrivePreconditioner(LevelPreconditioner):
+    """The drive part of the trace-fixed steady-state operator (pi_precond_create_drive): per
+    Schur sector A X + X A^H with A = -i H_s - qbar_s I (the sector's Hamiltonian block and its
+    mean loss), solved exactly in the orthogonal eigenbasis of H_s, plus the trace border by
+    Sherman-Morrison; FP32 arithmetic.  It carries the drive (Jx, Jy), which the level sweep
+    leaves out, and leaves out the loss variation along a sector and the gains, which the level
+    sweep carries.  As the GMRES preconditioner it is applied twice per step; beside a level
+    preconditioner (GMRESAlgorithm(preconditioner=level, drive_preconditioner=drive)) the solve
+    moves from the level sweep to it, and then to both in turn, when a restart cycle makes
+    little progress.  No counterpart in the reference, whose Schur-sector preconditioner
+    LU-factors every sector block densely (krylov.jl:594-700)."""
+
+    def __init__(self, compiled, coords="population", operator_scale=None):
+        if coords not in _COORDS:
+            raise PiArgumentError("coords must be 'reference' or 'population'")
+        self.compiled = _as_compiled(compiled)
+        self.coords = coords
+        handle = C.c_void_p()
+        _lib.check(_lib.load().pi_precond_create_drive(self.compiled.handle, _COORDS[coords],
+                                                       float(operator_scale) if operator_scale else 0.0,
+                                                       C.byref(handle)), "drive_preconditioner")
+        self._handle = handle
+        info = _lib.pi_precond_info_t()
+        _lib.check(_lib.load().pi_precond_info(handle, C.byref(info)), "pi_precond_info")
+        self.info = {f: getattr(info, f) for f, _ in info._fields_}
+
+
+def drive_preconditioner(compiled, coords="population", operator_scale=None):
+    """Builds a DrivePreconditioner for a compiled model (see its docstring); pass the level
+    preconditioner's operator_scale to use both in one solve."""
+    return DrivePreconditioner(compiled, coords=coords, operator_scale=operator_scale)
+
+
+def drive_preconditioner_tables(model):
+    """Host-only export of the drive preconditioner's eigen tables (pi_precond_drive_export)
+    for a PIModel: per sector the eigenvector matrix U (n x n, column i for h[i]), the
+    eigenvalues h of the sector Hamiltonian block and c = -2 x the sector's mean loss."""
+    lib = _lib.load()
+    kinds, ops, rates, hbar, ks = _term_arrays(model)
+    counts = np.zeros(3, dtype=np.int64)
+    args = (model.basis.N, model.basis.d, len(ks), _lib.iptr(ks), len(model.terms), _lib.iptr(kinds),
+            _lib.dptr(ops), _lib.dptr(rates), _lib.dptr(hbar), _lib.llptr(counts))
+    _lib.check(lib.pi_precond_drive_export(*args, None, None, None), "pi_precond_drive_export")
+    S, nu, nh = (int(v) for v in counts)
+    U, h, c = np.zeros(nu), np.zeros(nh), np.zeros(S)
+    _lib.check(lib.pi_precond_drive_export(*args, _lib.dptr(U), _lib.dptr(h), _lib.dptr(c)),
+               "pi_precond_drive_export")
+    out, uo, ho = [], 0, 0
+    for n in model.basis.dims:
+        out.append(dict(U=U[uo:uo + n * n].reshape((n, n), order="F"), h=h[ho:ho + n]))
+        uo += n * n
+        ho += n
+    for d, cs in zip(out, c):
+        d["c"] = float(cs)
+    return out
+
+
 def level_preconditioner_tables(model, coords="population", regularization=0.0, operator_scale=1.0):
     """Host-only export of the preconditioner tables (pi_precond_export) for a PIModel: a
     dict of numpy arrays; no device needed."""
@@ -1281,6 +1346,11 @@ def stationary_state(x, algorithm=None, return_info=False, atol=1e-10, rtol=1e-8
     o.max_refinements = max_refinements
     o.coords = _COORDS[coords]
     o.preconditioner = P.handle if P is not None else None
+    Pd = algorithm.drive_preconditioner
+    if Pd is not None:
+        if Pd.compiled is not compiled or Pd.coords != coords:
+            raise PiArgumentError("the drive preconditioner was built for another compiled model or coordinates")
+        o.drive_preconditioner = Pd.handle
     xd = torch.zeros(n, dtype=torch.complex128, device="cuda")
     if initial_state is not None:
         init = initial_state.data if isinstance(initial_state, PIState) else np.asarray(initial_state)
@@ -1298,7 +1368,8 @@ def stationary_state(x, algorithm=None, return_info=False, atol=1e-10, rtol=1e-8
     d = {f: getattr(info, f) for f, _ in info._fields_}
     d.update(method="krylov", krylov_dimension=algorithm.krylovdim, precision=algorithm.precision,
              state=rho.data, coords=coords, preconditioned=P is not None,
-             preconditioner="LevelPreconditioner" if P is not None else None)
+             preconditioner=type(P).__name__ if P is not None else None,
+             drive_preconditioner=Pd is not None)
     return SteadyStateResult(rho, d, algorithm)
 
 
