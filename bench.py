@@ -238,11 +238,14 @@ def request_stream(count, seed=0, nmin=10, nmax=300, steady_fraction=0.3):
     return reqs
 
 
-def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9, precisions=("fp64", "mixed")):
+def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9, precisions=("fp64", "mixed"),
+                steady_solvers=4):
     """Continuous-batching server on a Poisson request stream at `rate` req/s (the lowest
     rate of the served configuration; the stream saturates the GPU): p50/p99 latency
     (finish - submit) and completed solves/s, FP64 vs mixed, same requests and arrival
-    times.  Plans are built before the clock starts."""
+    times.  Plans are built before the clock starts.  steady_solvers > 0 solves the steady
+    requests preconditioned on that many solver threads beside the batched engine (level
+    sweep and drive part, adaptive); 0 runs them unpreconditioned in the engine."""
     reqs = request_stream(count, seed)
     sm = picuda.spin_matrices(2)
     rng = np.random.default_rng(seed + 1)
@@ -253,10 +256,10 @@ def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9, precis
     out = {"requests": count, "rate_per_s": rate, "memory_budget_bytes": budget,
            "dynamics": sum(1 for r in reqs if r["kind"] == "dynamics"),
            "steady": sum(1 for r in reqs if r["kind"] == "steady"),
-           "max_dim": int(max(len(m.basis) for m in models))}
+           "max_dim": int(max(len(m.basis) for m in models)), "steady_solvers": steady_solvers}
     states, finals = {}, {}
     for prec in precisions:
-        with picuda.Server(precision=prec, memory_budget=budget) as srv:
+        with picuda.Server(precision=prec, memory_budget=budget, steady_solvers=steady_solvers) as srv:
             t0 = time.perf_counter()
             done = []
             for i, r in enumerate(reqs):
@@ -301,12 +304,17 @@ def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9, precis
     out["mixed_max_Jz_per_N_dev_vs_fp64"] = jdev
     out["requests_compared"] = kept
     for kind in ("steady",):
+        # compared in population coordinates z = sqrt(f) x, the coordinates of the solves'
+        # residual tests: at large N the reference coordinates of the high-multiplicity
+        # sectors vanish and the max-norm would weigh only negligible populations
         dev, worst = 0.0, None
         for tag, ref in states["fp64"].items():
             got = states["mixed"].get(tag)
             if got is None or reqs[tag - 1]["kind"] != kind:
                 continue
-            d = float(np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300))
+            sq = np.concatenate([np.full(n * n, f) for n, f in zip(comp[tag - 1].basis.dims,
+                                                                     comp[tag - 1].sector_scales())])
+            d = float(np.abs(sq * (got - ref)).max() / max(np.abs(sq * ref).max(), 1e-300))
             if d >= dev:
                 dev, worst = d, tag
         out[f"mixed_max_state_rel_dev_vs_fp64_{kind}"] = dev
@@ -317,14 +325,15 @@ def serve_rates(picuda, torch, count=24, rate=50.0, seed=0, budget=160e9, precis
     return out
 
 
-def serve_sweep(picuda, torch, rates, count, fp64_rates=1):
+def serve_sweep(picuda, torch, rates, count, fp64_rates=1, steady_solvers=4):
     """The served configuration's rate sweep: `count` requests per rate, mixed precision at
     every rate, plain FP64 at the first `fp64_rates` rates (the FP64 server needs minutes per
     rate at this size)."""
-    out = {"requests_per_rate": count, "rates": list(rates), "per_rate": {}}
+    out = {"requests_per_rate": count, "rates": list(rates), "per_rate": {}, "steady_solvers": steady_solvers}
     for i, rate in enumerate(rates):
         precs = ("fp64", "mixed") if i < fp64_rates else ("mixed",)
-        out["per_rate"][str(rate)] = serve_rates(picuda, torch, count, rate, precisions=precs)
+        out["per_rate"][str(rate)] = serve_rates(picuda, torch, count, rate, precisions=precs,
+                                                 steady_solvers=steady_solvers)
     return out
 
 
@@ -755,6 +764,10 @@ def main():
     ap.add_argument("--engine-schedule", default="auto",
                     help="FP32 engine step-apply schedule: auto, per_tile or blocks per SM (an int)")
     ap.add_argument("--serve-requests", type=int, default=24)
+    ap.add_argument("--serve-steady-solvers", type=int, default=4,
+                    help="preconditioned steady-state solver threads of the served sections (0: in the engine)")
+    ap.add_argument("--serve-fp64-rates", type=int, default=1,
+                    help="rates of the sweep that also run the plain FP64 server")
     ap.add_argument("--serve-sweep", default=None,
                     help="comma-separated request rates: run only the served rate sweep (e.g. 50,200,1000,2000)")
     ap.add_argument("--only-steady", action="store_true", help="run only the steady-state rate section")
@@ -808,10 +821,13 @@ def main():
         return 0
     if args.serve_sweep:
         rates = [float(v) for v in args.serve_sweep.split(",")]
-        print(json.dumps({"serve_sweep": serve_sweep(picuda, torch, rates, args.serve_requests)}))
+        print(json.dumps({"serve_sweep": serve_sweep(picuda, torch, rates, args.serve_requests,
+                                                     fp64_rates=args.serve_fp64_rates,
+                                                     steady_solvers=args.serve_steady_solvers)}))
         return 0
     if args.only_serve:
-        print(json.dumps({"only_serve": True, "serve": serve_rates(picuda, torch, args.serve_requests)}))
+        print(json.dumps({"only_serve": True, "serve": serve_rates(picuda, torch, args.serve_requests,
+                                                                   steady_solvers=args.serve_steady_solvers)}))
         return 0
     if args.only_expv:
         # two saved intervals of dt = 0.05 (expv m = 30), Jz and J+J- streamed
@@ -935,7 +951,8 @@ def main():
 
     solves = solve_rates(picuda, torch) if rank == 0 else None
     scan = scan_rates(picuda, torch, args.scan_instances, args.scan_intervals) if rank == 0 else None
-    serve = serve_rates(picuda, torch, args.serve_requests) if rank == 0 else None
+    serve = serve_rates(picuda, torch, args.serve_requests,
+                        steady_solvers=args.serve_steady_solvers) if rank == 0 else None
     steady = steady_rates(picuda, torch, args.steady_requests) if rank == 0 else None
     steady_served = (steady_rates(picuda, torch, args.steady_requests, family="served")
                      if rank == 0 else None)

@@ -286,7 +286,8 @@ int pi_precond_create(pi_plan* plan, int coords, double regularization, double o
  * within-sector operator, A X + X A^H with A = -i H_s - qbar_s I (H_s the sector's Hamiltonian
  * block, real symmetric tridiagonal; qbar_s its mean loss), solved exactly in the orthogonal
  * eigenbasis of H_s (X = U [(U^T R U) ./ d] U^T, d_ij = (-i (h_i - h_j) - 2 qbar_s) / s), with
- * the trace border v t^H by Sherman-Morrison; FP32 arithmetic, FP64 or FP32 vectors.  It
+ * the trace border v t^H by Sherman-Morrison; FP64 vectors in FP64 arithmetic (the plain
+ * FP64 solve), FP32 vectors in FP32 (the mixed solve's inner steps).  It
  * carries the drive exactly and leaves out the loss variation along a sector, the sandwich
  * gains and the coupling between sectors, which the level sweep (pi_precond_create) carries
  * exactly and the drive part leaves out.  As opts.preconditioner GMRES applies it twice per
@@ -535,6 +536,13 @@ typedef struct {
   double memory_budget;  /* device bytes admitted requests may hold (default 160e9) */
   int max_active;        /* concurrent requests, 0 = unlimited */
   int use_graphs;        /* capture each Krylov cycle as a CUDA graph (default 1) */
+  int steady_solvers;    /* 0 (default): steady-state requests run unpreconditioned in the
+                            batched engine (the reference's method).  k > 0: k host threads solve
+                            them beside the engine, each request with its own level and drive
+                            preconditioners (population coordinates, the adaptive ladder of
+                            pi_gmres_opts_t.drive_preconditioner; the drive part alone where the
+                            level sweep does not apply), GMRES(krylovdim) in the server's
+                            precision on the plan's stream; maxiter defaults to 2000 there */
 } pi_server_opts_t;
 
 enum { PI_REQUEST_DYNAMICS = 0, PI_REQUEST_STEADY = 1 };

@@ -185,65 +185,85 @@ namespace {
 
 constexpr int kDT = 32;  // tile edge: lane = row, 8 warps x 4 columns
 
+template <typename T>
+struct Cx;
+template <>
+struct Cx<float> {
+  using type = float2;
+};
+template <>
+struct Cx<double> {
+  using type = double2;
+};
+
+// Tables of one arithmetic precision T.
+template <typename T>
 struct DriveDev {
   const int4* tiles;        // (sector, i0, j0, 0)
   const int* n;
   const long long* offset;
   const long long* u_off;
   const long long* h_off;
-  const float* U;
-  const float* h;           // eigenvalues / s
-  const float* c;           // c_s / s
+  const T* U;
+  const T* h;               // eigenvalues / s
+  const T* c;               // c_s / s
 };
 
-__device__ __forceinline__ float2 ld2(const float2* p) { return *p; }
-__device__ __forceinline__ float2 ld2(const double2* p) {
-  const double2 v = *p;
-  return make_float2((float)v.x, (float)v.y);
-}
-__device__ __forceinline__ void st2(float2* p, float2 v) { *p = v; }
-__device__ __forceinline__ void st2(double2* p, float2 v) { *p = make_double2(v.x, v.y); }
+template <typename T2>
+__device__ __forceinline__ T2 cvt2(float2 v);
+template <>
+__device__ __forceinline__ float2 cvt2<float2>(float2 v) { return v; }
+template <>
+__device__ __forceinline__ double2 cvt2<double2>(float2 v) { return make_double2(v.x, v.y); }
+template <typename T2>
+__device__ __forceinline__ T2 cvt2(double2 v);
+template <>
+__device__ __forceinline__ float2 cvt2<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
+template <>
+__device__ __forceinline__ double2 cvt2<double2>(double2 v) { return v; }
 
-// One 32 x 32 tile of a sector product with the real eigenvector matrix U (n x n):
-//   LEFT:  C = op(U) B,  RIGHT: C = B op(U),  op(U) = U^T when TRANS;
+// One 32 x 32 tile of a sector product with the real eigenvector matrix U (n x n), in
+// arithmetic T:  LEFT: C = op(U) B,  RIGHT: C = B op(U),  op(U) = U^T when TRANS;
 // B and C complex n x n column-major at the sector's offset; DIVIDE divides C[i][j] by
 // d_ij = c_s/s - i (h_i - h_j)/s.
-template <bool RIGHT, bool TRANS, bool DIVIDE, typename TI, typename TO>
-__global__ void __launch_bounds__(256) k_drive_mm(DriveDev D, const TI* __restrict__ in, TO* __restrict__ out) {
-  __shared__ float sU[kDT][kDT + 1];
-  __shared__ float2 sB[kDT][kDT + 1];
+template <typename T, bool RIGHT, bool TRANS, bool DIVIDE, typename TI, typename TO>
+__global__ void __launch_bounds__(256) k_drive_mm(DriveDev<T> D, const TI* __restrict__ in, TO* __restrict__ out) {
+  using T2 = typename Cx<T>::type;
+  __shared__ T sU[kDT][kDT + 1];
+  __shared__ T2 sB[kDT][kDT + 1];
   const int4 tl = D.tiles[blockIdx.x];
   const int s = tl.x, i0 = tl.y, j0 = tl.z;
   const int n = D.n[s];
   const long long off = D.offset[s];
-  const float* U = D.U + D.u_off[s];
+  const T* U = D.U + D.u_off[s];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  float2 acc[4];
+  const T2 zero{0, 0};
+  T2 acc[4];
 #pragma unroll
-  for (int c = 0; c < 4; ++c) acc[c] = make_float2(0.f, 0.f);
+  for (int c = 0; c < 4; ++c) acc[c] = zero;
   for (int k0 = 0; k0 < n; k0 += kDT) {
     for (int q = w; q < kDT; q += 8) {
       if (!RIGHT) {
         // sU[kk][ii] = op(U)(i0 + ii, k0 + kk); sB[kk][jj] = B(k0 + kk, j0 + jj)
         if (TRANS) {  // U[k][i]: contiguous in k
           const int k = k0 + lane, i = i0 + q;
-          sU[lane][q] = (k < n && i < n) ? U[k + (long long)i * n] : 0.f;
+          sU[lane][q] = (k < n && i < n) ? U[k + (long long)i * n] : T(0);
         } else {      // U[i][k]: contiguous in i
           const int i = i0 + lane, k = k0 + q;
-          sU[q][lane] = (k < n && i < n) ? U[i + (long long)k * n] : 0.f;
+          sU[q][lane] = (k < n && i < n) ? U[i + (long long)k * n] : T(0);
         }
         const int k = k0 + lane, j = j0 + q;
-        sB[lane][q] = (k < n && j < n) ? ld2(in + off + k + (long long)j * n) : make_float2(0.f, 0.f);
+        sB[lane][q] = (k < n && j < n) ? cvt2<T2>(in[off + k + (long long)j * n]) : zero;
       } else {
         // sB[ii][kk] = B(i0 + ii, k0 + kk); sU[kk][jj] = op(U)(k0 + kk, j0 + jj)
         const int i = i0 + lane, k = k0 + q;
-        sB[lane][q] = (i < n && k < n) ? ld2(in + off + i + (long long)k * n) : make_float2(0.f, 0.f);
+        sB[lane][q] = (i < n && k < n) ? cvt2<T2>(in[off + i + (long long)k * n]) : zero;
         if (TRANS) {  // U[j][k]: contiguous in j
           const int j = j0 + lane, kk = k0 + q;
-          sU[q][lane] = (j < n && kk < n) ? U[j + (long long)kk * n] : 0.f;
+          sU[q][lane] = (j < n && kk < n) ? U[j + (long long)kk * n] : T(0);
         } else {      // U[k][j]: contiguous in k
           const int kk = k0 + lane, j = j0 + q;
-          sU[lane][q] = (j < n && kk < n) ? U[kk + (long long)j * n] : 0.f;
+          sU[lane][q] = (j < n && kk < n) ? U[kk + (long long)j * n] : T(0);
         }
       }
     }
@@ -251,20 +271,20 @@ __global__ void __launch_bounds__(256) k_drive_mm(DriveDev D, const TI* __restri
 #pragma unroll 8
     for (int kk = 0; kk < kDT; ++kk) {
       if (!RIGHT) {
-        const float a = sU[kk][lane];
+        const T a = sU[kk][lane];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          const float2 b = sB[kk][4 * w + c];
-          acc[c].x = fmaf(a, b.x, acc[c].x);
-          acc[c].y = fmaf(a, b.y, acc[c].y);
+          const T2 b = sB[kk][4 * w + c];
+          acc[c].x = fma(a, b.x, acc[c].x);
+          acc[c].y = fma(a, b.y, acc[c].y);
         }
       } else {
-        const float2 b = sB[lane][kk];
+        const T2 b = sB[lane][kk];
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          const float a = sU[kk][4 * w + c];
-          acc[c].x = fmaf(a, b.x, acc[c].x);
-          acc[c].y = fmaf(a, b.y, acc[c].y);
+          const T a = sU[kk][4 * w + c];
+          acc[c].x = fma(a, b.x, acc[c].x);
+          acc[c].y = fma(a, b.y, acc[c].y);
         }
       }
     }
@@ -272,64 +292,73 @@ __global__ void __launch_bounds__(256) k_drive_mm(DriveDev D, const TI* __restri
   }
   const int i = i0 + lane;
   if (i >= n) return;
-  const float* h = D.h + D.h_off[s];
-  const float cs = D.c[s];
-  const float hi = DIVIDE ? h[i] : 0.f;
+  const T* h = D.h + D.h_off[s];
+  const T cs = D.c[s];
+  const T hi = DIVIDE ? h[i] : T(0);
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const int j = j0 + 4 * w + c;
     if (j >= n) break;
-    float2 v = acc[c];
+    T2 v = acc[c];
     if (DIVIDE) {
       // v / (cs - i (h_i - h_j)) = v (cs + i (h_i - h_j)) / (cs^2 + (h_i - h_j)^2)
-      const float dm = hi - h[j];
-      const float inv = 1.f / fmaf(cs, cs, dm * dm);
-      v = make_float2((v.x * cs - v.y * dm) * inv, (v.x * dm + v.y * cs) * inv);
+      const T dm = hi - h[j];
+      const T inv = T(1) / fma(cs, cs, dm * dm);
+      v = T2{(v.x * cs - v.y * dm) * inv, (v.x * dm + v.y * cs) * inv};
     }
-    st2(out + off + i + (long long)j * n, v);
+    out[off + i + (long long)j * n] = cvt2<TO>(v);
   }
 }
 
-// z -= Dv (t^H z) / den, with t^H z read from the device scalar `alpha`.
-template <typename TO>
-__global__ void k_drive_border(TO* __restrict__ z, const float2* __restrict__ dv, const double2* __restrict__ alpha,
+// z -= Dv (t^H z) / den, with t^H z read from the device scalar `alpha`; in z's precision.
+template <typename T2>
+__global__ void k_drive_border(T2* __restrict__ z, const T2* __restrict__ dv, const double2* __restrict__ alpha,
                                double2 inv_den, long long n) {
   const double2 a = *alpha;
   const double gr = a.x * inv_den.x - a.y * inv_den.y, gi = a.x * inv_den.y + a.y * inv_den.x;
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-    const float2 d = dv[e];
-    float2 v = ld2(z + e);
-    v.x -= (float)(d.x * gr - d.y * gi);
-    v.y -= (float)(d.x * gi + d.y * gr);
-    st2(z + e, v);
+    const T2 d = dv[e];
+    T2 v = z[e];
+    v.x -= d.x * gr - d.y * gi;
+    v.y -= d.x * gi + d.y * gr;
+    z[e] = v;
   }
 }
 
-// v = t / |t|^2 on the diagonal entries (FP32), zero elsewhere (the caller zeroes v first).
+// v = t / |t|^2 on the diagonal entries, zero elsewhere (the caller zeroes v first).
+template <typename T2>
 __global__ void k_drive_fill_border(const DevSector* __restrict__ sectors, const int* __restrict__ diag_sector,
-                                    const long long* __restrict__ diag_index, int ndiag, float2* __restrict__ v,
+                                    const long long* __restrict__ diag_index, int ndiag, T2* __restrict__ v,
                                     int coords) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndiag; i += gridDim.x * blockDim.x) {
     const DevSector& sec = sectors[diag_sector[i]];
-    v[diag_index[i]] = make_float2((float)(coords ? sec.border_z : sec.border_x), 0.f);
+    v[diag_index[i]] = cvt2<T2>(make_double2(coords ? sec.border_z : sec.border_x, 0.0));
   }
 }
 
 inline int grid_for(long long n) { return (int)std::max(1LL, std::min((n + 255) / 256, 4LL * 152)); }
+
+// One arithmetic precision's device state: tables, scratch, the border vector D^-1 v.
+template <typename T>
+struct Chain {
+  using T2 = typename Cx<T>::type;
+  DriveDev<T> dev{};
+  T2* t1 = nullptr;
+  T2* t2 = nullptr;
+  T2* dv = nullptr;
+  double2 inv_den{1.0, 0.0};
+};
 
 }  // namespace
 
 struct DriveState {
   pi_plan* plan = nullptr;
   DriveHost host;
-  DriveDev dev{};
   int ntiles = 0;
   long long dim = 0;
-  float2* t1 = nullptr;
-  float2* t2 = nullptr;
-  float2* dv = nullptr;
+  Chain<float> c32;    // FP32 vectors: FP32 arithmetic
+  Chain<double> c64;   // FP64 vectors: FP64 arithmetic
   double2* alpha = nullptr;
-  double2 inv_den{1.0, 0.0};
   std::vector<void*> allocs;
   size_t bytes = 0;
   double setup_seconds = 0.0;
@@ -356,15 +385,75 @@ cudaError_t upload(DriveState* D, const std::vector<X>& v, const X** out) {
   return e;
 }
 
-// out = D_blockdiag^-1 in (no border), FP32 arithmetic
-template <typename TI, typename TO>
-cudaError_t block_solve(DriveState* D, const TI* in, TO* out, cudaStream_t st) {
+// out = D_blockdiag^-1 in (no border), in the chain's arithmetic
+template <typename T, typename TI, typename TO>
+cudaError_t block_solve(DriveState* D, Chain<T>& C, const TI* in, TO* out, cudaStream_t st) {
+  using T2 = typename Cx<T>::type;
   const int g = D->ntiles;
-  k_drive_mm<false, true, false, TI, float2><<<g, 256, 0, st>>>(D->dev, in, D->t1);        // U^T R
-  k_drive_mm<true, false, true, float2, float2><<<g, 256, 0, st>>>(D->dev, D->t1, D->t2);  // (.) U ./ d
-  k_drive_mm<false, false, false, float2, float2><<<g, 256, 0, st>>>(D->dev, D->t2, D->t1);  // U (.)
-  k_drive_mm<true, true, false, float2, TO><<<g, 256, 0, st>>>(D->dev, D->t1, out);          // (.) U^T
+  k_drive_mm<T, false, true, false, TI, T2><<<g, 256, 0, st>>>(C.dev, in, C.t1);     // U^T R
+  k_drive_mm<T, true, false, true, T2, T2><<<g, 256, 0, st>>>(C.dev, C.t1, C.t2);    // (.) U ./ d
+  k_drive_mm<T, false, false, false, T2, T2><<<g, 256, 0, st>>>(C.dev, C.t2, C.t1);  // U (.)
+  k_drive_mm<T, true, true, false, T2, TO><<<g, 256, 0, st>>>(C.dev, C.t1, out);     // (.) U^T
   return cudaGetLastError();
+}
+
+// Uploads one precision's tables and scratch, forms D^-1 v and 1 / (1 + t^H D^-1 v).
+template <typename T>
+int setup_chain(DriveState* D, Chain<T>& C, const std::vector<int4>& tiles, const int* nn, const long long* of,
+                const long long* uo, const long long* ho, int coords, std::string* err) {
+  using T2 = typename Cx<T>::type;
+  const DriveHost& H = D->host;
+  const int S = (int)H.n.size();
+  std::vector<T> Ut(H.U.begin(), H.U.end()), ht(H.h.size()), ct(S);
+  for (size_t i = 0; i < H.h.size(); ++i) ht[i] = (T)(H.h[i] / H.scale);
+  for (int s = 0; s < S; ++s) ct[s] = (T)(H.c[s] / H.scale);
+  cudaError_t e = cudaSuccess;
+  const int4* tl = nullptr;
+  const T *Ud = nullptr, *hd = nullptr, *cd_ = nullptr;
+  if (e == cudaSuccess) e = upload(D, tiles, &tl);
+  if (e == cudaSuccess) e = upload(D, Ut, &Ud);
+  if (e == cudaSuccess) e = upload(D, ht, &hd);
+  if (e == cudaSuccess) e = upload(D, ct, &cd_);
+  C.dev = DriveDev<T>{tl, nn, of, uo, ho, Ud, hd, cd_};
+  void* p = nullptr;
+  const size_t vb = sizeof(T2) * (size_t)D->dim;
+  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) C.t1 = (T2*)p;
+  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) C.t2 = (T2*)p;
+  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) C.dv = (T2*)p;
+  cudaStream_t st = D->plan->stream;
+  const DevicePlan& dp = D->plan->dev;
+  // the border vector v, a temporary of the setup
+  T2* v = nullptr;
+  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) v = (T2*)p;
+  if (e == cudaSuccess) e = cudaMemsetAsync(v, 0, vb, st);
+  if (e == cudaSuccess && dp.ndiag > 0) {
+    k_drive_fill_border<T2><<<grid_for(dp.ndiag), 256, 0, st>>>(dp.sectors, dp.diag_sector, dp.diag_index, dp.ndiag,
+                                                                v, coords);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = block_solve<T, T2, T2>(D, C, v, C.dv, st);
+  if (e == cudaSuccess) e = trace_dot(dp, C.dv, sizeof(T) == sizeof(float) ? 1 : 0, coords, D->alpha, st);
+  double2 tdv{0.0, 0.0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&tdv, D->alpha, sizeof(double2), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) {
+    // the border vector's buffer is not needed after setup
+    D->allocs.erase(std::find(D->allocs.begin(), D->allocs.end(), (void*)v));
+    D->bytes -= std::max<size_t>(vb, 16);
+    e = cudaFree(v);
+  }
+  if (e != cudaSuccess) {
+    *err = std::string("drive preconditioner setup: ") + cudaGetErrorString(e);
+    return PI_ERR_CUDA;
+  }
+  const std::complex<double> den(1.0 + tdv.x, tdv.y);
+  if (!(std::abs(den) > 1e-12) || !std::isfinite(std::abs(den))) {
+    *err = "the drive preconditioner's trace border is singular";
+    return PI_ERR_NOT_CONVERGED;
+  }
+  const std::complex<double> inv = 1.0 / den;
+  C.inv_den = make_double2(inv.real(), inv.imag());
+  return PI_OK;
 }
 
 }  // namespace
@@ -389,78 +478,43 @@ int drive_create(pi_plan* plan, int coords, double scale, DriveState** out, std:
       for (int b = 0; b < nt; ++b) tiles.push_back(make_int4(s, a * kDT, b * kDT, 0));
   }
   D->ntiles = (int)tiles.size();
-  std::vector<float> Uf(H.U.begin(), H.U.end()), hf(H.h.size()), cf(S);
-  for (size_t i = 0; i < H.h.size(); ++i) hf[i] = (float)(H.h[i] / scale);
-  for (int s = 0; s < S; ++s) cf[s] = (float)(H.c[s] / scale);
   cudaError_t e = cudaSuccess;
-  const int4* tl = nullptr;
   const int* nn = nullptr;
   const long long *of = nullptr, *uo = nullptr, *ho = nullptr;
-  const float *Ud = nullptr, *hd = nullptr, *cd_ = nullptr;
-  if (e == cudaSuccess) e = upload(D, tiles, &tl);
+  void* p = nullptr;
   if (e == cudaSuccess) e = upload(D, H.n, &nn);
   if (e == cudaSuccess) e = upload(D, H.offset, &of);
   if (e == cudaSuccess) e = upload(D, H.u_off, &uo);
   if (e == cudaSuccess) e = upload(D, H.h_off, &ho);
-  if (e == cudaSuccess) e = upload(D, Uf, &Ud);
-  if (e == cudaSuccess) e = upload(D, hf, &hd);
-  if (e == cudaSuccess) e = upload(D, cf, &cd_);
-  D->dev = DriveDev{tl, nn, of, uo, ho, Ud, hd, cd_};
-  void* p = nullptr;
-  const size_t vb = sizeof(float2) * (size_t)D->dim;
-  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) D->t1 = (float2*)p;
-  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) D->t2 = (float2*)p;
-  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) D->dv = (float2*)p;
   if (e == cudaSuccess && (e = dalloc(D, sizeof(double2) * 2, &p)) == cudaSuccess) D->alpha = (double2*)p;
-  float2* v = nullptr;
-  if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) v = (float2*)p;
-  cudaStream_t st = plan->stream;
-  const DevicePlan& dp = plan->dev;
-  if (e == cudaSuccess) e = cudaMemsetAsync(v, 0, vb, st);
-  if (e == cudaSuccess && dp.ndiag > 0) {
-    k_drive_fill_border<<<grid_for(dp.ndiag), 256, 0, st>>>(dp.sectors, dp.diag_sector, dp.diag_index, dp.ndiag, v,
-                                                           coords);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = block_solve<float2, float2>(D, v, D->dv, st);
-  if (e == cudaSuccess) e = trace_dot(dp, D->dv, 1, coords, D->alpha, st);
-  double2 tdv{0.0, 0.0};
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&tdv, D->alpha, sizeof(double2), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     drive_free(D);
-    *err = std::string("drive preconditioner setup: ") + cudaGetErrorString(e);
+    *err = std::string("drive preconditioner upload: ") + cudaGetErrorString(e);
     return PI_ERR_CUDA;
   }
-  const std::complex<double> den(1.0 + tdv.x, tdv.y);
-  if (!(std::abs(den) > 1e-12) || !std::isfinite(std::abs(den))) {
+  rc = setup_chain<float>(D, D->c32, tiles, nn, of, uo, ho, coords, err);
+  if (!rc) rc = setup_chain<double>(D, D->c64, tiles, nn, of, uo, ho, coords, err);
+  if (rc) {
     drive_free(D);
-    *err = "the drive preconditioner's trace border is singular";
-    return PI_ERR_NOT_CONVERGED;
+    return rc;
   }
-  const std::complex<double> inv = 1.0 / den;
-  D->inv_den = make_double2(inv.real(), inv.imag());
   D->setup_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   *out = D;
   return PI_OK;
 }
 
 cudaError_t drive_apply(DriveState* D, const void* r, int r_f32, void* z, int z_f32, cudaStream_t st) {
-  cudaError_t e;
-  if (r_f32 && z_f32)
-    e = block_solve<float2, float2>(D, (const float2*)r, (float2*)z, st);
-  else if (!r_f32 && !z_f32)
-    e = block_solve<double2, double2>(D, (const double2*)r, (double2*)z, st);
-  else
-    return cudaErrorInvalidValue;
+  if (r_f32 != z_f32) return cudaErrorInvalidValue;
+  cudaError_t e = r_f32 ? block_solve<float, float2, float2>(D, D->c32, (const float2*)r, (float2*)z, st)
+                        : block_solve<double, double2, double2>(D, D->c64, (const double2*)r, (double2*)z, st);
   if (e != cudaSuccess) return e;
-  const DevicePlan& dp = D->plan->dev;
-  e = trace_dot(dp, z, z_f32, D->host.coords, D->alpha, st);
+  e = trace_dot(D->plan->dev, z, z_f32, D->host.coords, D->alpha, st);
   if (e != cudaSuccess) return e;
   if (z_f32)
-    k_drive_border<float2><<<grid_for(D->dim), 256, 0, st>>>((float2*)z, D->dv, D->alpha, D->inv_den, D->dim);
+    k_drive_border<float2><<<grid_for(D->dim), 256, 0, st>>>((float2*)z, D->c32.dv, D->alpha, D->c32.inv_den, D->dim);
   else
-    k_drive_border<double2><<<grid_for(D->dim), 256, 0, st>>>((double2*)z, D->dv, D->alpha, D->inv_den, D->dim);
+    k_drive_border<double2><<<grid_for(D->dim), 256, 0, st>>>((double2*)z, D->c64.dv, D->alpha, D->c64.inv_den,
+                                                              D->dim);
   return cudaGetLastError();
 }
 

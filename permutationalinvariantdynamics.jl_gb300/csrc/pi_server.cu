@@ -5,7 +5,10 @@
 // while their device footprint fits the memory budget (and the active-request cap), folds
 // them into the next tick's batched launches, and retires finished requests (their state
 // written back, their workspaces freed, a completion posted with timestamps).  States and
-// Krylov bases of active requests stay resident in HBM for their whole life.
+// Krylov bases of active requests stay resident in HBM for their whole life.  With
+// steady_solvers > 0 the worker hands admitted steady-state requests to a pool of solver
+// threads instead, which run preconditioned single-instance solves on the plans' own streams
+// beside the engine; their footprint stays charged to the budget until they complete.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -19,6 +22,8 @@
 #include <vector>
 
 #include "pi_batch.hpp"
+#include "pi_handle.hpp"
+#include "pi_precond.hpp"
 
 using Clock = std::chrono::steady_clock;
 
@@ -71,6 +76,10 @@ struct pi_server {
   std::string fail_msg;
   pi_server_stats_t stats{};
   std::thread worker;
+  // preconditioned steady-state solver pool (steady_solvers > 0)
+  std::deque<Active> steady_queue;
+  std::condition_variable steady_wake;
+  std::vector<std::thread> solvers;
 
   double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
   size_t footprint(const pi_request_t& r) const {
@@ -80,6 +89,9 @@ struct pi_server {
     if (r.kind == PI_REQUEST_DYNAMICS) {
       b += 2 * sizeof(double2) * (size_t)dim;
       if (opts.precision == PI_FP32) b += sizeof(double2) * (size_t)dim * r.nobs;
+    } else if (opts.steady_solvers > 0) {
+      // GMRES basis (m + 1) and its FP64 vectors, the preconditioner tables and scratch
+      b = es * (size_t)dim * (opts.krylovdim + 1) + 24 * sizeof(double2) * (size_t)dim;
     } else {
       b += 3 * sizeof(double2) * (size_t)dim;
     }
@@ -109,15 +121,79 @@ struct pi_server {
       }
     }
     std::snprintf(c.message, sizeof(c.message), "%s", msg.c_str());
+    finish_post(c, a.footprint);
+  }
+  void finish_post(const pi_completion_t& c, size_t fp) {
     std::lock_guard<std::mutex> lk(mu);
     done.push_back(c);
     stats.completed += 1;
     stats.active -= 1;
-    stats.bytes_in_use -= (double)a.footprint;
+    stats.bytes_in_use -= (double)fp;
     completed.notify_all();
+    wake.notify_all();  // freed budget may admit queued requests
   }
   void run();
+  void solve_steady();
 };
+
+// One solver thread: preconditioned single-instance steady states of admitted requests.
+void pi_server::solve_steady() {
+  cudaSetDevice(device);
+  for (;;) {
+    Active a;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      steady_wake.wait(lk, [&] { return stop || !steady_queue.empty(); });
+      if (stop) return;
+      a = std::move(steady_queue.front());
+      steady_queue.pop_front();
+    }
+    const pi_request_t& r = a.req;
+    a.start_time = now();
+    pi_precond* lev = nullptr;
+    pi_precond* drv = nullptr;
+    int rc = pi_precond_create(r.plan, PI_COORDS_POPULATION, 0.0, 0.0, &lev);
+    if (rc) lev = nullptr;  // e.g. decay and pump channels together: the drive part alone
+    rc = pi_precond_create_drive(r.plan, PI_COORDS_POPULATION, lev ? precond_scale(lev) : 0.0, &drv);
+    pi_gmres_info_t info;
+    std::memset(&info, 0, sizeof(info));
+    std::string msg;
+    if (rc == PI_OK) {
+      pi_gmres_opts_t o;
+      pi_gmres_default_opts(&o);
+      o.krylovdim = opts.krylovdim;
+      o.precision = opts.precision;
+      o.maxiter = r.maxiter > 0 ? r.maxiter : 2000;
+      if (r.atol > 0) o.atol = r.atol;
+      if (r.rtol > 0) o.rtol = r.rtol;
+      o.coords = PI_COORDS_POPULATION;
+      o.preconditioner = lev ? lev : drv;
+      o.drive_preconditioner = lev ? drv : nullptr;
+      rc = pi_steady_state(r.plan, r.state_dev, &o, &info);
+    }
+    if (rc != PI_OK) {
+      char buf[512];
+      pi_last_error(buf, sizeof(buf));
+      msg = buf;
+    }
+    if (lev) pi_precond_destroy(lev);
+    if (drv) pi_precond_destroy(drv);
+    pi_completion_t c;
+    std::memset(&c, 0, sizeof(c));
+    c.tag = r.tag;
+    c.kind = r.kind;
+    c.status = rc;
+    c.submit_time = a.submit_time;
+    c.start_time = a.start_time;
+    c.finish_time = now();
+    c.iterations = info.iterations;
+    c.operator_applications = info.operator_applications;
+    c.residual = info.normalized_residual;
+    c.trace_error = info.trace_error;
+    std::snprintf(c.message, sizeof(c.message), "%s", msg.c_str());
+    finish_post(c, a.footprint);
+  }
+}
 
 void pi_server::run() {
   cudaSetDevice(device);
@@ -149,6 +225,12 @@ void pi_server::run() {
       a.submit_time = p.submit_time;
       a.start_time = now();
       const pi_request_t& r = p.req;
+      if (r.kind == PI_REQUEST_STEADY && opts.steady_solvers > 0) {
+        std::lock_guard<std::mutex> lk(mu);
+        steady_queue.push_back(std::move(a));
+        steady_wake.notify_one();
+        continue;
+      }
       if (r.kind == PI_REQUEST_DYNAMICS) {
         pi_expv_opts_t o;
         pi_expv_default_opts(&o);
@@ -219,6 +301,7 @@ void pi_server_default_opts(pi_server_opts_t* o) {
   o->memory_budget = 160e9;
   o->max_active = 0;
   o->use_graphs = 1;
+  o->steady_solvers = 0;
 }
 
 int pi_server_create(const pi_server_opts_t* opts, int device, pi_server** out) {
@@ -228,6 +311,8 @@ int pi_server_create(const pi_server_opts_t* opts, int device, pi_server** out) 
   if (opts->precision != PI_FP64 && opts->precision != PI_FP32)
     return fail(PI_ERR_INVALID_ARGUMENT, "precision must be PI_FP64 or PI_FP32");
   if (!(opts->memory_budget > 0)) return fail(PI_ERR_INVALID_ARGUMENT, "memory_budget must be positive");
+  if (opts->steady_solvers < 0 || opts->steady_solvers > 64)
+    return fail(PI_ERR_INVALID_ARGUMENT, "steady_solvers must lie in 0:64");
   std::unique_ptr<pi_server> S(new pi_server());
   S->opts = *opts;
   S->device = device;
@@ -236,6 +321,7 @@ int pi_server_create(const pi_server_opts_t* opts, int device, pi_server** out) 
   if (S->engine->err != cudaSuccess) return cuda_fail(S->engine->err, "serving engine");
   pi_server* raw = S.get();
   S->worker = std::thread([raw] { raw->run(); });
+  for (int i = 0; i < opts->steady_solvers; ++i) S->solvers.emplace_back([raw] { raw->solve_steady(); });
   *out = S.release();
   return PI_OK;
 }
@@ -302,8 +388,17 @@ int pi_server_destroy(pi_server* S) {
     std::lock_guard<std::mutex> lk(S->mu);
     S->stop = true;
     S->wake.notify_all();
+    S->steady_wake.notify_all();
   }
   if (S->worker.joinable()) S->worker.join();
+  for (auto& t : S->solvers)
+    if (t.joinable()) t.join();
+  // requests handed to the pool but not started
+  while (!S->steady_queue.empty()) {
+    Active a = std::move(S->steady_queue.front());
+    S->steady_queue.pop_front();
+    S->post(a, PI_ERR_BUSY, "server stopped before the request finished");
+  }
   delete S;
   return PI_OK;
 }

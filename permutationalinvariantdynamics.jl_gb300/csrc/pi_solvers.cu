@@ -332,6 +332,11 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
     std::fill(g.begin(), g.end(), cd(0, 0));
     R.chk(scale_f64(P ? pz : r, V, n, make_double2(1.0 / beta, 0.0), 0, R.s));
     g[0] = beta;
+    // With a preconditioner the recomputed |P r| after a restart differs from the cycle's
+    // estimate |g| by the preconditioner's rounding (FP32 parts, combined stages); a cycle that
+    // stops exactly at tol can then restart just above it, cycle after cycle.  Preconditioned
+    // cycles target tol / 2, as the mixed-precision inner solves do.
+    const double ctol = P ? 0.5 * tol : tol;
     int kdone = 0;
     const int steps = std::min(m, maxiter - res.iterations);
     for (int j = 0; j < steps && R.ok(); ++j) {
@@ -364,7 +369,7 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
       g[j + 1] = -std::conj(sg) * g1 + c * g2;
       ++res.iterations;
       kdone = j + 1;
-      if (std::abs(g[j + 1]) <= tol) break;
+      if (std::abs(g[j + 1]) <= ctol) break;
     }
     if (!R.ok()) break;
     upper_triangular_solve(H, g, kdone, y);

@@ -145,7 +145,7 @@ class pi_dynamics_job_t(C.Structure):
 
 class pi_server_opts_t(C.Structure):
     _fields_ = [("krylovdim", C.c_int), ("precision", C.c_int), ("memory_budget", C.c_double),
-                ("max_active", C.c_int), ("use_graphs", C.c_int)]
+                ("max_active", C.c_int), ("use_graphs", C.c_int), ("steady_solvers", C.c_int)]
 
 
 PI_REQUEST_DYNAMICS = 0

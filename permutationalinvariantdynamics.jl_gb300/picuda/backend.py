@@ -1232,7 +1232,7 @@ class DrivePreconditioner(LevelPreconditioner):
     """The drive part of the trace-fixed steady-state operator (pi_precond_create_drive): per
     Schur sector A X + X A^H with A = -i H_s - qbar_s I (the sector's Hamiltonian block and its
     mean loss), solved exactly in the orthogonal eigenbasis of H_s, plus the trace border by
-    Sherman-Morrison; FP32 arithmetic.  It carries the drive (Jx, Jy), which the level sweep
+    Sherman-Morrison, in the precision of the vectors it maps.  It carries the drive (Jx, Jy), which the level sweep
     leaves out, and leaves out the loss variation along a sector and the gains, which the level
     sweep carries.  As the GMRES preconditioner it is applied twice per step; beside a level
     preconditioner (GMRESAlgorithm(preconditioner=level, drive_preconditioner=drive)) the solve

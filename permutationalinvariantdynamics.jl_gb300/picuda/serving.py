@@ -44,10 +44,15 @@ class Completion:
 
 
 class Server:
-    """Serving engine: precision 'fp64' or 'mixed', memory_budget in bytes of HBM."""
+    """Serving engine: precision 'fp64' or 'mixed', memory_budget in bytes of HBM.
+    steady_solvers = k > 0 solves steady-state requests on k host threads beside the batched
+    engine, each preconditioned (level sweep and drive part, adaptive); 0 keeps them in the
+    engine, unpreconditioned."""
 
     def __init__(self, krylovdim=30, precision="fp64", memory_budget=160e9, max_active=0,
-                 use_graphs=True, device=0):
+                 use_graphs=True, device=0, steady_solvers=0):
+        if isinstance(steady_solvers, bool) or int(steady_solvers) < 0:
+            raise _lib.PiArgumentError("steady_solvers must be a nonnegative integer")
         if precision not in ("fp64", "mixed"):
             raise _lib.PiArgumentError("precision must be 'fp64' or 'mixed'")
         self._torch = _torch()
@@ -59,6 +64,7 @@ class Server:
         o.memory_budget = float(memory_budget)
         o.max_active = int(max_active)
         o.use_graphs = 1 if use_graphs else 0
+        o.steady_solvers = int(steady_solvers)
         h = C.c_void_p()
         _lib.check(self._lib.pi_server_create(C.byref(o), device, C.byref(h)), "pi_server_create")
         self._h = h

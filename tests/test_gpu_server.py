@@ -110,3 +110,47 @@ def test_server_mixed_close_to_fp64(torch_cuda):
     for k in res["fp64"]:
         ref = res["fp64"][k]
         assert np.abs(res["mixed"][k] - ref).max() <= 2e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_server_preconditioned_steady_requests(torch_cuda, precision):
+    """steady_solvers > 0: steady requests are solved beside the engine, preconditioned by the
+    level sweep and the drive part (adaptive), while dynamics requests share the engine.  A
+    strongly driven N = 40 request, which the unpreconditioned method does not bring to
+    tolerance, converges; every steady state equals a direct preconditioned solve of the same
+    model and stays the same alone and in the mix."""
+    from oracle import pi_oracle as O
+    std = [M.scan_model(40, 1.7, 0.06, 0.02), M.btc_c3(24, 1.0), M.driven_c1(8)]
+    dyn = [M.scan_model(14, 1.1, 0.2, 0.05), M.ensemble_c2(16)]
+    comp = [picuda.compile(m) for m in std]
+    with picuda.Server(precision=precision, steady_solvers=2) as srv:
+        tags = {}
+        for i, m in enumerate(dyn):
+            tags[srv.submit_dynamics(m, _excited(m), 0.5, 0.05, observables={"exc": EXC})] = ("d", i)
+        for i, c in enumerate(comp):
+            tags[srv.submit_steady(c)] = ("s", i)
+        done = srv.drain()
+    with picuda.Server(precision=precision, steady_solvers=1) as srv:
+        alone = srv.submit_steady(comp[0])
+        (a,) = srv.drain()
+        assert a.tag == alone and a.ok, a.message
+    assert len(done) == len(tags)
+    for c in done:
+        kind, i = tags[c.tag]
+        assert c.ok, c.message
+        if kind != "s":
+            continue
+        lev = picuda.level_preconditioner(comp[i], coords="population")
+        drv = picuda.drive_preconditioner(comp[i], coords="population", operator_scale=lev.operator_scale)
+        alg = picuda.GMRESAlgorithm(krylovdim=30, maxiter=2000, precision=precision, preconditioner=lev,
+                                    drive_preconditioner=drv)
+        ref = picuda.stationary_state(comp[i], algorithm=alg)
+        assert np.array_equal(c.state, ref.data), i
+        if i == 0:
+            assert np.array_equal(c.state, a.state)
+        plan = O.Plan(M.to_oracle(std[i]))
+        t = np.zeros(len(plan), dtype=np.complex128)
+        t[plan.trace_idx] = plan.trace_val
+        s = O.estimated_operator_scale(lambda z: O.apply(plan, z), len(plan))
+        assert np.linalg.norm(O.apply(plan, c.state)) / s <= 1e-8 * max(np.linalg.norm(c.state), 1.0)
+        assert abs(np.vdot(t, c.state) - 1) <= 1e-8
