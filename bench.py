@@ -404,6 +404,47 @@ def steady_rates(picuda, torch, count=16, seed=7, family="driven"):
     return out
 
 
+def drive_steady(picuda, torch, N=100, omega=1.5, gdown=0.1, gphi=0.05, repeats=3):
+    """A strongly driven steady state (H = Omega Jx, local decay, local dephasing, collective
+    decay 1/N; Omega well above the dissipation), where the reference's unpreconditioned
+    GMRES and the level sweep stall: GMRES(30) in population coordinates with the level
+    sweep and the drive part (adaptive ladder), FP64 against mixed precision, atol 1e-10,
+    rtol 1e-8.  Preconditioners are built before the clock (their setup time is reported);
+    each solve is timed alone."""
+    m = scan_model(picuda, N, omega, gdown, gphi)
+    c = picuda.compile(m)
+    t0 = time.perf_counter()
+    lev = picuda.level_preconditioner(c, coords="population")
+    t1 = time.perf_counter()
+    drv = picuda.drive_preconditioner(c, coords="population", operator_scale=lev.operator_scale)
+    t2 = time.perf_counter()
+    out = {"N": N, "dim": len(m.basis), "omega": omega, "gamma_down": gdown, "gamma_phi": gphi,
+           "krylovdim": 30, "level_setup_s": t1 - t0, "drive_setup_s": t2 - t1,
+           "drive_device_bytes": drv.info["device_bytes"]}
+    states = {}
+    for prec in ("fp64", "mixed"):
+        alg = picuda.GMRESAlgorithm(krylovdim=30, maxiter=3000, precision=prec, preconditioner=lev,
+                                    drive_preconditioner=drv)
+        times, info = [], None
+        for _ in range(repeats):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = picuda.stationary_state(c, algorithm=alg, return_info=True)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+            info = res.info
+        states[prec] = res.state.data
+        out[prec] = {"seconds_median": float(np.median(times)), "converged": bool(info["converged"]),
+                     "iterations": info["iterations"], "restarts": info["restarts"],
+                     "stage": info["preconditioner_stage"], "normalized_residual": info["normalized_residual"],
+                     "trace_error": info["trace_error"], "operator_applications": info["operator_applications"]}
+    sq = np.concatenate([np.full(n * n, f) for n, f in zip(c.basis.dims, c.sector_scales())])
+    out["mixed_state_rel_dev_vs_fp64_population"] = float(
+        np.abs(sq * (states["mixed"] - states["fp64"])).max() / np.abs(sq * states["fp64"]).max())
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds_median"] / out["mixed"]["seconds_median"]
+    return out
+
+
 def btc_model(picuda, N, omega_over_kappa):
     """Boundary-time-crystal-like steady-state configuration: H = Omega Jx with
     Omega = omega_over_kappa * kappa, collective decay kappa = 1/N on J-, local dephasing 0.01,
@@ -780,6 +821,8 @@ def main():
     ap.add_argument("--c3-no-plain", action="store_true",
                     help="skip the unpreconditioned reference-method attempt (profiling runs)")
     ap.add_argument("--steady-requests", type=int, default=16)
+    ap.add_argument("--only-drive-steady", type=int, default=None, metavar="N",
+                    help="one strongly driven steady state of N qubits with the drive preconditioner")
     ap.add_argument("--only-rk4", default=None, choices=["fp64", "mixed"],
                     help="one short RK4 solve of the large time-evolution model (a profiling target)")
     ap.add_argument("--only-expv", default=None, choices=["fp64", "mixed"],
@@ -806,6 +849,10 @@ def main():
         precs = ("fp64", "mixed") if args.scan_precision == "both" else (args.scan_precision,)
         print(json.dumps({"only_scan": True, "scan": scan_rates(picuda, torch, args.scan_instances,
                                                                   args.scan_intervals, precisions=precs)}))
+        return 0
+    if args.only_drive_steady:
+        print(json.dumps({"only_drive_steady": True,
+                          "drive_steady": drive_steady(picuda, torch, N=args.only_drive_steady)}))
         return 0
     if args.only_steady:
         print(json.dumps({"only_steady": True, "steady": steady_rates(picuda, torch, args.steady_requests),
@@ -957,6 +1004,7 @@ def main():
     steady_served = (steady_rates(picuda, torch, args.steady_requests, family="served")
                      if rank == 0 else None)
     steady_c3 = steady_c3_rates(picuda, torch, repeats=args.c3_repeats) if rank == 0 else None
+    drive = drive_steady(picuda, torch, N=100, repeats=2) if rank == 0 else None
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -1007,6 +1055,7 @@ def main():
             "steady": steady,
             "steady_served_family": steady_served,
             "steady_c3": steady_c3,
+            "drive_steady": drive,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": cl,
