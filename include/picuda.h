@@ -354,8 +354,9 @@ typedef struct {
                              `preconditioner` a PI_PRECOND_DRIVE one of the same plan, coordinates
                              and scale: the solve starts with the level sweep and moves, after a
                              restart cycle that reduced the raw residual by less than 3x, to the
-                             drive part applied twice, and after another such cycle to drive,
-                             level and drive in turn (regime-adaptive; no reference counterpart) */
+                             drive part applied twice, and after a cycle of that stage that
+                             gained less than 1.25x to drive, level and drive in turn
+                             (regime-adaptive; no reference counterpart) */
 } pi_gmres_opts_t;
 
 typedef struct {
@@ -541,8 +542,8 @@ typedef struct {
                             them beside the engine, each request with its own level and drive
                             preconditioners (population coordinates, the adaptive ladder of
                             pi_gmres_opts_t.drive_preconditioner; the drive part alone where the
-                            level sweep does not apply), GMRES(krylovdim) in the server's
-                            precision on the plan's stream; maxiter defaults to 2000 there */
+                            level sweep does not apply), GMRES(max(krylovdim, 50)) in the
+                            server's precision on the plan's stream; maxiter defaults to 2000 */
 } pi_server_opts_t;
 
 enum { PI_REQUEST_DYNAMICS = 0, PI_REQUEST_STEADY = 1 };

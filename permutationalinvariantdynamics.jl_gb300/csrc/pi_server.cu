@@ -90,8 +90,8 @@ struct pi_server {
       b += 2 * sizeof(double2) * (size_t)dim;
       if (opts.precision == PI_FP32) b += sizeof(double2) * (size_t)dim * r.nobs;
     } else if (opts.steady_solvers > 0) {
-      // GMRES basis (m + 1) and its FP64 vectors, the preconditioner tables and scratch
-      b = es * (size_t)dim * (opts.krylovdim + 1) + 24 * sizeof(double2) * (size_t)dim;
+      // GMRES(max(m, 50)) basis and its FP64 vectors, the preconditioner tables and scratch
+      b = es * (size_t)dim * (std::max(opts.krylovdim, 50) + 1) + 24 * sizeof(double2) * (size_t)dim;
     } else {
       b += 3 * sizeof(double2) * (size_t)dim;
     }
@@ -161,7 +161,7 @@ void pi_server::solve_steady() {
     if (rc == PI_OK) {
       pi_gmres_opts_t o;
       pi_gmres_default_opts(&o);
-      o.krylovdim = opts.krylovdim;
+      o.krylovdim = std::max(opts.krylovdim, 50);  // GMRES(50), the steady-state restart length
       o.precision = opts.precision;
       o.maxiter = r.maxiter > 0 ? r.maxiter : 2000;
       if (r.atol > 0) o.atol = r.atol;

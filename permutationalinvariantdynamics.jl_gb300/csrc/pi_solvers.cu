@@ -241,6 +241,13 @@ void upper_triangular_solve(const std::vector<std::vector<cd>>& H, const std::ve
   }
 }
 
+// Raw-residual reduction per restart cycle below which the preconditioner ladder moves on:
+// the level sweep gives way to the drive part after a cycle that gained less than 3x; the
+// drive part (which converges steadily where the drive dominates) gives way to drive, level
+// and drive only when it nearly stagnates (less than 1.25x), where the loss is as strong as
+// the drive.
+inline double ladder_factor(int stage) { return stage == 0 ? 3.0 : 1.25; }
+
 struct GmresResult {
   bool converged = false;
   int iterations = 0, restarts = 0;
@@ -382,9 +389,9 @@ GmresResult gmres_f64(Run& R, double2* x, const double2* b, int m, double atol, 
       res.converged = true;
       return res;
     }
-    if (ladder && stage < 2 && rawbeta > prev_raw / 3.0) {
-      // the cycle reduced the raw residual by less than 3x: the next preconditioner stage,
-      // with the preconditioned tests rescaled to it
+    if (ladder && stage < 2 && rawbeta > prev_raw / ladder_factor(stage)) {
+      // the cycle made too little progress: the next preconditioner stage, with the
+      // preconditioned tests rescaled to it
       ++stage;
       *stage_out = stage;
       prec(b, pz);
@@ -459,9 +466,9 @@ GmresResult gmres_mixed(Run& R, double2* x, const double2* b, int m, double atol
     R.apply_bordered(x, w64, invscale, alpha);
     R.chk((k_sub<<<grid_n(n), 256, 0, R.s>>>(b, w64, r, n), cudaGetLastError()));
     const double rawbeta = R.norm(r);
-    if (ladder && stage < 2 && prev_raw > 0 && rawbeta > prev_raw / 3.0) {
-      // the last refinement cycle reduced the raw residual by less than 3x: the next
-      // preconditioner stage, with the preconditioned tests rescaled to it
+    if (ladder && stage < 2 && prev_raw > 0 && rawbeta > prev_raw / ladder_factor(stage)) {
+      // the last refinement cycle made too little progress: the next preconditioner stage,
+      // with the preconditioned tests rescaled to it
       ++stage;
       *stage_out = stage;
       prec(b, pz, 0);

@@ -142,7 +142,7 @@ def test_server_preconditioned_steady_requests(torch_cuda, precision):
             continue
         lev = picuda.level_preconditioner(comp[i], coords="population")
         drv = picuda.drive_preconditioner(comp[i], coords="population", operator_scale=lev.operator_scale)
-        alg = picuda.GMRESAlgorithm(krylovdim=30, maxiter=2000, precision=precision, preconditioner=lev,
+        alg = picuda.GMRESAlgorithm(krylovdim=50, maxiter=2000, precision=precision, preconditioner=lev,
                                     drive_preconditioner=drv)
         ref = picuda.stationary_state(comp[i], algorithm=alg)
         assert np.array_equal(c.state, ref.data), i
