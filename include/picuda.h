@@ -282,15 +282,15 @@ typedef struct {
 enum { PI_PRECOND_LEVEL = 0, PI_PRECOND_DRIVE = 1 };
 int pi_precond_create(pi_plan* plan, int coords, double regularization, double operator_scale,
                       pi_precond** out);
-/* Drive preconditioner (PI_PRECOND_DRIVE): per Schur sector the normal part of the
- * within-sector operator, A X + X A^H with A = -i H_s - qbar_s I (H_s the sector's Hamiltonian
- * block, real symmetric tridiagonal; qbar_s its mean loss), solved exactly in the orthogonal
- * eigenbasis of H_s (X = U [(U^T R U) ./ d] U^T, d_ij = (-i (h_i - h_j) - 2 qbar_s) / s), with
- * the trace border v t^H by Sherman-Morrison; FP64 vectors in FP64 arithmetic (the plain
- * FP64 solve), FP32 vectors in FP32 (the mixed solve's inner steps).  It
- * carries the drive exactly and leaves out the loss variation along a sector, the sandwich
- * gains and the coupling between sectors, which the level sweep (pi_precond_create) carries
- * exactly and the drive part leaves out.  As opts.preconditioner GMRES applies it twice per
+/* Drive preconditioner (PI_PRECOND_DRIVE): per Schur sector the commutator with H_s (the
+ * sector's Hamiltonian block, real symmetric tridiagonal) and the diagonal, in H_s's
+ * orthogonal eigenbasis, of the loss anticommutator, solved exactly there
+ * (X = U [(U^T R U) ./ d] U^T, d_ij = (-i (h_i - h_j) - (q_i + q_j) / 2) / s, q_i the loss
+ * eigenmode i sees, floored at half the sector's mean loss), with the trace border v t^H by
+ * Sherman-Morrison; FP64 vectors in FP64 arithmetic (the plain FP64 solve), FP32 vectors in
+ * FP32 (the mixed solve's inner steps).  It carries the drive exactly and leaves out the loss
+ * coupling between eigenmodes, the sandwich gains and the coupling between sectors, which
+ * the level sweep (pi_precond_create) carries exactly where the drive does not dominate.  As opts.preconditioner GMRES applies it twice per
  * step (z = D r; z += D (r - B z), B the bordered operator).  The host eigendecompositions run
  * on the host threads.  The reference's preconditioner for the same system is the dense LU of
  * every sector block of L/s + v t^H (krylov.jl:594-699), infeasible beyond N ~ 40. */
@@ -329,12 +329,13 @@ int pi_precond_export(int N, int d, int nsectors, const int* sector_ks, int nter
                       double regularization, double operator_scale, long long* counts,
                       pi_precond_tables_t* tables);
 /* Host-only inspection of the drive preconditioner's tables for the same model arguments:
- * counts[0..2] = sectors, sum n_s^2, sum n_s; with U, h, c non-NULL also the eigenvector pool
- * (sector by sector, n_s x n_s column-major, column i the eigenvector of h[i]), the eigenvalue
- * pool and c_s = -2 x the mean loss of every sector (all unscaled). */
+ * counts[0..2] = sectors, sum n_s^2, sum n_s; with U, h, c, q non-NULL also the eigenvector
+ * pool (sector by sector, n_s x n_s column-major, column i the eigenvector of h[i]), the
+ * eigenvalue pool, c_s = -2 x the mean loss of every sector and, per eigenmode, the loss it
+ * sees (U^T Q U)_ii floored at -c_s / 4 (all unscaled). */
 int pi_precond_drive_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
                             const double* ops, const double* rates, const double* hbar, long long* counts,
-                            double* U, double* h, double* c);
+                            double* U, double* h, double* c, double* q);
 
 typedef struct {
   int krylovdim;          /* GMRES restart length m (default 30) */

@@ -460,7 +460,7 @@ int pi_stencil_export_adjoint(int N, int d, int nsectors, const int* sector_ks, 
 
 int pi_precond_drive_export(int N, int d, int nsectors, const int* sector_ks, int nterms, const int* term_kind,
                             const double* ops, const double* rates, const double* hbar, long long* counts,
-                            double* U, double* h, double* c) {
+                            double* U, double* h, double* c, double* q) {
   if (!counts) return fail(PI_ERR_INVALID_ARGUMENT, "null counts");
   QubitPlan hp;
   int rc = build_host_plan(N, d, nsectors, sector_ks, nterms, term_kind, ops, rates, hbar, &hp);
@@ -475,6 +475,7 @@ int pi_precond_drive_export(int N, int d, int nsectors, const int* sector_ks, in
   if (U) std::copy(D.U.begin(), D.U.end(), U);
   if (h) std::copy(D.h.begin(), D.h.end(), h);
   if (c) std::copy(D.c.begin(), D.c.end(), c);
+  if (q) std::copy(D.q.begin(), D.q.end(), q);
   return PI_OK;
 }
 

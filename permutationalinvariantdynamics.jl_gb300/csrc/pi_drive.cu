@@ -103,8 +103,9 @@ int build_drive_precond(const QubitPlan& hp, int coords, double scale, DriveHost
   }
   D.U.assign(uo, 0.0);
   D.h.assign(ho, 0.0);
+  D.q.assign(ho, 0.0);
   // per sector: the Hamiltonian block from the own-sector stencil terms
-  std::vector<std::vector<double>> diag(S), off(S);
+  std::vector<std::vector<double>> diag(S), off(S), loss(S);
   for (int s = 0; s < S; ++s) {
     const int n = D.n[s];
     std::vector<cd> al(n, 0.0), be(n, 0.0);
@@ -135,11 +136,13 @@ int build_drive_precond(const QubitPlan& hp, int coords, double scale, DriveHost
     }
     diag[s].resize(n);
     off[s].assign(n, 0.0);
+    loss[s].resize(n);
     double mre = 0.0;
     for (int a = 0; a < n; ++a) {
       // -i h_a in alpha and +i h_b in beta, up to a constant split that cancels in h_i - h_j
       diag[s][a] = 0.5 * (-al[a].imag() + be[a].imag());
       mre += al[a].real() + be[a].real();
+      loss[s][a] = -(al[a].real() + be[a].real());  // q_a: the split's constant cancels at a = b
     }
     for (int a = 0; a + 1 < n; ++a) {
       off[s][a] = 0.5 * (up[a] + dn[a + 1]);
@@ -161,8 +164,16 @@ int build_drive_precond(const QubitPlan& hp, int coords, double scale, DriveHost
       const int n = D.n[s];
       d = diag[s];
       e = off[s];
+      const double* U = D.U.data() + D.u_off[s];
       if (!tridiag_eigen(n, d.data(), e.data(), D.U.data() + D.u_off[s])) failed.store(s);
       std::copy(d.begin(), d.end(), D.h.begin() + D.h_off[s]);
+      // the loss each eigenmode sees, (U^T Q U)_ii, floored at half the mean loss -c_s / 2
+      const double floor_q = -0.25 * D.c[s];
+      for (int i = 0; i < n; ++i) {
+        double qi = 0.0;
+        for (int a = 0; a < n; ++a) qi += U[a + (size_t)i * n] * U[a + (size_t)i * n] * loss[s][a];
+        D.q[D.h_off[s] + i] = std::max(qi, floor_q);
+      }
     }
   };
   const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -206,15 +217,13 @@ struct DriveDev {
   const long long* h_off;
   const T* U;
   const T* h;               // eigenvalues / s
-  const T* c;               // c_s / s
+  const T* q;               // per eigenmode: its loss / s
 };
 
 template <typename T2>
 __device__ __forceinline__ T2 cvt2(float2 v);
 template <>
 __device__ __forceinline__ float2 cvt2<float2>(float2 v) { return v; }
-template <>
-__device__ __forceinline__ double2 cvt2<double2>(float2 v) { return make_double2(v.x, v.y); }
 template <typename T2>
 __device__ __forceinline__ T2 cvt2(double2 v);
 template <>
@@ -225,7 +234,7 @@ __device__ __forceinline__ double2 cvt2<double2>(double2 v) { return v; }
 // One 32 x 32 tile of a sector product with the real eigenvector matrix U (n x n), in
 // arithmetic T:  LEFT: C = op(U) B,  RIGHT: C = B op(U),  op(U) = U^T when TRANS;
 // B and C complex n x n column-major at the sector's offset; DIVIDE divides C[i][j] by
-// d_ij = c_s/s - i (h_i - h_j)/s.
+// d_ij = -(q_i + q_j)/(2 s) - i (h_i - h_j)/s.
 template <typename T, bool RIGHT, bool TRANS, bool DIVIDE, typename TI, typename TO>
 __global__ void __launch_bounds__(256) k_drive_mm(DriveDev<T> D, const TI* __restrict__ in, TO* __restrict__ out) {
   using T2 = typename Cx<T>::type;
@@ -293,18 +302,20 @@ __global__ void __launch_bounds__(256) k_drive_mm(DriveDev<T> D, const TI* __res
   const int i = i0 + lane;
   if (i >= n) return;
   const T* h = D.h + D.h_off[s];
-  const T cs = D.c[s];
+  const T* q = D.q + D.h_off[s];
   const T hi = DIVIDE ? h[i] : T(0);
+  const T qi = DIVIDE ? q[i] : T(0);
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     const int j = j0 + 4 * w + c;
     if (j >= n) break;
     T2 v = acc[c];
     if (DIVIDE) {
-      // v / (cs - i (h_i - h_j)) = v (cs + i (h_i - h_j)) / (cs^2 + (h_i - h_j)^2)
+      // v / (dr - i dm) = v (dr + i dm) / (dr^2 + dm^2), dr = -(q_i + q_j)/2, dm = h_i - h_j
       const T dm = hi - h[j];
-      const T inv = T(1) / fma(cs, cs, dm * dm);
-      v = T2{(v.x * cs - v.y * dm) * inv, (v.x * dm + v.y * cs) * inv};
+      const T dr = T(-0.5) * (qi + q[j]);
+      const T inv = T(1) / fma(dr, dr, dm * dm);
+      v = T2{(v.x * dr - v.y * dm) * inv, (v.x * dm + v.y * dr) * inv};
     }
     out[off + i + (long long)j * n] = cvt2<TO>(v);
   }
@@ -403,17 +414,16 @@ int setup_chain(DriveState* D, Chain<T>& C, const std::vector<int4>& tiles, cons
                 const long long* uo, const long long* ho, int coords, std::string* err) {
   using T2 = typename Cx<T>::type;
   const DriveHost& H = D->host;
-  const int S = (int)H.n.size();
-  std::vector<T> Ut(H.U.begin(), H.U.end()), ht(H.h.size()), ct(S);
+  std::vector<T> Ut(H.U.begin(), H.U.end()), ht(H.h.size()), qt(H.q.size());
   for (size_t i = 0; i < H.h.size(); ++i) ht[i] = (T)(H.h[i] / H.scale);
-  for (int s = 0; s < S; ++s) ct[s] = (T)(H.c[s] / H.scale);
+  for (size_t i = 0; i < H.q.size(); ++i) qt[i] = (T)(H.q[i] / H.scale);
   cudaError_t e = cudaSuccess;
   const int4* tl = nullptr;
   const T *Ud = nullptr, *hd = nullptr, *cd_ = nullptr;
   if (e == cudaSuccess) e = upload(D, tiles, &tl);
   if (e == cudaSuccess) e = upload(D, Ut, &Ud);
   if (e == cudaSuccess) e = upload(D, ht, &hd);
-  if (e == cudaSuccess) e = upload(D, ct, &cd_);
+  if (e == cudaSuccess) e = upload(D, qt, &cd_);
   C.dev = DriveDev<T>{tl, nn, of, uo, ho, Ud, hd, cd_};
   void* p = nullptr;
   const size_t vb = sizeof(T2) * (size_t)D->dim;

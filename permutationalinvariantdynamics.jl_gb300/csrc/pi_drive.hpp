@@ -1,11 +1,12 @@
 // Drive preconditioner of the trace-fixed steady-state GMRES (pi_drive.cu).
 //
 // Per Schur sector s the within-sector operator holds the Hamiltonian commutator -i[H_s, X],
-// the loss anticommutator -(Q_s X + X Q_s)/2 and the sector's own sandwich gains.  Its normal
-// part A X + X A^H with A = -i H_s - qbar_s I (H_s the sector's real symmetric tridiagonal
-// Hamiltonian block, qbar_s the sector's mean loss) is solved exactly through H_s's orthogonal
-// eigenvectors U_s (H_s = U_s diag(h) U_s^T):
-//   X = U_s [ (U_s^T R U_s) ./ d ] U_s^T,   d_ij = (-i (h_i - h_j) + c_s) / s,  c_s = -2 qbar_s,
+// the loss anticommutator -(Q_s X + X Q_s)/2 and the sector's own sandwich gains.  In the
+// orthogonal eigenbasis U_s of H_s (the sector's real symmetric tridiagonal Hamiltonian
+// block, H_s = U_s diag(h) U_s^T) the commutator is diagonal and the loss is kept as its
+// diagonal part, the loss q_i = (U_s^T Q_s U_s)_ii each eigenmode sees (floored at half the
+// sector's mean loss); that operator is solved exactly:
+//   X = U_s [ (U_s^T R U_s) ./ d ] U_s^T,   d_ij = (-i (h_i - h_j) - (q_i + q_j) / 2) / s,
 // and the trace border v t^H of the bordered operator L/s + v t^H is added by Sherman-Morrison
 // over the whole block-diagonal map.  The loss variation along a sector, the sandwich gains and
 // the coupling between sectors are left out: this part carries the drive exactly, which is what
@@ -34,6 +35,7 @@ struct DriveHost {
   std::vector<long long> h_off;   // per sector: offset of its eigenvalues
   std::vector<double> c;          // per sector: c_s = -2 x mean loss (before the 1/s scaling)
   std::vector<double> U, h;       // pools
+  std::vector<double> q;          // per eigenmode (pool like h): the loss it sees, floored
   double max_asymmetry = 0.0;     // largest |H_ab - H_ba| of the lowered Hamiltonian blocks
   double max_nonhermitian = 0.0;  // largest real part of a row-shift +-1 coefficient (left out)
 };

@@ -210,7 +210,7 @@ PROTOTYPES = {
     "pi_steady_state": (C.c_int, [_P, _P, C.POINTER(pi_gmres_opts_t), C.POINTER(pi_gmres_info_t)]),
     "pi_precond_create": (C.c_int, [_P, C.c_int, C.c_double, C.c_double, C.POINTER(_P)]),
     "pi_precond_create_drive": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(_P)]),
-    "pi_precond_drive_export": (C.c_int, [C.c_int, C.c_int, C.c_int, _I, C.c_int, _I, _D, _D, _D, _LL, _D, _D, _D]),
+    "pi_precond_drive_export": (C.c_int, [C.c_int, C.c_int, C.c_int, _I, C.c_int, _I, _D, _D, _D, _LL, _D, _D, _D, _D]),
     "pi_precond_destroy": (C.c_int, [_P]),
     "pi_precond_info": (C.c_int, [_P, C.POINTER(pi_precond_info_t)]),
     "pi_precond_apply": (C.c_int, [_P, _P, _P, _P]),

@@ -1230,8 +1230,8 @@ def level_preconditioner(compiled, coords="population", regularization=0.0, oper
 
 class DrivePreconditioner(LevelPreconditioner):
     """The drive part of the trace-fixed steady-state operator (pi_precond_create_drive): per
-    Schur sector A X + X A^H with A = -i H_s - qbar_s I (the sector's Hamiltonian block and its
-    mean loss), solved exactly in the orthogonal eigenbasis of H_s, plus the trace border by
+    Schur sector the commutator with the sector's Hamiltonian block H_s and the loss each of its
+    eigenmodes sees, solved exactly in the orthogonal eigenbasis of H_s, plus the trace border by
     Sherman-Morrison, in the precision of the vectors it maps.  It carries the drive (Jx, Jy), which the level sweep
     leaves out, and leaves out the loss variation along a sector and the gains, which the level
     sweep carries.  As the GMRES preconditioner it is applied twice per step; beside a level
@@ -1264,20 +1264,21 @@ def drive_preconditioner(compiled, coords="population", operator_scale=None):
 def drive_preconditioner_tables(model):
     """Host-only export of the drive preconditioner's eigen tables (pi_precond_drive_export)
     for a PIModel: per sector the eigenvector matrix U (n x n, column i for h[i]), the
-    eigenvalues h of the sector Hamiltonian block and c = -2 x the sector's mean loss."""
+    eigenvalues h of the sector Hamiltonian block, c = -2 x the sector's mean loss and q, the
+    loss each eigenmode sees (floored at -c / 4)."""
     lib = _lib.load()
     kinds, ops, rates, hbar, ks = _term_arrays(model)
     counts = np.zeros(3, dtype=np.int64)
     args = (model.basis.N, model.basis.d, len(ks), _lib.iptr(ks), len(model.terms), _lib.iptr(kinds),
             _lib.dptr(ops), _lib.dptr(rates), _lib.dptr(hbar), _lib.llptr(counts))
-    _lib.check(lib.pi_precond_drive_export(*args, None, None, None), "pi_precond_drive_export")
+    _lib.check(lib.pi_precond_drive_export(*args, None, None, None, None), "pi_precond_drive_export")
     S, nu, nh = (int(v) for v in counts)
-    U, h, c = np.zeros(nu), np.zeros(nh), np.zeros(S)
-    _lib.check(lib.pi_precond_drive_export(*args, _lib.dptr(U), _lib.dptr(h), _lib.dptr(c)),
+    U, h, c, q = np.zeros(nu), np.zeros(nh), np.zeros(S), np.zeros(nh)
+    _lib.check(lib.pi_precond_drive_export(*args, _lib.dptr(U), _lib.dptr(h), _lib.dptr(c), _lib.dptr(q)),
                "pi_precond_drive_export")
     out, uo, ho = [], 0, 0
     for n in model.basis.dims:
-        out.append(dict(U=U[uo:uo + n * n].reshape((n, n), order="F"), h=h[ho:ho + n]))
+        out.append(dict(U=U[uo:uo + n * n].reshape((n, n), order="F"), h=h[ho:ho + n], q=q[ho:ho + n]))
         uo += n * n
         ho += n
     for d, cs in zip(out, c):

@@ -1,10 +1,11 @@
 """The drive preconditioner's host construction (pi_precond_drive_export, no GPU).
 
 Per Schur sector the library takes the Hamiltonian block H_s from its own lowered stencil
-(row-shift terms and the diagonal of the centre term) and the mean loss from the centre
+(row-shift terms and the diagonal of the centre term) and the loss diagonal from the centre
 term's real part, and diagonalises H_s with its own tridiagonal QL.  The tables must match
 the oracle's sector blocks: U orthonormal with H_s U = U diag(h) (h up to the constant that
-the lowering's split of the diagonal leaves open), c_s = -2 x the mean of the loss diagonal.
+the lowering's split of the diagonal leaves open), c_s = -2 x the mean of the loss diagonal,
+and q_i = (U^T Q_s U)_ii floored at -c_s / 4.
 A numpy restatement of the preconditioner built from the tables must make GMRES(50) converge
 on a strongly driven model where the unpreconditioned method stalls."""
 import numpy as np
@@ -51,6 +52,9 @@ def test_tables_diagonalise_the_sector_hamiltonians(name):
         assert np.abs(Q - np.diag(np.diag(Q))).max() <= 1e-13 * max(np.abs(Q).max(), 1.0)
         want = -2.0 * float(np.mean(np.diag(Q).real))
         assert t["c"] == pytest.approx(min(want, -1e-6), rel=1e-12, abs=1e-14)
+        # the loss each eigenmode sees, (U^T Q U)_ii, floored at half the mean loss
+        qmode = np.einsum("ai,a,ai->i", U, np.diag(Q).real, U)
+        assert np.abs(t["q"] - np.maximum(qmode, -0.25 * t["c"])).max() <= 1e-12 * max(np.abs(Q).max(), 1.0)
 
 
 def test_tridiagonal_ql_on_a_large_collective_block():
@@ -76,8 +80,8 @@ def _normal_part(model, tables, s_op):
         z = np.empty_like(r)
         for sec, tab in enumerate(tables):
             o, m = b.offsets[sec], b.dims[sec]
-            U, h = tab["U"], tab["h"]
-            d = (tab["c"] - 1j * (h[:, None] - h[None, :])) / s_op
+            U, h, q = tab["U"], tab["h"], tab["q"]
+            d = (-0.5 * (q[:, None] + q[None, :]) - 1j * (h[:, None] - h[None, :])) / s_op
             R = r[o:o + m * m].reshape((m, m), order="F")
             z[o:o + m * m] = (U @ ((U.T @ R @ U) / d) @ U.T).reshape(-1, order="F")
         return z

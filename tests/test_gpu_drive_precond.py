@@ -43,13 +43,16 @@ def test_apply_matches_numpy_restatement(torch_cuda):
     rng = np.random.default_rng(5)
     r = rng.standard_normal(len(b)) + 1j * rng.standard_normal(len(b))
 
+    def dmat(tab):
+        h, q = tab["h"], tab["q"]
+        return (-0.5 * (q[:, None] + q[None, :]) - 1j * (h[:, None] - h[None, :])) / 17.0
+
     def D(x):
         z = np.empty_like(x)
         for sec, tab in enumerate(tables):
             o, m = b.offsets[sec], b.dims[sec]
-            d = (tab["c"] - 1j * (tab["h"][:, None] - tab["h"][None, :])) / 17.0
             R = x[o:o + m * m].reshape((m, m), order="F")
-            z[o:o + m * m] = (tab["U"] @ ((tab["U"].T @ R @ tab["U"]) / d) @ tab["U"].T).reshape(-1, order="F")
+            z[o:o + m * m] = (tab["U"] @ ((tab["U"].T @ R @ tab["U"]) / dmat(tab)) @ tab["U"].T).reshape(-1, order="F")
         return z
 
     Dv = D(v)
@@ -59,15 +62,13 @@ def test_apply_matches_numpy_restatement(torch_cuda):
     P.apply(z, torch.from_numpy(r).cuda())
     got = z.cpu().numpy()
     assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max()
-    # M z = r: the preconditioner inverts its own operator
+    # M z = r: the preconditioner inverts its own operator, U [(U^T X U) * d] U^T + v t^H X
     Bz = np.empty_like(got)
     for sec, tab in enumerate(tables):
         o, m = b.offsets[sec], b.dims[sec]
-        U, h = tab["U"], tab["h"]
-        Hs = U @ np.diag(h) @ U.T
-        A = -1j * Hs + 0.5 * tab["c"] * np.eye(m)
+        U = tab["U"]
         X = got[o:o + m * m].reshape((m, m), order="F")
-        Bz[o:o + m * m] = ((A @ X + X @ A.conj().T) / 17.0).reshape(-1, order="F")
+        Bz[o:o + m * m] = (U @ ((U.T @ X @ U) * dmat(tab)) @ U.T).reshape(-1, order="F")
     Bz = Bz + v * np.vdot(t, got)
     assert np.abs(Bz - r).max() <= 1e-10 * np.abs(r).max()
 
