@@ -542,9 +542,10 @@ typedef struct {
                             batched engine (the reference's method).  k > 0: k host threads solve
                             them beside the engine, each request with its own level and drive
                             preconditioners (population coordinates, the adaptive ladder of
-                            pi_gmres_opts_t.drive_preconditioner; the drive part alone where the
-                            level sweep does not apply), GMRES(max(krylovdim, 50)) in the
-                            server's precision on the plan's stream; maxiter defaults to 2000 */
+                            pi_gmres_opts_t.drive_preconditioner; unpreconditioned, the
+                            reference's method, where the level sweep does not apply),
+                            GMRES(max(krylovdim, 50)) in the server's precision on the plan's
+                            stream; maxiter defaults to 2000 */
 } pi_server_opts_t;
 
 enum { PI_REQUEST_DYNAMICS = 0, PI_REQUEST_STEADY = 1 };

@@ -152,9 +152,12 @@ void pi_server::solve_steady() {
     a.start_time = now();
     pi_precond* lev = nullptr;
     pi_precond* drv = nullptr;
+    // Where the level sweep does not apply (decay and pump channels together: its gains
+    // would point both ways) the request is solved with the reference's unpreconditioned
+    // method; the drive part alone is no preconditioner for such dissipation-dominated models.
     int rc = pi_precond_create(r.plan, PI_COORDS_POPULATION, 0.0, 0.0, &lev);
-    if (rc) lev = nullptr;  // e.g. decay and pump channels together: the drive part alone
-    rc = pi_precond_create_drive(r.plan, PI_COORDS_POPULATION, lev ? precond_scale(lev) : 0.0, &drv);
+    if (rc) lev = nullptr;
+    rc = lev ? pi_precond_create_drive(r.plan, PI_COORDS_POPULATION, precond_scale(lev), &drv) : PI_OK;
     pi_gmres_info_t info;
     std::memset(&info, 0, sizeof(info));
     std::string msg;
@@ -166,9 +169,9 @@ void pi_server::solve_steady() {
       o.maxiter = r.maxiter > 0 ? r.maxiter : 2000;
       if (r.atol > 0) o.atol = r.atol;
       if (r.rtol > 0) o.rtol = r.rtol;
-      o.coords = PI_COORDS_POPULATION;
-      o.preconditioner = lev ? lev : drv;
-      o.drive_preconditioner = lev ? drv : nullptr;
+      o.coords = lev ? PI_COORDS_POPULATION : PI_COORDS_REFERENCE;
+      o.preconditioner = lev;
+      o.drive_preconditioner = drv;
       rc = pi_steady_state(r.plan, r.state_dev, &o, &info);
     }
     if (rc != PI_OK) {

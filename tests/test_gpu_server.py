@@ -154,3 +154,19 @@ def test_server_preconditioned_steady_requests(torch_cuda, precision):
         s = O.estimated_operator_scale(lambda z: O.apply(plan, z), len(plan))
         assert np.linalg.norm(O.apply(plan, c.state)) / s <= 1e-8 * max(np.linalg.norm(c.state), 1.0)
         assert abs(np.vdot(t, c.state) - 1) <= 1e-8
+
+
+def test_server_steady_pool_falls_back_to_the_reference_method(torch_cuda):
+    """A model with decay and pump channels together has no level sweep (its charge-keeping
+    gains point both ways) and no drive: the pool solves it unpreconditioned, the reference's
+    method, bitwise as a direct GMRES(50) solve does."""
+    model = picuda.Models.local_pump_decay(8, down=1.0, up=0.3)
+    c = picuda.compile(model)
+    with pytest.raises(picuda.PiError):
+        picuda.level_preconditioner(c, coords="population")
+    with picuda.Server(precision="fp64", steady_solvers=1) as srv:
+        srv.submit_steady(c)
+        (done,) = srv.drain()
+    assert done.ok, done.message
+    ref = picuda.stationary_state(c, algorithm=picuda.GMRESAlgorithm(krylovdim=50, maxiter=2000))
+    assert np.array_equal(done.state, ref.data)
