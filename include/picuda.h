@@ -287,9 +287,8 @@ int pi_precond_create(pi_plan* plan, int coords, double regularization, double o
  * orthogonal eigenbasis, of the loss anticommutator, solved exactly there
  * (X = U [(U^T R U) ./ d] U^T, d_ij = (-i (h_i - h_j) - (q_i + q_j) / 2) / s, q_i the loss
  * eigenmode i sees, floored at half the sector's mean loss), with the trace border v t^H by
- * Sherman-Morrison; FP64 vectors in FP64 arithmetic (the plain FP64 solve), FP32 vectors (the
- * mixed solve's inner steps) in FP32, or in FP64 for plans with blocks above 128 (N > 127),
- * where FP32 products left the mixed solves short of accuracy.  It carries the drive exactly and leaves out the loss
+ * Sherman-Morrison; FP64 vectors in FP64 arithmetic (the plain FP64 solve), FP32 vectors in
+ * FP32 (the mixed solve's inner steps).  It carries the drive exactly and leaves out the loss
  * coupling between eigenmodes, the sandwich gains and the coupling between sectors, which
  * the level sweep (pi_precond_create) carries exactly where the drive does not dominate.  As opts.preconditioner GMRES applies it twice per
  * step (z = D r; z += D (r - B z), B the bordered operator).  The host eigendecompositions run

@@ -349,15 +349,6 @@ __global__ void k_drive_fill_border(const DevSector* __restrict__ sectors, const
 
 inline int grid_for(long long n) { return (int)std::max(1LL, std::min((n + 255) / 256, 4LL * 152)); }
 
-__global__ void k_drive_widen(const float2* __restrict__ a, double2* __restrict__ b, long long n) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
-    b[e] = make_double2(a[e].x, a[e].y);
-}
-__global__ void k_drive_narrow(const double2* __restrict__ a, float2* __restrict__ b, long long n) {
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
-    b[e] = make_float2((float)a[e].x, (float)a[e].y);
-}
-
 // One arithmetic precision's device state: tables, scratch, the border vector D^-1 v.
 template <typename T>
 struct Chain {
@@ -371,23 +362,13 @@ struct Chain {
 
 }  // namespace
 
-// Largest sector at which FP32 vectors are mapped in FP32 arithmetic.  Beyond it the FP32
-// eigenvector products (about 1e-6 relative at n = 150-290) left the mixed solves' inner steps
-// short of the accuracy they need: on the served stream's steady requests the mixed solves
-// stalled near 1e-3 at N >= 149, and mapping their FP32 vectors through the FP64 chain
-// converged 54 of 58 against 49 (the FP64 solves: 55).
-constexpr int kDriveF32MaxBlock = 128;
-
 struct DriveState {
   pi_plan* plan = nullptr;
   DriveHost host;
   int ntiles = 0;
   long long dim = 0;
-  Chain<float> c32;    // FP32 vectors of plans with blocks <= kDriveF32MaxBlock: FP32 arithmetic
-  Chain<double> c64;   // FP64 vectors, and FP32 vectors of larger plans: FP64 arithmetic
-  bool f32_via_f64 = false;
-  double2* wide_in = nullptr;   // FP64 copies of an FP32 vector's input and output (large plans)
-  double2* wide_out = nullptr;
+  Chain<float> c32;    // FP32 vectors: FP32 arithmetic
+  Chain<double> c64;   // FP64 vectors: FP64 arithmetic
   double2* alpha = nullptr;
   std::vector<void*> allocs;
   size_t bytes = 0;
@@ -521,18 +502,8 @@ int drive_create(pi_plan* plan, int coords, double scale, DriveState** out, std:
     *err = std::string("drive preconditioner upload: ") + cudaGetErrorString(e);
     return PI_ERR_CUDA;
   }
-  D->f32_via_f64 = *std::max_element(H.n.begin(), H.n.end()) > kDriveF32MaxBlock;
-  rc = D->f32_via_f64 ? PI_OK : setup_chain<float>(D, D->c32, tiles, nn, of, uo, ho, coords, err);
+  rc = setup_chain<float>(D, D->c32, tiles, nn, of, uo, ho, coords, err);
   if (!rc) rc = setup_chain<double>(D, D->c64, tiles, nn, of, uo, ho, coords, err);
-  if (!rc && D->f32_via_f64) {
-    const size_t vb = sizeof(double2) * (size_t)D->dim;
-    if ((e = dalloc(D, vb, &p)) == cudaSuccess) D->wide_in = (double2*)p;
-    if (e == cudaSuccess && (e = dalloc(D, vb, &p)) == cudaSuccess) D->wide_out = (double2*)p;
-    if (e != cudaSuccess) {
-      *err = std::string("drive preconditioner scratch: ") + cudaGetErrorString(e);
-      rc = PI_ERR_CUDA;
-    }
-  }
   if (rc) {
     drive_free(D);
     return rc;
@@ -544,17 +515,6 @@ int drive_create(pi_plan* plan, int coords, double scale, DriveState** out, std:
 
 cudaError_t drive_apply(DriveState* D, const void* r, int r_f32, void* z, int z_f32, cudaStream_t st) {
   if (r_f32 != z_f32) return cudaErrorInvalidValue;
-  if (r_f32 && D->f32_via_f64) {
-    // a large plan: the FP32 vector goes through the FP64 chain and comes back rounded
-    k_drive_widen<<<grid_for(D->dim), 256, 0, st>>>((const float2*)r, D->wide_in, D->dim);
-    cudaError_t e = block_solve<double, double2, double2>(D, D->c64, D->wide_in, D->wide_out, st);
-    if (e == cudaSuccess) e = trace_dot(D->plan->dev, D->wide_out, 0, D->host.coords, D->alpha, st);
-    if (e != cudaSuccess) return e;
-    k_drive_border<double2><<<grid_for(D->dim), 256, 0, st>>>(D->wide_out, D->c64.dv, D->alpha, D->c64.inv_den,
-                                                              D->dim);
-    k_drive_narrow<<<grid_for(D->dim), 256, 0, st>>>(D->wide_out, (float2*)z, D->dim);
-    return cudaGetLastError();
-  }
   cudaError_t e = r_f32 ? block_solve<float, float2, float2>(D, D->c32, (const float2*)r, (float2*)z, st)
                         : block_solve<double, double2, double2>(D, D->c64, (const double2*)r, (double2*)z, st);
   if (e != cudaSuccess) return e;

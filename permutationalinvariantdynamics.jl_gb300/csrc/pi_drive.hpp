@@ -53,8 +53,8 @@ int build_drive_precond(const QubitPlan& hp, int coords, double scale, DriveHost
 
 struct DriveState;
 int drive_create(pi_plan* plan, int coords, double scale, DriveState** out, std::string* err);
-// z = M^-1 r (one application), on `stream`; r and z both FP64 (FP64 arithmetic) or both
-// FP32 (FP32 arithmetic, or FP64 for plans with blocks above 128).  Uses the state's scratch:
+// z = M^-1 r for M = blockdiag(A_s X + X A_s^H)/s + v t^H (one application), on `stream`; r
+// and z both FP64 (FP64 arithmetic) or both FP32 (FP32 arithmetic).  Uses the state's scratch:
 // one application at a time per state (the solves of a plan are serialised by the plan).
 cudaError_t drive_apply(DriveState* D, const void* r, int r_f32, void* z, int z_f32, cudaStream_t stream);
 void drive_free(DriveState* D);
